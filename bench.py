@@ -1,0 +1,412 @@
+#!/usr/bin/env python
+"""Benchmark of the Schwarz smoother hot path (SchwarzPreconditioner::vmult) on GB300.
+
+Workload (the configuration the headline metric is quoted on): 3D Poisson, SIPG DG Q4 on the
+unit cube with 64^3 Cartesian cells (32,768,000 DoFs), additive vertex-patch Schwarz smoother
+(250,047 patches of 10^3 DoFs, 8 tiled colors), FP32 gather / fast-diagonalization / scatter
+into FP64 vectors, relaxation 0.15.  One step = one vmult.  Inputs: f ~ U[-1,1] per DoF from
+numpy's Philox generator (seed 0), synthetic -- there is no dataset in this domain.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Under torchrun (N > 1) every rank runs an independent replica on its own GPU (the smoother
+does not shard on one level; value = DoFs of all ranks / max time).  The reference arm times
+the CPU oracle port (the reference itself needs deal.II, absent here) with all host threads.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import shutil
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "smoother DoF/s (SchwarzPreconditioner::vmult; CG+MG solve s to 1e-8 rel. residual and FP32 vs FP64 in 'solve')"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--dim", type=int, default=3)
+    ap.add_argument("--degree", type=int, default=4)
+    ap.add_argument("--cells", type=int, default=64)
+    ap.add_argument("--precision", choices=["fp32", "fp64"], default="fp32")
+    ap.add_argument("--omega", type=float, default=0.15)
+    ap.add_argument("--no-solve", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--seed", type=int, default=0)
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def workload(args):
+    n, k, dim = args.cells, args.degree, args.dim
+    N = n ** dim * (k + 1) ** dim
+    P = (n - 1) ** dim
+    nl = 2 * (k + 1)
+    flops_per_patch = 4 * dim * nl ** (dim + 1) + 2 * nl ** dim
+    return dict(N=N, P=P, n1d=nl, flops_per_patch=flops_per_patch,
+                flops=P * flops_per_patch, bytes=N * 16)
+
+
+def philox_src(N, seed):
+    import numpy as np
+    return np.random.Generator(np.random.Philox(seed)).uniform(-1.0, 1.0, N)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 100 ms (recipe's clocks line)."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+        self.t0 = self.t1 = None
+
+    def start(self):
+        if not shutil.which("nvidia-smi"):
+            return
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        self.proc = subprocess.Popen(
+            ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu=timestamp,{self.FIELDS}",
+             "--format=csv,noheader,nounits", "-lms", "100"],
+            stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        time.sleep(0.3)
+
+    def mark(self, which):
+        setattr(self, which, time.time())
+
+    def stop(self):
+        if not self.proc:
+            return None
+        time.sleep(0.15)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 10:
+                continue
+            try:
+                rows.append(dict(sm=float(parts[2]), smax=float(parts[3]), active=parts[5],
+                                 hw=parts[6], hwt=parts[7], swt=parts[8], pcap=parts[9]))
+            except ValueError:
+                continue
+        os.unlink(self.path)
+        if not rows:
+            return None
+        # samples taken while the timed loop ran (the last ones if it was shorter than 100 ms)
+        n_timed = max(1, min(len(rows), int((self.t1 - self.t0) / 0.1) + 2)) if self.t0 else len(rows)
+        sel = rows[-(n_timed + 1):-1] if len(rows) > n_timed else rows
+        reasons = set()
+        for r in sel:
+            for key, name in (("hw", "hw_slowdown"), ("hwt", "hw_thermal_slowdown"),
+                              ("swt", "sw_thermal_slowdown"), ("pcap", "sw_power_cap")):
+                if r[key].lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(r["sm"] for r in sel), "sm_max_mhz": max(r["smax"] for r in sel),
+                "reasons": sorted(reasons), "samples": len(sel)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic(dim, k):
+    """DRAM bytes per launch of the FD color kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", f"fd_color_kernel_{dim}d_k{k}.txt")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        m = re.match(r"\s*dram_bytes_per_launch_full_size:\s*([0-9.eE+]+)", line)
+        if m:
+            return float(m.group(1))
+    return None
+
+
+def cpu_baseline(args, W):
+    """Oracle port (plain C, OpenMP over patches of a color, FP64) on all host threads: a
+    full vmult of the same workload, repeated, ~a few seconds."""
+    from oracle import oracle as O
+    O.build()
+    import numpy as np
+    threads = O.num_threads()
+    n = args.cells
+    h = O.SchwarzHandle(args.dim, args.degree, (n,) * args.dim, patch_variant=1, omega=args.omega)
+    src = philox_src(W["N"], args.seed)
+    dst = np.zeros_like(src)
+    h.apply(dst, src)  # warm-up (page-in)
+    reps, t0 = 0, time.perf_counter()
+    while True:
+        h.apply(dst, src)
+        reps += 1
+        el = time.perf_counter() - t0
+        if el > 8.0 or reps >= 5:
+            break
+    h.close()
+    per = el / reps
+    return {"value": W["N"] / per, "unit": "DoF/s", "cores": threads, "kind": "port",
+            "sample": f"{reps} full FP64 vmults of the same 3D DGQ{args.degree} {n}^3 workload, "
+                      f"{per:.3f} s each, {threads} OpenMP threads"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    W = workload(args)
+    from oracle import oracle as O
+    O.build()
+    import numpy as np
+    n = args.cells
+    h = O.SchwarzHandle(args.dim, args.degree, (n,) * args.dim, patch_variant=1, omega=args.omega)
+    src = philox_src(W["N"], args.seed)
+    dst = np.zeros_like(src)
+    # one step = a bounded sample: 1/8 of the patches (about one color's worth) per step
+    P = h.n_patches
+    chunk = max(1, P // 8)
+    steps, warm = args.steps, args.warmup
+    for i in range(warm):
+        h.apply_range((i * chunk) % P, min(P, (i * chunk) % P + chunk), dst, src)
+    t0 = time.perf_counter()
+    done = 0
+    for i in range(steps):
+        b = (i * chunk) % P
+        e = min(P, b + chunk)
+        h.apply_range(b, e, dst, src)
+        done += e - b
+    el = time.perf_counter() - t0
+    h.close()
+    value = W["N"] * (done / P) / el
+    threads = O.num_threads()
+    line = {"metric": METRIC, "value": value, "unit": "DoF/s", "n_gpus": args.gpus, "steps": steps,
+            "warmup": warm, "ms_per_step": 1e3 * el / steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": f"additive vertex-patch Schwarz vmult, 3D SIPG DGQ{args.degree}, "
+                                   f"{n}^3 cells, {W['N']} DoFs",
+                       "sample_per_step": f"{chunk} of {P} patches"},
+            "cpu_baseline": {"value": value, "unit": "DoF/s", "cores": threads, "kind": "port",
+                             "sample": f"{steps} steps of {chunk} patches (1/8 of a vmult) each, "
+                                       f"CPU oracle port, {threads} OpenMP threads"},
+            "e2e": {"value": value, "unit": "DoF/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    import tpss_gb300 as tpss
+    W = workload(args)
+    n, k, dim = args.cells, args.degree, args.dim
+    prec = tpss.Precision.fp32 if args.precision == "fp32" else tpss.Precision.fp64
+    sh = tpss.SubdomainHandler(tpss.SubdomainHandler.AdditionalData(
+        dim=dim, degree=k, n_cells=(n,) * dim, patch_variant=tpss.PatchVariant.vertex))
+    p = tpss.SchwarzPreconditioner()
+    p.initialize(sh, None, tpss.SchwarzPreconditioner.AdditionalData(relaxation=args.omega,
+                                                                     precision=prec))
+    n_colors = sh.n_colors()
+    src_h = philox_src(W["N"], args.seed + rank)
+    src = torch.tensor(src_h, dtype=torch.float64, device="cuda")
+    dst = torch.empty_like(src)
+    stream = torch.cuda.current_stream()
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    for _ in range(args.warmup):
+        p.vmult(dst, src)
+    td0 = p.get_time_data()
+    barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks.mark("t0")
+    e0.record(stream)
+    for _ in range(args.steps):
+        p.vmult(dst, src)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clocks.mark("t1")
+    barrier()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    td1 = p.get_time_data()
+    t_max = ms
+    if dist is not None:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_max = float(t.item())
+    value = world * W["N"] / (t_max * 1e-3)
+
+    # dominant kernel: the fused color kernel, timed by the library's "Apply inverses" CUDA
+    # events on the launching stream (colors launched back to back)
+    apply_s = td1[1].time - td0[1].time
+    apply_calls = td1[1].n_calls - td0[1].n_calls
+    per_launch = apply_s / max(1, apply_calls * n_colors)
+    P = W["P"]
+    units_per_launch = P / n_colors
+    flops_launch = units_per_launch * W["flops_per_patch"]
+    bytes_launch = units_per_launch * W["n1d"] ** dim * 24  # gather src + RMW dst, 8 B each
+    hbm_peak, hbm_kind = measured_peaks()
+    fma_peak = tpss_fma_peak(tpss, prec)
+    achieved_gbs = bytes_launch / per_launch / 1e9
+    achieved_tf = flops_launch / per_launch / 1e12
+    traffic = ncu_traffic(dim, k)
+    roofline = {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
+                "frac": achieved_gbs / hbm_peak, "traffic": traffic,
+                "peak_source": f"{hbm_kind} (MEASURED_PEAKS.json hbm_gbs)",
+                "kernel": f"schwarz_color_kernel<{args.precision},3,2,{k + 1}>",
+                "per_launch_ms": per_launch * 1e3,
+                "algorithmic_bytes_per_launch": bytes_launch,
+                "binding": "fp32 FMA pipe (CUDA cores)" if prec == tpss.Precision.fp32 else "fp64 FMA pipe",
+                "compute": {"achieved": achieved_tf, "peak": fma_peak / 1e12, "unit": "TFLOP/s",
+                            "frac": achieved_tf * 1e12 / fma_peak,
+                            "peak_source": "measured in this run (tpss_diag_fma_peak)",
+                            "algorithmic_flops_per_launch": flops_launch}}
+
+    out = {"metric": METRIC, "value": value, "unit": "DoF/s", "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": t_max, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32" if prec == tpss.Precision.fp32 else "f64",
+           "data": "synthetic (f ~ U[-1,1] per DoF, numpy Philox seed %d)" % args.seed,
+           "config": {"workload": f"additive vertex-patch Schwarz vmult, 3D SIPG DGQ{k}, {n}^3 cells, "
+                                  f"{W['N']} DoFs, {P} patches of {W['n1d']}^3, FP32 smoother / FP64 vectors",
+                      "dim": dim, "degree": k, "cells_per_direction": n, "n_dofs": W["N"],
+                      "n_patches": P, "n_colors": n_colors, "relaxation": args.omega,
+                      "l2": "inputs larger than L2 (src and dst 262 MB each)",
+                      "parallelism": "replicas" if world > 1 else "single GPU"},
+           "gpu_launches": args.steps * n_colors,
+           "roofline": roofline, "clocks": clk}
+
+    if not args.no_e2e:
+        out["e2e"] = e2e(tpss, p, src_h, args, W, world, dist)
+    if not args.no_solve:
+        out["solve"] = solve_times(tpss, args)
+    if rank == 0 and not args.no_cpu:
+        out["cpu_baseline"] = cpu_baseline(args, W)
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def tpss_fma_peak(tpss, prec):
+    import ctypes as C
+    v = C.c_double(0.0)
+    tpss._lib.check(tpss.load().tpss_diag_fma_peak(prec, 1 << 16, C.byref(v), None))
+    v2 = C.c_double(0.0)
+    tpss._lib.check(tpss.load().tpss_diag_fma_peak(prec, 1 << 16, C.byref(v2), None))
+    return max(v.value, v2.value)
+
+
+def e2e(tpss, p, src_h, args, W, world, dist):
+    """Same metric through the C ABI with host buffers: H2D of src, vmult, D2H of dst."""
+    import torch
+    N = W["N"]
+    h_src = torch.tensor(src_h, dtype=torch.float64).pin_memory()
+    h_dst = torch.empty(N, dtype=torch.float64).pin_memory()
+    d_src = torch.empty(N, dtype=torch.float64, device="cuda")
+    d_dst = torch.empty_like(d_src)
+    stream = torch.cuda.current_stream()
+    steps = max(3, min(args.steps, 50))
+
+    def step():
+        d_src.copy_(h_src, non_blocking=True)
+        p.vmult(d_dst, d_src)
+        h_dst.copy_(d_dst, non_blocking=True)
+
+    for _ in range(3):
+        step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    if dist is not None:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    return {"value": world * N / (ms * 1e-3), "unit": "DoF/s", "h2d_bytes_per_step": N * 8,
+            "d2h_bytes_per_step": N * 8, "ms_per_step": ms, "steps": steps}
+
+
+def solve_times(tpss, args):
+    """CG + GMG solve to 1e-8 relative residual, FP32 vs FP64 smoother (same workload mesh,
+    one root cell, 7 levels, dense coarse solve, V-cycle captured in a CUDA graph)."""
+    import torch
+    res = {}
+    n, k, dim = args.cells, args.degree, args.dim
+    N = n ** dim * (k + 1) ** dim
+    f = torch.tensor(philox_src(N, args.seed), dtype=torch.float64, device="cuda")
+    for name, prec in (("fp32", tpss.Precision.fp32), ("fp64", tpss.Precision.fp64)):
+        mg = tpss.MultigridSolver(dim, k, 1, n, relaxation=args.omega, precision=prec,
+                                  coarse_solver=1, use_graph=True)
+        u = torch.zeros_like(f)
+        mg.vmult(u, f)  # warm-up: graph capture
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        it, hist = mg.solve(u, f, rel_tol=1e-8)
+        torch.cuda.synchronize()
+        el = time.perf_counter() - t0
+        res[name] = {"seconds": el, "iterations": it, "final_rel_residual": float(hist[-1] / hist[0])}
+        del mg
+    res["fp32_over_fp64_time"] = res["fp32"]["seconds"] / res["fp64"]["seconds"]
+    res["workload"] = (f"CG + V-cycle (1 pre/1 post additive vertex-patch Schwarz step, omega "
+                       f"{args.omega}), 3D SIPG DGQ{k} {n}^3, f ~ U[-1,1], to 1e-8 rel. residual")
+    return res
+
+
+def main():
+    args = parse()
+    if args.steps < 1 or args.warmup < 3:
+        raise SystemExit("need --steps >= 1 and --warmup >= 3")
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,223 @@
+/*
+ * tpss_gpu.h -- C ABI of the GB300 (sm_103a) Schwarz-smoother library.
+ *
+ * This is the drop-in boundary for the TPSS Schwarz smoother path (jwitte08/TPSS):
+ * SchwarzPreconditioner / SchwarzSmoother applied on one multigrid level, with the
+ * SubdomainHandler's patch layout, coloring and damping semantics, plus the matrix-free SIPG
+ * operator, DG level transfer and CG + V-cycle that the smoother runs inside.
+ *
+ * Conventions
+ *  - Every entry point returns an int status (TPSS_OK == 0) and never aborts;
+ *    tpss_last_error() gives a message for the calling thread's last failure.
+ *  - Vectors passed to *_vmult / *_step / *_solve are DEVICE pointers to FP64 arrays in the
+ *    layout's DoF numbering (cell-wise blocks of (k+1)^dim lexicographic DoFs, the deal.II
+ *    FE_DGQ level numbering); the library owns all other device memory behind opaque handles.
+ *  - Work is ordered on the caller's stream (a cudaStream_t passed as void*; NULL = legacy
+ *    default stream).  Handles are not reentrant: one stream at a time per handle, as the
+ *    reference's SchwarzPreconditioner::vmult is const but mutates timers and scratch
+ *    (schwarz_preconditioner.h:184-236).
+ *  - No torch or deal.II types appear here; plain pointers and sizes only.
+ */
+#ifndef TPSS_GPU_H
+#define TPSS_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define TPSS_OK 0
+#define TPSS_ERR_INVALID_ARGUMENT 1
+#define TPSS_ERR_NOT_IMPLEMENTED 2 /* reference throws ExcMessage("TODO ...") here too */
+#define TPSS_ERR_CUDA 3
+#define TPSS_ERR_OUT_OF_MEMORY 4
+#define TPSS_ERR_NOT_FINITE 5 /* AssertIsFinite(dst.l2_norm()) of schwarz_preconditioner.templates.h:238 */
+#define TPSS_ERR_NOT_CONVERGED 6
+#define TPSS_ERR_STATE 7
+
+/* TPSS::DoFLayout (TPSS/TPSS.h) */
+#define TPSS_DOF_DGQ 0
+/* TPSS::PatchVariant */
+#define TPSS_PATCH_CELL 0
+#define TPSS_PATCH_VERTEX 1
+/* TPSS::SmootherVariant */
+#define TPSS_ADDITIVE 0
+#define TPSS_MULTIPLICATIVE 1
+/* arithmetic of the smoother (gather, local solve, scatter); vectors stay FP64 */
+#define TPSS_FP64 0
+#define TPSS_FP32 1
+
+typedef struct tpss_layout tpss_layout;
+typedef struct tpss_operator tpss_operator;
+typedef struct tpss_precond tpss_precond;
+typedef struct tpss_smoother tpss_smoother;
+typedef struct tpss_mg tpss_mg;
+
+/*
+ * Patch layout of one level: replaces SubdomainHandler::reinit
+ * (TPSS/subdomain_handler.templates.h:3-154) with PatchInfo vertex/cell patch gathering
+ * (TPSS/patch_info.templates.h:59-409), the user coloring (apps/coloring.h:347-401 tiled
+ * 2^dim colors for vertex patches; one color for additive cell patches; two red-black colors
+ * for multiplicative cell patches), interior-before-boundary order within a color
+ * (patch_info.templates.h:605-680) and DoFInfo's cell-wise DoF caching
+ * (TPSS/dof_info.templates.h:44-182).
+ */
+typedef struct tpss_layout_desc
+{
+  int dim;              /* 2 or 3 */
+  int degree;           /* k, 1..7 */
+  int dof_layout;       /* TPSS_DOF_DGQ */
+  int patch_variant;    /* TPSS_PATCH_VERTEX or TPSS_PATCH_CELL */
+  int smoother_variant; /* TPSS_ADDITIVE or TPSS_MULTIPLICATIVE (selects the coloring) */
+  int n_cells[3];       /* cells per direction of the structured (Cartesian) level */
+  const double *cell_h[3];        /* host: n_cells[d] cell widths per direction; NULL = 1/n */
+  const int64_t *cell_dof_start;  /* host: first DoF of each lexicographic cell (x fastest);
+                                     NULL = cell index * (k+1)^dim */
+  const int32_t *patch_color;     /* host: optional user coloring, one entry per patch in the
+                                     default patch order (tpss_layout_patches); NULL = default */
+} tpss_layout_desc;
+
+/* Replaces SubdomainHandler<dim,Number>::reinit (TPSS/subdomain_handler.h:33-225). */
+int tpss_layout_create(const tpss_layout_desc *desc, tpss_layout **out);
+/* SchwarzPreconditioner::m() (schwarz_preconditioner.h:153-163) and PartitionData counts. */
+int tpss_layout_info(const tpss_layout *layout, int64_t *n_dofs, int64_t *n_patches,
+                     int *n_colors);
+/* Host copy of the patch list: lower cell coordinate (3 ints, unused directions 0) and color
+ * of each patch in storage order (colors ascending, interior patches first). */
+int tpss_layout_patches(const tpss_layout *layout, int32_t *lower_cells, int32_t *colors);
+void tpss_layout_destroy(tpss_layout *layout);
+
+/*
+ * Matrix-free SIPG Laplace operator of one level (apps/laplace_integrator.h:578-743):
+ * dst = A src with interior penalty ip*gamma*(1/h_in+1/h_out)/2 and Dirichlet boundary
+ * penalty 2*ip*gamma/h, gamma = k(k+1) (apps/common_integrator.h:30-37).
+ */
+int tpss_operator_create(const tpss_layout *layout, double ip_factor, tpss_operator **out);
+/* MF::Operator::vmult (apps/laplace_integrator.h:578-598), FP64. */
+int tpss_operator_vmult(tpss_operator *op, double *dst, const double *src, void *stream);
+void tpss_operator_destroy(tpss_operator *op);
+
+/* SchwarzPreconditioner::AdditionalData (schwarz_preconditioner.h:495-515) plus the
+ * local-solver and arithmetic choices. */
+typedef struct tpss_precond_desc
+{
+  double relaxation;           /* local damping omega (> 0) */
+  int reverse;                 /* reverse color sequence (multiplicative) */
+  int symmetrized;             /* forward + backward color sweep (multiplicative) */
+  int use_ras_weights;         /* divide local solutions by patch multiplicity (additive) */
+  int use_ras_boolean_weights; /* not implemented: returns TPSS_ERR_NOT_IMPLEMENTED */
+  int precision;               /* TPSS_FP64 or TPSS_FP32 smoother arithmetic */
+  double ip_factor;            /* EquationData::ip_factor of the local SIPG matrices */
+  int check_finite;            /* 1: vmult checks that dst is finite (one extra reduction) */
+} tpss_precond_desc;
+
+/*
+ * SchwarzPreconditioner::initialize(subdomain_handler, operator, additional_data)
+ * (schwarz_preconditioner.templates.h:1-60): assembles the 1-D SIPG mass/Laplace matrices of
+ * every patch and direction (FD::MatrixIntegrator::assemble_subspace_inverses,
+ * apps/laplace_integrator.h:226-250) and solves their generalized eigenproblems in FP64 on
+ * the GPU.  `op` is the level operator (required for TPSS_MULTIPLICATIVE, may be NULL for
+ * additive); it is not owned and must outlive the preconditioner.
+ */
+int tpss_precond_create(const tpss_layout *layout, tpss_operator *op,
+                        const tpss_precond_desc *desc, tpss_precond **out);
+/* Shallow copy with different AdditionalData (schwarz_preconditioner.templates.h:63-86):
+ * shares the layout and local solvers of `other`. */
+int tpss_precond_create_shallow(const tpss_precond *other, const tpss_precond_desc *desc,
+                                tpss_precond **out);
+/* SchwarzPreconditioner::vmult (schwarz_preconditioner.templates.h:209-239): dst is set to
+ * zero and receives sum over colors of omega R_j^T A_j^-1 R_j src. */
+int tpss_precond_vmult(tpss_precond *p, double *dst, const double *src, void *stream);
+/* vmult_add (schwarz_preconditioner.templates.h:185-194): dst += P src. */
+int tpss_precond_vmult_add(tpss_precond *p, double *dst, const double *src, void *stream);
+/* Tvmult: the reference throws "TODO transpose operation is not implemented"; so does this
+ * (TPSS_ERR_NOT_IMPLEMENTED). */
+int tpss_precond_Tvmult(tpss_precond *p, double *dst, const double *src, void *stream);
+
+/* TimeInfo (TPSS/time_info.h:23-64): the five preconditioner timers of
+ * schwarz_preconditioner.templates.h:22-26, in seconds, measured with CUDA events. */
+typedef struct tpss_time_info
+{
+  double time;
+  int64_t n_calls;
+  char description[64];
+} tpss_time_info;
+int tpss_precond_time_info(tpss_precond *p, tpss_time_info *out, int *n_inout);
+void tpss_precond_destroy(tpss_precond *p);
+
+/*
+ * SchwarzSmoother / SmootherRichardson (smoother/schwarz_smoother.h:16-52,
+ * smoother/smoother_richardson.h:41-156): step computes x += damping * P (b - A x)
+ * n_steps times; vmult sets x = 0 first.  Neither the operator nor the preconditioner is
+ * owned.
+ */
+int tpss_smoother_create(tpss_operator *op, tpss_precond *p, int n_steps, double damping,
+                         tpss_smoother **out);
+int tpss_smoother_step(tpss_smoother *s, double *x, const double *b, void *stream);
+int tpss_smoother_vmult(tpss_smoother *s, double *x, const double *b, void *stream);
+void tpss_smoother_destroy(tpss_smoother *s);
+
+/*
+ * Geometric multigrid on the unit cube (apps/poisson_problem.h:642-755,
+ * apps/multigrid.h:201-399): n_rep^dim root cells refined to n_cells_fine per direction,
+ * SIPG level operators, DG embedding transfer, Schwarz pre/post smoothers on levels >= 1,
+ * coarse CG to an absolute residual of coarse_tol on level 0, one V-cycle per application.
+ */
+typedef struct tpss_mg_desc
+{
+  int dim, degree;
+  int n_rep;          /* root cells per direction */
+  int n_cells_fine;   /* n_rep * 2^L */
+  double ip_factor;
+  int patch_variant, smoother_variant;
+  double relaxation;  /* Schwarz local damping */
+  int precision;      /* smoother arithmetic, TPSS_FP64 / TPSS_FP32 */
+  double coarse_tol;  /* absolute; reference default 1e-12 (apps/multigrid.h:82-91) */
+  int coarse_solver;  /* 0: CG to coarse_tol (CoarseGridParameter IterativeAcc, the reference
+                         default); 1: dense inverse of the coarse matrix (the FullSVD variant of
+                         apps/multigrid.h:176-182), which lets the whole V-cycle be one graph */
+  int use_graph;      /* capture the V-cycle in CUDA graphs (one graph with the dense coarse
+                         solver; down- and up-sweep graphs around the CG coarse solve) */
+} tpss_mg_desc;
+
+int tpss_mg_create(const tpss_mg_desc *desc, tpss_mg **out);
+/* Finest-level vector size. */
+int tpss_mg_n_dofs(const tpss_mg *mg, int64_t *n_dofs);
+/* PreconditionMG::vmult: dst = V-cycle(src) on the finest level. */
+int tpss_mg_vmult(tpss_mg *mg, double *dst, const double *src, void *stream);
+/* SolverCG with ReductionControl (apps/poisson_problem.h:726-755, apps/rt_parameter.h:39-41):
+ * solves A u = f (u := 0 first), stopping when ||r|| <= max(abs_tol, rel_tol ||r_0||).
+ * On return *iterations holds the CG iteration count and res_history (host, length
+ * max_iter+1, may be NULL) the residual norms. */
+int tpss_mg_cg_solve(tpss_mg *mg, double *u, const double *f, double rel_tol, double abs_tol,
+                     int max_iter, int *iterations, double *res_history, void *stream);
+/* Level objects for direct use (level 0 = coarsest). */
+int tpss_mg_level(tpss_mg *mg, int level, tpss_layout **layout, tpss_operator **op,
+                  tpss_precond **precond);
+int tpss_mg_n_levels(const tpss_mg *mg, int *n_levels);
+void tpss_mg_destroy(tpss_mg *mg);
+
+/* DG level transfer between lexicographic structured levels (MGTransferMatrixFree for DGQ):
+ * fine += P coarse (prolongate_and_add), coarse += P^T fine (restrict_and_add). */
+int tpss_transfer_prolongate_add(int dim, int degree, const int *n_cells_coarse,
+                                 double *fine, const double *coarse, void *stream);
+int tpss_transfer_restrict_add(int dim, int degree, const int *n_cells_coarse, double *coarse,
+                               const double *fine, void *stream);
+
+/* Measurement helper with no counterpart in the reference: FMA-pipe throughput of the
+ * current GPU in FLOP/s for TPSS_FP32 or TPSS_FP64 (8 independent FMA chains per thread on
+ * every SM, `iters` FMAs per chain, timed with CUDA events).  The roofline denominator of the
+ * CUDA-core-bound fast-diagonalization kernels. */
+int tpss_diag_fma_peak(int precision, int iters, double *flops_per_second, void *stream);
+
+const char *tpss_last_error(void);
+/* Library version string. */
+const char *tpss_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TPSS_GPU_H */

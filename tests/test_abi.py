@@ -1,0 +1,119 @@
+"""C-ABI library checks that need no GPU: it loads, exports every symbol that
+include/tpss_gpu.h declares, builds patch layouts identical to the oracle's, and rejects
+invalid input with the documented status codes."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def header_symbols():
+    src = open(os.path.join(ROOT, "include", "tpss_gpu.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(tpss_[a-zA-Z0-9_]+)\s*\(", src)))
+
+
+def test_library_exports_every_declared_symbol(tpss):
+    lib = tpss.load()
+    syms = header_symbols()
+    assert len(syms) >= 25
+    for s in syms:
+        assert hasattr(lib, s), s
+    from tpss_gb300 import _lib
+    assert set(syms) == set(_lib.SIGNATURES), set(syms) ^ set(_lib.SIGNATURES)
+    assert b"sm_103a" in lib.tpss_version()
+
+
+@pytest.mark.parametrize("dim,nc,pv,sv", [(2, (5, 4), 1, 0), (3, (3, 4, 5), 1, 0), (2, (3, 3), 0, 0),
+                                          (3, (3, 2, 2), 0, 1), (2, (6, 5), 0, 1), (2, (2, 2), 1, 0),
+                                          (3, (2, 2, 2), 1, 1), (2, (64, 64), 1, 0)])
+def test_layout_matches_oracle(tpss, oracle, dim, nc, pv, sv):
+    ad = tpss.SubdomainHandler.AdditionalData(dim=dim, degree=2, n_cells=nc, patch_variant=pv,
+                                              smoother_variant=sv)
+    sh = tpss.SubdomainHandler(ad)
+    lo, col = sh.patches()
+    lo2, col2, nco = oracle.patches(dim, nc, pv, sv)
+    assert sh.n_colors() == nco
+    np.testing.assert_array_equal(lo, lo2)
+    np.testing.assert_array_equal(col, col2)
+    assert sh.n_dofs() == int(np.prod(nc)) * 3 ** dim
+
+
+def test_layout_colors_are_conflict_free(tpss):
+    ad = tpss.SubdomainHandler.AdditionalData(dim=3, degree=1, n_cells=(6, 5, 4), patch_variant=1)
+    sh = tpss.SubdomainHandler(ad)
+    lo, col = sh.patches()
+    for c in range(sh.n_colors()):
+        cells = set()
+        for l in lo[col == c]:
+            for b in range(8):
+                cell = (l[0] + (b & 1), l[1] + ((b >> 1) & 1), l[2] + ((b >> 2) & 1))
+                assert cell not in cells
+                cells.add(cell)
+    # interior patches before boundary patches within each color
+    nc = np.array([6, 5, 4])
+    for c in range(sh.n_colors()):
+        bd = [bool(np.any(l == 0) or np.any(l + 1 == nc - 1)) for l in lo[col == c]]
+        assert bd == sorted(bd)
+
+
+def test_user_coloring_conflict_is_rejected(tpss):
+    ad = tpss.SubdomainHandler.AdditionalData(dim=2, degree=1, n_cells=(4, 4), patch_variant=1)
+    P = tpss.SubdomainHandler(ad).n_subdomains()
+    ad.coloring = [0] * P  # all overlapping vertex patches in one color
+    with pytest.raises(tpss.TPSSInvalidArgument, match="conflict"):
+        tpss.SubdomainHandler(ad)
+    ad.coloring = list(range(P))  # one patch per color is always race-free
+    sh = tpss.SubdomainHandler(ad)
+    assert sh.n_colors() == P
+
+
+@pytest.mark.parametrize("bad", [dict(dim=4), dict(degree=0), dict(degree=8),
+                                 dict(n_cells=(0, 3)), dict(patch_variant=7)])
+def test_invalid_layouts(tpss, bad):
+    args = dict(dim=2, degree=2, n_cells=(3, 3), patch_variant=1)
+    args.update(bad)
+    with pytest.raises(tpss.TPSSInvalidArgument):
+        tpss.SubdomainHandler(tpss.SubdomainHandler.AdditionalData(**args))
+
+
+def test_cell_dof_start_must_be_a_permutation(tpss):
+    ad = tpss.SubdomainHandler.AdditionalData(dim=2, degree=1, n_cells=(2, 2), patch_variant=1,
+                                              cell_dof_start=[0, 4, 4, 12])
+    with pytest.raises(tpss.TPSSInvalidArgument):
+        tpss.SubdomainHandler(ad)
+
+
+def test_precond_option_errors_before_gpu_work(tpss):
+    """Both RAS options together and RAS boolean weights are rejected as in
+    schwarz_preconditioner.templates.h:599-600 -- before any device memory is touched."""
+    ad = tpss.SubdomainHandler.AdditionalData(dim=2, degree=1, n_cells=(3, 3), patch_variant=1)
+    sh = tpss.SubdomainHandler(ad)
+    p = tpss.SchwarzPreconditioner()
+    with pytest.raises(tpss.TPSSInvalidArgument, match="more than one RAS"):
+        p.initialize(sh, None, tpss.SchwarzPreconditioner.AdditionalData(
+            use_ras_weights=True, use_ras_boolean_weights=True))
+    with pytest.raises(tpss.TPSSNotImplemented):
+        p.initialize(sh, None, tpss.SchwarzPreconditioner.AdditionalData(use_ras_boolean_weights=True))
+    with pytest.raises(tpss.TPSSInvalidArgument, match="relaxation"):
+        p.initialize(sh, None, tpss.SchwarzPreconditioner.AdditionalData(relaxation=0.0))
+
+
+def test_damping_lookup(tpss, oracle):
+    for pv in (0, 1):
+        for sv in (0, 1):
+            for dim in (2, 3):
+                assert tpss.lookup_damping_factor(pv, sv, dim) == oracle.lookup_damping_factor(pv, sv, dim)
+
+
+def test_null_arguments_return_status(tpss):
+    lib = tpss.load()
+    assert lib.tpss_layout_create(None, None) == 1
+    assert b"null" in lib.tpss_last_error()
+    assert lib.tpss_precond_vmult(None, None, None, None) == 1
+    n = C.c_int(0)
+    assert lib.tpss_mg_n_levels(None, C.byref(n)) == 1

@@ -1,0 +1,304 @@
+"""GPU parity of the Schwarz smoother path against the CPU oracle (through the C ABI).
+
+Tolerances (stated per spec precision rules):
+  FP64 smoother, operator, transfer: relative max-norm error <= 1e-12
+  FP32 smoother (FP32 gather / FD / scatter into FP64 vectors): relative error <= 2e-5
+  CG+MG: identical iteration counts to the oracle.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def rel_err(a, b):
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+def philox(seed, n):
+    return np.random.Generator(np.random.Philox(seed)).uniform(-1.0, 1.0, n)
+
+
+def gpu_vmult(tpss, cuda, dim, k, nc, src, pv=1, sv=0, omega=1.0, ip=1.0, precision=0, h=None,
+              cell_start=None, ras=False, reverse=False, symmetrized=False, coloring=None):
+    import torch
+    ad = tpss.SubdomainHandler.AdditionalData(dim=dim, degree=k, n_cells=nc, patch_variant=pv,
+                                              smoother_variant=sv, cell_h=h,
+                                              cell_dof_start=cell_start, coloring=coloring)
+    sh = tpss.SubdomainHandler(ad)
+    op = tpss.LaplaceOperator(sh, ip) if sv == 1 else None
+    p = tpss.SchwarzPreconditioner()
+    p.initialize(sh, op, tpss.SchwarzPreconditioner.AdditionalData(
+        relaxation=omega, precision=precision, ip_factor=ip, use_ras_weights=ras,
+        reverse=reverse, symmetrized=symmetrized))
+    s = torch.tensor(src, dtype=torch.float64, device=cuda)
+    d = torch.full_like(s, 123.0)  # vmult must overwrite dst
+    p.vmult(d, s)
+    torch.cuda.synchronize()
+    return d.cpu().numpy(), p
+
+
+CASES = [
+    # dim, k, n_cells, patch_variant
+    (2, 1, (4, 4), 1), (2, 3, (6, 5), 1), (2, 5, (3, 4), 1), (2, 7, (3, 3), 1),
+    (3, 1, (3, 3, 3), 1), (3, 2, (4, 3, 5), 1), (3, 4, (4, 4, 4), 1), (3, 7, (2, 3, 2), 1),
+    (2, 2, (5, 3), 0), (2, 6, (3, 3), 0), (3, 3, (3, 2, 4), 0), (3, 5, (2, 2, 3), 0),
+]
+
+
+@pytest.mark.parametrize("dim,k,nc,pv", CASES)
+def test_additive_fp64_parity(tpss, oracle, cuda, dim, k, nc, pv):
+    N = int(np.prod(nc)) * (k + 1) ** dim
+    src = philox(100 + k, N)
+    om = 0.37
+    got, _ = gpu_vmult(tpss, cuda, dim, k, nc, src, pv=pv, omega=om)
+    ref = oracle.schwarz_vmult(dim, k, nc, src, patch_variant=pv, omega=om)
+    assert rel_err(got, ref) <= 1e-12
+
+
+@pytest.mark.parametrize("dim,k,nc,pv", CASES)
+def test_additive_fp32_parity(tpss, oracle, cuda, dim, k, nc, pv):
+    N = int(np.prod(nc)) * (k + 1) ** dim
+    src = philox(200 + k, N)
+    got, _ = gpu_vmult(tpss, cuda, dim, k, nc, src, pv=pv, omega=0.5, precision=1)
+    ref = oracle.schwarz_vmult(dim, k, nc, src, patch_variant=pv, omega=0.5)
+    assert rel_err(got, ref) <= 2e-5
+
+
+def test_golden_vmult_fixtures(tpss, cuda):
+    g = np.load(os.path.join(GOLDEN, "vmult.npz"))
+    cases = json.load(open(os.path.join(GOLDEN, "vmult_cases.json")))
+    for i, c in enumerate(cases):
+        got, _ = gpu_vmult(tpss, cuda, c["dim"], c["k"], c["n_cells"], g[f"c{i}_src"],
+                           pv=c["patch_variant"], sv=c["smoother_variant"], omega=c["omega"],
+                           ip=c["ip"])
+        assert rel_err(got, g[f"c{i}_dst"]) <= 1e-12, i
+
+
+def test_nonuniform_h_permuted_cells_ras(tpss, oracle, cuda):
+    dim, k, nc = 3, 2, (4, 3, 3)
+    g = np.random.default_rng(1)
+    h = [g.uniform(0.5, 1.5, n) for n in nc]
+    h = [x / x.sum() for x in h]
+    ncell = int(np.prod(nc))
+    nd = (k + 1) ** dim
+    cell_start = g.permutation(ncell) * nd
+    src = philox(7, ncell * nd)
+    for ras in (False, True):
+        got, _ = gpu_vmult(tpss, cuda, dim, k, nc, src, pv=1, omega=0.8, h=h, cell_start=cell_start,
+                           ras=ras)
+        ref = oracle.schwarz_vmult(dim, k, nc, src, patch_variant=1, omega=0.8, h=h,
+                                   cell_start=cell_start, use_ras=ras)
+        assert rel_err(got, ref) <= 1e-12, ras
+
+
+@pytest.mark.parametrize("dim,k,nc,pv,rev,sym", [(2, 3, (5, 4), 1, False, False),
+                                                 (2, 2, (4, 4), 0, False, False),
+                                                 (3, 2, (3, 3, 3), 1, True, False),
+                                                 (3, 1, (3, 4, 3), 0, False, True),
+                                                 (2, 4, (4, 3), 1, False, True)])
+def test_multiplicative_parity(tpss, oracle, cuda, dim, k, nc, pv, rev, sym):
+    N = int(np.prod(nc)) * (k + 1) ** dim
+    src = philox(31, N)
+    got, _ = gpu_vmult(tpss, cuda, dim, k, nc, src, pv=pv, sv=1, omega=1.0, reverse=rev,
+                       symmetrized=sym)
+    ref = oracle.schwarz_vmult(dim, k, nc, src, patch_variant=pv, smoother_variant=1, omega=1.0,
+                               reverse=rev, symmetrized=sym)
+    assert rel_err(got, ref) <= 1e-11
+
+
+def test_user_coloring_same_additive_result(tpss, oracle, cuda):
+    dim, k, nc = 2, 2, (5, 5)
+    ad = tpss.SubdomainHandler.AdditionalData(dim=dim, degree=k, n_cells=nc, patch_variant=1)
+    P = tpss.SubdomainHandler(ad).n_subdomains()
+    src = philox(3, 25 * 9)
+    got, _ = gpu_vmult(tpss, cuda, dim, k, nc, src, pv=1, omega=1.0, coloring=list(range(P)))
+    ref = oracle.schwarz_vmult(dim, k, nc, src, patch_variant=1, omega=1.0)
+    assert rel_err(got, ref) <= 1e-12
+
+
+def test_edge_cases(tpss, oracle, cuda):
+    import torch
+    # a single vertex patch (2^dim cells) and no vertex patch at all (1 cell per direction)
+    for dim in (2, 3):
+        N = 2 ** dim * 27 if dim == 3 else 4 * 9
+        src = philox(1, N)
+        got, _ = gpu_vmult(tpss, cuda, dim, 2, (2,) * dim, src, pv=1)
+        assert rel_err(got, oracle.schwarz_vmult(dim, 2, (2,) * dim, src, patch_variant=1)) <= 1e-12
+        src1 = philox(2, 3 ** dim)
+        got1, p = gpu_vmult(tpss, cuda, dim, 2, (1,) * dim, src1, pv=1)
+        assert np.all(got1 == 0.0) and p.subdomain_handler.n_subdomains() == 0
+    # elongated meshes
+    src = philox(4, 9 * 2 * 4)
+    got, _ = gpu_vmult(tpss, cuda, 2, 1, (9, 2), src, pv=1)
+    assert rel_err(got, oracle.schwarz_vmult(2, 1, (9, 2), src, patch_variant=1)) <= 1e-12
+    # Tvmult is not implemented in the reference either
+    ad = tpss.SubdomainHandler.AdditionalData(dim=2, degree=1, n_cells=(3, 3), patch_variant=1)
+    sh = tpss.SubdomainHandler(ad)
+    p = tpss.SchwarzPreconditioner()
+    p.initialize(sh, None, tpss.SchwarzPreconditioner.AdditionalData())
+    x = torch.zeros(sh.n_dofs(), dtype=torch.float64, device=cuda)
+    with pytest.raises(tpss.TPSSNotImplemented):
+        p.Tvmult(x, x.clone())
+    with pytest.raises(ValueError):
+        p.vmult(x[:-1], x[:-1].clone())
+    with pytest.raises(tpss.TPSSInvalidArgument):
+        p.vmult(x, x)  # aliasing dst and src is rejected
+
+
+def test_vmult_add_and_time_data(tpss, oracle, cuda):
+    import torch
+    dim, k, nc = 2, 3, (4, 4)
+    N = 16 * 16
+    src = philox(5, N)
+    base = philox(6, N)
+    ad = tpss.SubdomainHandler.AdditionalData(dim=dim, degree=k, n_cells=nc, patch_variant=1)
+    sh = tpss.SubdomainHandler(ad)
+    p = tpss.SchwarzPreconditioner()
+    p.initialize(sh, None, tpss.SchwarzPreconditioner.AdditionalData(relaxation=0.25))
+    d = torch.tensor(base, dtype=torch.float64, device=cuda)
+    p.vmult_add(d, torch.tensor(src, dtype=torch.float64, device=cuda))
+    ref = base + oracle.schwarz_vmult(dim, k, nc, src, patch_variant=1, omega=0.25)
+    assert rel_err(d.cpu().numpy(), ref) <= 1e-12
+    td = p.get_time_data()
+    assert len(td) == 5 and td[4].description.startswith("[SchwarzPrecond] Step")
+    assert td[4].n_calls >= 1 and td[1].time > 0.0 and td[2].n_calls == 1
+    # shallow copy shares the local solvers
+    q = tpss.SchwarzPreconditioner()
+    q.initialize(p, tpss.SchwarzPreconditioner.AdditionalData(relaxation=0.5))
+    d2 = torch.zeros(N, dtype=torch.float64, device=cuda)
+    q.vmult(d2, torch.tensor(src, dtype=torch.float64, device=cuda))
+    ref2 = oracle.schwarz_vmult(dim, k, nc, src, patch_variant=1, omega=0.5)
+    assert rel_err(d2.cpu().numpy(), ref2) <= 1e-12
+
+
+@pytest.mark.parametrize("dim,k,nc,ip", [(2, 3, (5, 4), 1.0), (3, 2, (3, 4, 2), 2.5), (3, 4, (4, 4, 4), 1.0),
+                                         (2, 7, (3, 3), 1.0)])
+def test_operator_parity(tpss, oracle, cuda, dim, k, nc, ip):
+    import torch
+    ad = tpss.SubdomainHandler.AdditionalData(dim=dim, degree=k, n_cells=nc, patch_variant=1)
+    sh = tpss.SubdomainHandler(ad)
+    op = tpss.LaplaceOperator(sh, ip)
+    src = philox(9, sh.n_dofs())
+    d = torch.zeros(sh.n_dofs(), dtype=torch.float64, device=cuda)
+    op.vmult(d, torch.tensor(src, dtype=torch.float64, device=cuda))
+    ref = oracle.sipg_vmult(dim, k, nc, src, ip=ip)
+    assert rel_err(d.cpu().numpy(), ref) <= 1e-12
+
+
+@pytest.mark.parametrize("dim,k,ncc", [(2, 3, (3, 2)), (3, 2, (2, 3, 2)), (3, 5, (2, 2, 2))])
+def test_transfer_parity(tpss, oracle, cuda, dim, k, ncc):
+    import torch
+    nf = [2 * n for n in ncc]
+    nd = (k + 1) ** dim
+    uc = philox(1, int(np.prod(ncc)) * nd)
+    uf = philox(2, int(np.prod(nf)) * nd)
+    f = torch.tensor(uf, dtype=torch.float64, device=cuda)
+    c = torch.tensor(uc, dtype=torch.float64, device=cuda)
+    tpss.prolongate_add(dim, k, ncc, f, c)
+    ref = oracle.prolongate_add(dim, k, ncc, uc, uf)
+    assert rel_err(f.cpu().numpy(), ref) <= 1e-13
+    c2 = torch.tensor(uc, dtype=torch.float64, device=cuda)
+    tpss.restrict_add(dim, k, ncc, c2, torch.tensor(uf, dtype=torch.float64, device=cuda))
+    ref2 = oracle.restrict_add(dim, k, ncc, uc, uf)
+    assert rel_err(c2.cpu().numpy(), ref2) <= 1e-13
+
+
+def test_smoother_step(tpss, oracle, cuda):
+    import torch
+    dim, k, nc = 2, 3, (6, 6)
+    ad = tpss.SubdomainHandler.AdditionalData(dim=dim, degree=k, n_cells=nc, patch_variant=1)
+    sh = tpss.SubdomainHandler(ad)
+    op = tpss.LaplaceOperator(sh, 1.0)
+    p = tpss.SchwarzPreconditioner()
+    p.initialize(sh, op, tpss.SchwarzPreconditioner.AdditionalData(relaxation=0.25))
+    sm = tpss.SchwarzSmoother()
+    sm.initialize(op, p, tpss.SchwarzSmoother.AdditionalData(number_of_smoothing_steps=2))
+    b = philox(3, sh.n_dofs())
+    x0 = philox(4, sh.n_dofs())
+    x = torch.tensor(x0, dtype=torch.float64, device=cuda)
+    sm.step(x, torch.tensor(b, dtype=torch.float64, device=cuda))
+    ref = x0.copy()
+    for _ in range(2):
+        r = b - oracle.sipg_vmult(dim, k, nc, ref)
+        ref = ref + oracle.schwarz_vmult(dim, k, nc, r, patch_variant=1, omega=0.25)
+    assert rel_err(x.cpu().numpy(), ref) <= 1e-12
+    y = torch.tensor(x0, dtype=torch.float64, device=cuda)
+    sm.vmult(y, torch.tensor(b, dtype=torch.float64, device=cuda))
+    ref = np.zeros_like(b)
+    for _ in range(2):
+        r = b - oracle.sipg_vmult(dim, k, nc, ref)
+        ref = ref + oracle.schwarz_vmult(dim, k, nc, r, patch_variant=1, omega=0.25)
+    assert rel_err(y.cpu().numpy(), ref) <= 1e-12
+
+
+def test_mg_cg_iterations_match_oracle(tpss, oracle, xcheck, cuda):
+    import torch
+    for c in json.load(open(os.path.join(GOLDEN, "mg_iterations.json"))):
+        N = c["n_cells_fine"] ** c["dim"] * (c["k"] + 1) ** c["dim"]
+        if c["rhs"] == "random":
+            f = np.random.Generator(np.random.Philox(c["rhs_seed"])).uniform(-1, 1, N)
+        else:
+            f = xcheck.bells_load_vector(c["dim"], c["k"], c["n_cells_fine"])
+        for coarse_solver in (0, 1):
+            for graph in (False, True):
+                mg = tpss.MultigridSolver(c["dim"], c["k"], c["n_rep"], c["n_cells_fine"],
+                                          patch_variant=c["patch_variant"],
+                                          smoother_variant=c["smoother_variant"],
+                                          coarse_solver=coarse_solver, use_graph=graph)
+                u = torch.zeros(N, dtype=torch.float64, device=cuda)
+                it, hist = mg.solve(u, torch.tensor(f, dtype=torch.float64, device=cuda),
+                                    rel_tol=c["rel_tol"])
+                assert it == c["iterations"], (c, coarse_solver, graph, it)
+                assert abs(hist[-1] - c["final_residual"]) <= 1e-6 * c["initial_residual"]
+        # the FP32 smoother converges in the same or fewer iterations (+1 allowed)
+        mg32 = tpss.MultigridSolver(c["dim"], c["k"], c["n_rep"], c["n_cells_fine"],
+                                    patch_variant=c["patch_variant"],
+                                    smoother_variant=c["smoother_variant"], precision=1,
+                                    coarse_solver=1)
+        u = torch.zeros(N, dtype=torch.float64, device=cuda)
+        it32, _ = mg32.solve(u, torch.tensor(f, dtype=torch.float64, device=cuda), rel_tol=c["rel_tol"])
+        assert it32 <= c["iterations"] + 1
+
+
+def test_mg_solution_matches_oracle(tpss, oracle, xcheck, cuda):
+    import torch
+    dim, k, nrep, ncf = 2, 4, 2, 16
+    f = xcheck.bells_load_vector(dim, k, ncf)
+    it_ref, u_ref, _ = oracle.mg_cg_solve(dim, k, nrep, ncf, f, rel_tol=1e-10)
+    mg = tpss.MultigridSolver(dim, k, nrep, ncf)
+    u = torch.zeros(f.size, dtype=torch.float64, device=cuda)
+    it, _ = mg.solve(u, torch.tensor(f, dtype=torch.float64, device=cuda), rel_tol=1e-10)
+    assert it == it_ref
+    assert rel_err(u.cpu().numpy(), u_ref) <= 1e-9
+
+
+def test_full_size_config2_fp32_vs_oracle(tpss, oracle, cuda):
+    """3D DGQ4 on 64^3 cells (32.8M DoFs): the FP32 smoother against the FP64 oracle at full
+    size, plus linearity and symmetry of the GPU operator."""
+    import torch
+    dim, k, n = 3, 4, 64
+    N = n ** 3 * 125
+    src = philox(2024, N)
+    got, p = gpu_vmult(tpss, cuda, dim, k, (n, n, n), src, pv=1, omega=0.15, precision=1)
+    ref = oracle.schwarz_vmult(dim, k, (n, n, n), src, patch_variant=1, omega=0.15)
+    assert rel_err(got, ref) <= 2e-5
+    # linearity P(a x + b y) = a P x + b P y and symmetry y.Px = x.Py (FP64 smoother)
+    p64 = tpss.SchwarzPreconditioner()
+    p64.initialize(p.subdomain_handler, None, tpss.SchwarzPreconditioner.AdditionalData(relaxation=0.15))
+    x = torch.tensor(src, dtype=torch.float64, device=cuda)
+    y = torch.tensor(philox(2025, N), dtype=torch.float64, device=cuda)
+    Px, Py, Pz = torch.empty_like(x), torch.empty_like(x), torch.empty_like(x)
+    p64.vmult(Px, x)
+    p64.vmult(Py, y)
+    p64.vmult(Pz, 2.0 * x - 3.0 * y)
+    lin = (Pz - (2.0 * Px - 3.0 * Py)).abs().max().item() / Pz.abs().max().item()
+    assert lin <= 1e-12
+    sym = abs((y * Px).sum().item() - (x * Py).sum().item()) / abs((y * Px).sum().item())
+    assert sym <= 1e-10
+    assert rel_err(Px.cpu().numpy(), ref) <= 1e-12

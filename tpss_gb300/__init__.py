@@ -1,0 +1,427 @@
+"""tpss_gb300 -- GB300 (sm_103a) Schwarz smoother of TPSS behind its operator interface.
+
+Python mirror of the reference's smoother-path API (jwitte08/TPSS):
+
+  SubdomainHandler      SubdomainHandler<dim,Number>::reinit / AdditionalData
+                        (include/solvers_and_preconditioners/TPSS/subdomain_handler.h:33-262)
+  LaplaceOperator       MF::Operator (apps/laplace_integrator.h:396-786), matrix-free SIPG
+  SchwarzPreconditioner SchwarzPreconditioner<dim,OperatorType,VectorType,MatrixType>
+                        (preconditioner/schwarz_preconditioner.h:88-588)
+  SchwarzSmoother       SchwarzSmoother / SmootherRichardson
+                        (smoother/schwarz_smoother.h, smoother/smoother_richardson.h)
+  MultigridSolver       GMG V-cycle + CG of apps/poisson_problem.h:642-755
+
+Every call goes through the C ABI of include/tpss_gpu.h (libtpss_gpu.so, built in-tree);
+vectors are torch CUDA float64 tensors (or raw device pointers) and work is ordered on
+torch's current CUDA stream.  There is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import _lib
+from ._lib import (TPSS_ADDITIVE, TPSS_FP32, TPSS_FP64, TPSS_MULTIPLICATIVE, TPSS_PATCH_CELL,
+                   TPSS_PATCH_VERTEX, TPSSError, TPSSInvalidArgument, TPSSNotConverged,
+                   TPSSNotImplemented, check, load)
+
+__all__ = ["SubdomainHandler", "LaplaceOperator", "SchwarzPreconditioner", "SchwarzSmoother",
+           "MultigridSolver", "PatchVariant", "SmootherVariant", "Precision", "TimeInfo",
+           "lookup_damping_factor", "prolongate_add", "restrict_add", "TPSSError",
+           "TPSSNotImplemented", "TPSSInvalidArgument", "TPSSNotConverged", "load"]
+
+
+class PatchVariant:
+    """TPSS::PatchVariant"""
+    cell = TPSS_PATCH_CELL
+    vertex = TPSS_PATCH_VERTEX
+
+
+class SmootherVariant:
+    """TPSS::SmootherVariant"""
+    additive = TPSS_ADDITIVE
+    multiplicative = TPSS_MULTIPLICATIVE
+
+
+class Precision:
+    fp64 = TPSS_FP64
+    fp32 = TPSS_FP32
+
+
+def lookup_damping_factor(patch_variant: int, smoother_variant: int, dim: int) -> float:
+    """TPSS::lookup_damping_factor (include/solvers_and_preconditioners/TPSS/TPSS.h:121-163)."""
+    if smoother_variant == SmootherVariant.multiplicative:
+        return 1.0
+    if patch_variant == PatchVariant.cell:
+        return 0.7
+    if dim == 2:
+        return 0.25
+    if dim == 3:
+        return 0.15
+    raise ValueError("This case is not listed!")
+
+
+def _stream(stream):
+    if stream is not None:
+        return C.c_void_p(int(stream))
+    import torch
+    return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _ptr(x, n: Optional[int] = None, writable: bool = False):
+    """Device pointer of a torch CUDA float64 contiguous tensor (or an int address)."""
+    if isinstance(x, int):
+        return C.c_void_p(x)
+    import torch
+    if not isinstance(x, torch.Tensor):
+        raise TypeError("vectors must be torch CUDA tensors or device addresses")
+    if not x.is_cuda or x.dtype != torch.float64 or not x.is_contiguous():
+        raise TypeError("vectors must be contiguous float64 CUDA tensors")
+    if n is not None and x.numel() != n:
+        raise ValueError(f"vector has {x.numel()} entries, expected {n}")
+    return C.c_void_p(x.data_ptr())
+
+
+@dataclass
+class TimeInfo:
+    """TPSS::TimeInfo (include/solvers_and_preconditioners/TPSS/time_info.h:23-64)."""
+    time: float
+    description: str
+    unit: str = "[s]"
+    n_calls: int = 0
+
+
+class SubdomainHandler:
+    """Patch layout of one structured level (SubdomainHandler::reinit).
+
+    Vertex patches are gathered around interior vertices with their cells in lexicographic
+    order; colors follow the tiled coloring (vertex patches), one color (additive cell
+    patches) or red-black (multiplicative cell patches), or a user coloring.
+    """
+
+    @dataclass
+    class AdditionalData:
+        dim: int = 2
+        degree: int = 1
+        n_cells: Sequence[int] = (2, 2)
+        patch_variant: int = PatchVariant.vertex
+        smoother_variant: int = SmootherVariant.additive
+        level: int = 0
+        cell_h: Optional[Sequence[Sequence[float]]] = None
+        cell_dof_start: Optional[Sequence[int]] = None
+        coloring: Optional[Sequence[int]] = None  # user coloring in default patch order
+
+    def __init__(self, additional_data: Optional["SubdomainHandler.AdditionalData"] = None):
+        self._h = None
+        self.additional_data = None
+        if additional_data is not None:
+            self.reinit(additional_data)
+
+    def reinit(self, ad: "SubdomainHandler.AdditionalData"):
+        L = load()
+        self.clear()
+        d = _lib.LayoutDesc()
+        d.dim, d.degree, d.dof_layout = ad.dim, ad.degree, _lib.TPSS_DOF_DGQ
+        d.patch_variant, d.smoother_variant = ad.patch_variant, ad.smoother_variant
+        nc = list(ad.n_cells) + [1] * (3 - len(ad.n_cells))
+        for i in range(3):
+            d.n_cells[i] = int(nc[i])
+        keep = []
+        if ad.cell_h is not None:
+            for i, h in enumerate(ad.cell_h):
+                arr = np.ascontiguousarray(h, dtype=np.float64)
+                keep.append(arr)
+                d.cell_h[i] = arr.ctypes.data_as(C.POINTER(C.c_double))
+        if ad.cell_dof_start is not None:
+            cs = np.ascontiguousarray(ad.cell_dof_start, dtype=np.int64)
+            keep.append(cs)
+            d.cell_dof_start = cs.ctypes.data_as(C.POINTER(C.c_int64))
+        if ad.coloring is not None:
+            col = np.ascontiguousarray(ad.coloring, dtype=np.int32)
+            keep.append(col)
+            d.patch_color = col.ctypes.data_as(C.POINTER(C.c_int32))
+        h = C.c_void_p()
+        check(L.tpss_layout_create(C.byref(d), C.byref(h)))
+        self._h = h
+        self.additional_data = ad
+        n_dofs, n_patches, n_colors = C.c_int64(), C.c_int64(), C.c_int()
+        check(L.tpss_layout_info(h, C.byref(n_dofs), C.byref(n_patches), C.byref(n_colors)))
+        self._n_dofs, self._n_patches, self._n_colors = n_dofs.value, n_patches.value, n_colors.value
+
+    def clear(self):
+        if self._h:
+            load().tpss_layout_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.clear()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def n_dofs(self) -> int:
+        return self._n_dofs
+
+    def n_subdomains(self) -> int:
+        return self._n_patches
+
+    def n_colors(self) -> int:
+        return self._n_colors
+
+    def get_additional_data(self):
+        return self.additional_data
+
+    def patches(self):
+        """(lower cell coordinates [P,3], colors [P]) in storage order."""
+        P = self._n_patches
+        lower = np.zeros((max(P, 1), 3), dtype=np.int32)
+        col = np.zeros(max(P, 1), dtype=np.int32)
+        check(load().tpss_layout_patches(self._h, lower.ctypes.data_as(C.POINTER(C.c_int32)),
+                                         col.ctypes.data_as(C.POINTER(C.c_int32))))
+        return lower[:P], col[:P]
+
+
+class LaplaceOperator:
+    """Matrix-free SIPG operator of one level (MF::Operator, FP64)."""
+
+    def __init__(self, subdomain_handler: SubdomainHandler, ip_factor: float = 1.0):
+        self.subdomain_handler = subdomain_handler
+        h = C.c_void_p()
+        check(load().tpss_operator_create(subdomain_handler.handle, float(ip_factor), C.byref(h)))
+        self._h = h
+        self.ip_factor = ip_factor
+
+    def m(self):
+        return self.subdomain_handler.n_dofs()
+
+    n = m
+
+    def vmult(self, dst, src, stream=None):
+        n = self.m()
+        check(load().tpss_operator_vmult(self._h, _ptr(dst, n), _ptr(src, n), _stream(stream)))
+
+    def Tvmult(self, dst, src, stream=None):
+        self.vmult(dst, src, stream)
+
+    @property
+    def handle(self):
+        return self._h
+
+    def __del__(self):
+        try:
+            if self._h:
+                load().tpss_operator_destroy(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+
+class SchwarzPreconditioner:
+    """SchwarzPreconditioner: vmult(dst, src) sets dst = sum_j omega R_j^T A_j^-1 R_j src."""
+
+    @dataclass
+    class AdditionalData:
+        relaxation: float = 1.0
+        reverse: bool = False
+        symmetrized: bool = False
+        use_ras_weights: bool = False
+        use_ras_boolean_weights: bool = False
+        precision: int = Precision.fp64
+        ip_factor: float = 1.0
+        check_finite: bool = False
+
+    def __init__(self):
+        self._h = None
+        self.subdomain_handler = None
+        self.linear_operator = None
+        self.additional_data = None
+
+    @staticmethod
+    def _desc(ad):
+        d = _lib.PrecondDesc()
+        d.relaxation = float(ad.relaxation)
+        d.reverse, d.symmetrized = int(ad.reverse), int(ad.symmetrized)
+        d.use_ras_weights = int(ad.use_ras_weights)
+        d.use_ras_boolean_weights = int(ad.use_ras_boolean_weights)
+        d.precision, d.ip_factor = int(ad.precision), float(ad.ip_factor)
+        d.check_finite = int(ad.check_finite)
+        return d
+
+    def initialize(self, subdomain_handler, linear_operator=None, additional_data=None):
+        """initialize(subdomain_handler, operator, additional_data), or the shallow copy
+        initialize(other_preconditioner, additional_data)."""
+        if isinstance(subdomain_handler, SchwarzPreconditioner):
+            other, ad = subdomain_handler, linear_operator
+            self.clear()
+            h = C.c_void_p()
+            check(load().tpss_precond_create_shallow(other._h, C.byref(self._desc(ad)), C.byref(h)))
+            self._h = h
+            self.subdomain_handler = other.subdomain_handler
+            self.linear_operator = other.linear_operator
+            self.additional_data = ad
+            return
+        ad = additional_data or SchwarzPreconditioner.AdditionalData()
+        self.clear()
+        h = C.c_void_p()
+        op = linear_operator.handle if linear_operator is not None else None
+        check(load().tpss_precond_create(subdomain_handler.handle, op, C.byref(self._desc(ad)),
+                                         C.byref(h)))
+        self._h = h
+        self.subdomain_handler = subdomain_handler
+        self.linear_operator = linear_operator
+        self.additional_data = ad
+
+    def clear(self):
+        if self._h:
+            load().tpss_precond_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.clear()
+        except Exception:
+            pass
+
+    def get_additional_data(self):
+        return self.additional_data
+
+    def get_subdomain_handler(self):
+        return self.subdomain_handler
+
+    def m(self):
+        return self.subdomain_handler.n_dofs()
+
+    n = m
+
+    def vmult(self, dst, src, stream=None):
+        n = self.m()
+        check(load().tpss_precond_vmult(self._h, _ptr(dst, n), _ptr(src, n), _stream(stream)))
+
+    def vmult_add(self, dst, src, stream=None):
+        n = self.m()
+        check(load().tpss_precond_vmult_add(self._h, _ptr(dst, n), _ptr(src, n), _stream(stream)))
+
+    def Tvmult(self, dst, src, stream=None):
+        n = self.m()
+        check(load().tpss_precond_Tvmult(self._h, _ptr(dst, n), _ptr(src, n), _stream(stream)))
+
+    def get_time_data(self):
+        L = load()
+        n = C.c_int(0)
+        check(L.tpss_precond_time_info(self._h, None, C.byref(n)))
+        arr = (_lib.TimeInfo * n.value)()
+        check(L.tpss_precond_time_info(self._h, arr, C.byref(n)))
+        return [TimeInfo(a.time, a.description.decode(), "[s]", a.n_calls) for a in arr]
+
+    @property
+    def handle(self):
+        return self._h
+
+
+class SchwarzSmoother:
+    """SchwarzSmoother / SmootherRichardson: step(x, b) does x += damping P (b - A x)."""
+
+    @dataclass
+    class AdditionalData:
+        number_of_smoothing_steps: int = 1
+        damping_factor: float = 1.0
+
+    def __init__(self):
+        self._h = None
+
+    def initialize(self, linear_operator: LaplaceOperator, preconditioner: SchwarzPreconditioner,
+                   additional_data=None):
+        ad = additional_data or SchwarzSmoother.AdditionalData()
+        self.clear()
+        h = C.c_void_p()
+        check(load().tpss_smoother_create(linear_operator.handle, preconditioner.handle,
+                                          int(ad.number_of_smoothing_steps),
+                                          float(ad.damping_factor), C.byref(h)))
+        self._h = h
+        self.linear_operator = linear_operator
+        self.preconditioner = preconditioner
+        self.additional_data = ad
+
+    def step(self, dst, src, stream=None):
+        n = self.preconditioner.m()
+        check(load().tpss_smoother_step(self._h, _ptr(dst, n), _ptr(src, n), _stream(stream)))
+
+    def vmult(self, dst, src, stream=None):
+        n = self.preconditioner.m()
+        check(load().tpss_smoother_vmult(self._h, _ptr(dst, n), _ptr(src, n), _stream(stream)))
+
+    def clear(self):
+        if self._h:
+            load().tpss_smoother_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.clear()
+        except Exception:
+            pass
+
+
+class MultigridSolver:
+    """CG preconditioned by one GMG V-cycle with Schwarz smoothers on the unit cube."""
+
+    def __init__(self, dim, degree, n_rep, n_cells_fine, patch_variant=PatchVariant.vertex,
+                 smoother_variant=SmootherVariant.additive, relaxation=None, ip_factor=1.0,
+                 precision=Precision.fp64, coarse_tol=1e-12, coarse_solver=0, use_graph=True):
+        if relaxation is None:
+            relaxation = lookup_damping_factor(patch_variant, smoother_variant, dim)
+        d = _lib.MgDesc()
+        d.dim, d.degree, d.n_rep, d.n_cells_fine = dim, degree, n_rep, n_cells_fine
+        d.ip_factor, d.patch_variant, d.smoother_variant = float(ip_factor), patch_variant, smoother_variant
+        d.relaxation, d.precision, d.coarse_tol = float(relaxation), precision, float(coarse_tol)
+        d.coarse_solver, d.use_graph = int(coarse_solver), int(use_graph)
+        h = C.c_void_p()
+        check(load().tpss_mg_create(C.byref(d), C.byref(h)))
+        self._h = h
+        n = C.c_int64()
+        check(load().tpss_mg_n_dofs(h, C.byref(n)))
+        self._n = n.value
+        nl = C.c_int()
+        check(load().tpss_mg_n_levels(h, C.byref(nl)))
+        self.n_levels = nl.value
+
+    def n_dofs(self):
+        return self._n
+
+    def vmult(self, dst, src, stream=None):
+        check(load().tpss_mg_vmult(self._h, _ptr(dst, self._n), _ptr(src, self._n), _stream(stream)))
+
+    def solve(self, u, f, rel_tol=1e-8, abs_tol=1e-14, max_iter=100, stream=None):
+        """CG solve of A u = f; returns (iterations, residual history)."""
+        hist = np.zeros(max_iter + 1)
+        it = C.c_int(0)
+        code = load().tpss_mg_cg_solve(self._h, _ptr(u, self._n), _ptr(f, self._n), float(rel_tol),
+                                       float(abs_tol), int(max_iter), C.byref(it),
+                                       hist.ctypes.data_as(C.POINTER(C.c_double)), _stream(stream))
+        check(code)
+        return it.value, hist[: it.value + 1]
+
+    def __del__(self):
+        try:
+            if self._h:
+                load().tpss_mg_destroy(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+
+def prolongate_add(dim, degree, n_cells_coarse, fine, coarse, stream=None):
+    nc = (C.c_int * 3)(*(list(n_cells_coarse) + [1] * (3 - len(n_cells_coarse))))
+    check(load().tpss_transfer_prolongate_add(dim, degree, nc, _ptr(fine), _ptr(coarse), _stream(stream)))
+
+
+def restrict_add(dim, degree, n_cells_coarse, coarse, fine, stream=None):
+    nc = (C.c_int * 3)(*(list(n_cells_coarse) + [1] * (3 - len(n_cells_coarse))))
+    check(load().tpss_transfer_restrict_add(dim, degree, nc, _ptr(coarse), _ptr(fine), _stream(stream)))

@@ -1,0 +1,322 @@
+// fd_kernels.cuh -- fused per-color Schwarz kernel: gather -> FD inverse -> damping -> scatter.
+//
+// One color of SchwarzPreconditioner::apply_local_solvers
+// (preconditioner/schwarz_preconditioner.templates.h:585-662) for DG patches:
+//   r_j = R_j src            PatchTransfer::gather (TPSS/patch_transfer.templates.h:3-23)
+//   u_j = A_j^-1 r_j          TensorProductMatrixSymmetricSum::apply_inverse (deal.II),
+//                            u = S Lambda^-1 S^T r with S = S_{d-1} x .. x S_0
+//   u_j *= omega             (schwarz_preconditioner.templates.h:631-633)
+//   dst += R_j^T u_j          PatchTransfer::scatter_add (patch_transfer.templates.h:54-116)
+// Patches of one color share no cell, so the scatter is a plain read-modify-write.
+//
+// Mapping: a CTA holds PPC patches in shared memory (patch-local lexicographic order,
+// direction 0 fastest).  Gather/scatter move whole cells: each cell's (k+1)^d DoFs are
+// contiguous in the global vector, so consecutive threads touch consecutive doubles.
+// The sum-factorized contractions run pencil-wise: a thread owns one 1-D pencil of a patch,
+// keeps it in registers, and contracts it against the 1-D matrix held in shared memory (rows
+// read as 16-byte vectors that all lanes of a warp share).  The last forward direction, the
+// division by the eigenvalue sums and the first backward direction are fused in registers.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace tpss
+{
+namespace fd
+{
+template<typename T>
+struct VecOf;
+template<>
+struct VecOf<float>
+{
+  using type = float4;
+  static constexpr int W = 4;
+};
+template<>
+struct VecOf<double>
+{
+  using type = double2;
+  static constexpr int W = 2;
+};
+
+__host__ __device__ constexpr int cpow(int b, int e) { return e == 0 ? 1 : b * cpow(b, e - 1); }
+
+template<typename T, int N>
+struct Pad
+{
+  static constexpr int W = VecOf<T>::W;
+  static constexpr int value = ((N + W - 1) / W) * W;
+};
+
+// o[i] = sum_m B[i][m] r[m], B row-major N x NPAD in shared memory.
+template<typename T, int N, int NPAD>
+__device__ __forceinline__ void rowmat(const T *__restrict__ B, const T (&r)[N], T (&o)[N])
+{
+  using V = typename VecOf<T>::type;
+  constexpr int W = VecOf<T>::W;
+#pragma unroll
+  for(int i = 0; i < N; ++i)
+  {
+    const V *row = reinterpret_cast<const V *>(B + i * NPAD);
+    T acc = T(0);
+#pragma unroll
+    for(int m4 = 0; m4 < NPAD / W; ++m4)
+    {
+      const V v = row[m4];
+      if constexpr(W == 4)
+      {
+        if(m4 * 4 + 0 < N) acc = fma(v.x, r[m4 * 4 + 0 < N ? m4 * 4 + 0 : 0], acc);
+        if(m4 * 4 + 1 < N) acc = fma(v.y, r[m4 * 4 + 1 < N ? m4 * 4 + 1 : 0], acc);
+        if(m4 * 4 + 2 < N) acc = fma(v.z, r[m4 * 4 + 2 < N ? m4 * 4 + 2 : 0], acc);
+        if(m4 * 4 + 3 < N) acc = fma(v.w, r[m4 * 4 + 3 < N ? m4 * 4 + 3 : 0], acc);
+      }
+      else
+      {
+        if(m4 * 2 + 0 < N) acc = fma(v.x, r[m4 * 2 + 0 < N ? m4 * 2 + 0 : 0], acc);
+        if(m4 * 2 + 1 < N) acc = fma(v.y, r[m4 * 2 + 1 < N ? m4 * 2 + 1 : 0], acc);
+      }
+    }
+    o[i] = acc;
+  }
+}
+
+// Per-entry layout of the FD table: [S^T: N x NPAD][S: N x NPAD][lambda: NPAD].
+template<typename T, int N>
+struct Entry
+{
+  static constexpr int NPAD = Pad<T, N>::value;
+  static constexpr int ST = 0, S = N * NPAD, LAM = 2 * N * NPAD;
+  static constexpr int size = (2 * N + 1) * NPAD;
+};
+
+template<typename T, int DIM, int NCP, int K1>
+struct Cfg
+{
+  static constexpr int N = NCP * K1;
+  static constexpr int NLOC = cpow(N, DIM);
+  static constexpr int NPENCIL = NLOC / N;
+  static constexpr int NCELL = cpow(NCP, DIM);
+  static constexpr int CELLDOFS = cpow(K1, DIM);
+  static constexpr int ESIZE = Entry<T, N>::size;
+  // patches per CTA: enough pencils for >= 128 threads, bounded by shared memory
+  static constexpr int PPC_WANT = NPENCIL >= 128 ? 1 : (128 + NPENCIL - 1) / NPENCIL;
+  static constexpr int SLOT_BYTES = NLOC * sizeof(T) + DIM * ESIZE * sizeof(T) + NCELL * 12;
+  static constexpr int PPC_MEM = (96 * 1024) / SLOT_BYTES > 0 ? (96 * 1024) / SLOT_BYTES : 1;
+  static constexpr int PPC = PPC_WANT < PPC_MEM ? PPC_WANT : PPC_MEM;
+  static constexpr int THREADS = ((PPC * NPENCIL + 31) / 32) * 32 < 64 ? 64 : ((PPC * NPENCIL + 31) / 32) * 32;
+  // shared memory carve-up (byte offsets, each 16-byte aligned)
+  static constexpr size_t al16(size_t x) { return (x + 15) / 16 * 16; }
+  static constexpr size_t OFF_FD = 0;
+  static constexpr size_t OFF_FIRST = al16(OFF_FD + (size_t)PPC * DIM * ESIZE * sizeof(T));
+  static constexpr size_t OFF_W = al16(OFF_FIRST + (size_t)PPC * NCELL * 8);
+  static constexpr size_t OFF_DATA = al16(OFF_W + (size_t)PPC * NCELL * 4);
+  static constexpr size_t smem_bytes() { return al16(OFF_DATA + (size_t)PPC * NLOC * sizeof(T)); }
+};
+
+// patch-local index of DoF e of patch cell cn
+template<int DIM, int NCP, int K1>
+__device__ __forceinline__ int patch_index(int cn, int e)
+{
+  constexpr int N = NCP * K1;
+  int idx = 0, stride = 1;
+#pragma unroll
+  for(int d = 0; d < DIM; ++d)
+  {
+    const int cd = NCP == 1 ? 0 : (cn % NCP);
+    const int id = e % K1;
+    cn /= NCP;
+    e /= K1;
+    idx += (cd * K1 + id) * stride;
+    stride *= N;
+  }
+  return idx;
+}
+
+// pencil base offset and stride for direction DIR
+template<int DIM, int N, int DIR>
+__device__ __forceinline__ int pencil_base(int p)
+{
+  constexpr int stride = cpow(N, DIR);
+  return (p % stride) + (p / stride) * stride * N;
+}
+
+template<typename T, int DIM, int N, int DIR, bool TRANSPOSED>
+__device__ __forceinline__ void pass(T *__restrict__ data, const T *__restrict__ entry, int p,
+                                     T scale)
+{
+  constexpr int NPAD = Entry<T, N>::NPAD;
+  constexpr int stride = cpow(N, DIR);
+  const int base = pencil_base<DIM, N, DIR>(p);
+  T r[N], o[N];
+#pragma unroll
+  for(int m = 0; m < N; ++m) r[m] = data[base + m * stride];
+  rowmat<T, N, NPAD>(entry + (TRANSPOSED ? Entry<T, N>::ST : Entry<T, N>::S), r, o);
+#pragma unroll
+  for(int i = 0; i < N; ++i) data[base + i * stride] = o[i] * scale;
+}
+
+// last direction: S^T along DIM-1, divide by sum of eigenvalues, S along DIM-1
+template<typename T, int DIM, int N>
+__device__ __forceinline__ void pass_last(T *__restrict__ data, const T *__restrict__ entries,
+                                          int p)
+{
+  constexpr int NPAD = Entry<T, N>::NPAD;
+  constexpr int ES = Entry<T, N>::size;
+  constexpr int DIR = DIM - 1;
+  constexpr int stride = cpow(N, DIR);
+  const int base = pencil_base<DIM, N, DIR>(p);
+  T r[N], o[N];
+#pragma unroll
+  for(int m = 0; m < N; ++m) r[m] = data[base + m * stride];
+  const T *eL = entries + DIR * ES;
+  rowmat<T, N, NPAD>(eL + Entry<T, N>::ST, r, o);
+  // eigenvalue sum of the other directions (p enumerates i_0 [+ N i_1])
+  T lsum = T(0);
+  {
+    int rem = p;
+#pragma unroll
+    for(int d = 0; d < DIM - 1; ++d)
+    {
+      lsum += entries[d * ES + Entry<T, N>::LAM + rem % N];
+      rem /= N;
+    }
+  }
+#pragma unroll
+  for(int i = 0; i < N; ++i) o[i] = o[i] / (lsum + eL[Entry<T, N>::LAM + i]);
+  rowmat<T, N, NPAD>(eL + Entry<T, N>::S, o, r);
+#pragma unroll
+  for(int i = 0; i < N; ++i) data[base + i * stride] = r[i];
+}
+
+struct KernelArgs
+{
+  const double *__restrict__ src;
+  double *__restrict__ dst;
+  const int64_t *__restrict__ patch_first;
+  const int32_t *__restrict__ patch_fd;
+  const void *__restrict__ fd;
+  const float *__restrict__ ras_w;
+  int64_t n_patches;
+  double omega;
+  int entry_stride;
+};
+
+template<typename T, int DIM, int NCP, int K1>
+__global__ void __launch_bounds__(Cfg<T, DIM, NCP, K1>::THREADS)
+  schwarz_color_kernel(KernelArgs a)
+{
+  using C = Cfg<T, DIM, NCP, K1>;
+  constexpr int N = C::N, NLOC = C::NLOC, PPC = C::PPC, NCELL = C::NCELL;
+  constexpr int CELLDOFS = C::CELLDOFS, ES = C::ESIZE;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T *s_fd = reinterpret_cast<T *>(smem_raw + C::OFF_FD);             // PPC * DIM * ES
+  int64_t *s_first = reinterpret_cast<int64_t *>(smem_raw + C::OFF_FIRST);  // PPC * NCELL
+  float *s_w = reinterpret_cast<float *>(smem_raw + C::OFF_W);          // PPC * NCELL
+  T *s_data = reinterpret_cast<T *>(smem_raw + C::OFF_DATA);           // PPC * NLOC
+
+  const T *fd = reinterpret_cast<const T *>(a.fd);
+  const int tid = threadIdx.x;
+  const int slot = tid / C::NPENCIL, pencil = tid % C::NPENCIL;
+  const T omega = T(a.omega);
+
+  for(int64_t p0 = (int64_t)blockIdx.x * PPC; p0 < a.n_patches; p0 += (int64_t)gridDim.x * PPC)
+  {
+    const int64_t left = a.n_patches - p0;
+    const int nvalid = left < PPC ? (int)left : PPC;
+    // --- patch metadata and the 1-D eigenbases
+    for(int i = tid; i < PPC * NCELL; i += C::THREADS)
+    {
+      const int s = i / NCELL;
+      if(s < nvalid)
+      {
+        s_first[i] = a.patch_first[p0 * NCELL + i];
+        s_w[i] = a.ras_w ? a.ras_w[p0 * NCELL + i] : 1.0f;
+      }
+    }
+    for(int i = tid; i < PPC * DIM * ES; i += C::THREADS)
+    {
+      const int sd = i / ES, s = sd / DIM;
+      if(s < nvalid)
+      {
+        const int e = a.patch_fd[p0 * DIM + sd];
+        s_fd[i] = fd[(size_t)e * a.entry_stride + (i % ES)];
+      }
+    }
+    __syncthreads();
+    // --- gather: whole cells, coalesced
+    for(int i = tid; i < PPC * NCELL * CELLDOFS; i += C::THREADS)
+    {
+      const int s = i / (NCELL * CELLDOFS);
+      const int rem = i % (NCELL * CELLDOFS);
+      const int cn = rem / CELLDOFS, e = rem % CELLDOFS;
+      if(s < nvalid)
+        s_data[s * NLOC + patch_index<DIM, NCP, K1>(cn, e)] = T(a.src[s_first[s * NCELL + cn] + e]);
+    }
+    __syncthreads();
+    const bool active = slot < nvalid;
+    T *my = s_data + slot * NLOC;
+    const T *ent = s_fd + slot * DIM * ES;
+    // --- forward S^T along directions 0..DIM-2
+    if(active) pass<T, DIM, N, 0, true>(my, ent + 0 * ES, pencil, T(1));
+    __syncthreads();
+    if constexpr(DIM == 3)
+    {
+      if(active) pass<T, DIM, N, 1, true>(my, ent + 1 * ES, pencil, T(1));
+      __syncthreads();
+    }
+    // --- last direction fused with the eigenvalue division
+    if(active) pass_last<T, DIM, N>(my, ent, pencil);
+    __syncthreads();
+    // --- backward S along directions DIM-2..0, damping folded into direction 0
+    if constexpr(DIM == 3)
+    {
+      if(active) pass<T, DIM, N, 1, false>(my, ent + 1 * ES, pencil, T(1));
+      __syncthreads();
+    }
+    if(active) pass<T, DIM, N, 0, false>(my, ent + 0 * ES, pencil, omega);
+    __syncthreads();
+    // --- scatter-add: whole cells, coalesced read-modify-write
+    for(int i = tid; i < PPC * NCELL * CELLDOFS; i += C::THREADS)
+    {
+      const int s = i / (NCELL * CELLDOFS);
+      const int rem = i % (NCELL * CELLDOFS);
+      const int cn = rem / CELLDOFS, e = rem % CELLDOFS;
+      if(s < nvalid)
+      {
+        const int64_t g = s_first[s * NCELL + cn] + e;
+        const double v = double(s_data[s * NLOC + patch_index<DIM, NCP, K1>(cn, e)]);
+        a.dst[g] += a.ras_w ? v * double(s_w[s * NCELL + cn]) : v;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+template<typename T, int DIM, int NCP, int K1>
+bool launch(const KernelArgs &a, cudaStream_t s, int n_sms)
+{
+  using C = Cfg<T, DIM, NCP, K1>;
+  const size_t smem = C::smem_bytes();
+  static int per_sm = 0;  // occupancy, queried once per instantiation
+  if(per_sm == 0)
+  {
+    if(cudaFuncSetAttribute(schwarz_color_kernel<T, DIM, NCP, K1>,
+                            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+      return false;
+    int occ = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, schwarz_color_kernel<T, DIM, NCP, K1>,
+                                                  C::THREADS, smem);
+    per_sm = occ < 1 ? 1 : occ;
+  }
+  if(a.n_patches <= 0) return true;
+  const int64_t batches = (a.n_patches + C::PPC - 1) / C::PPC;
+  const int64_t cap = (int64_t)n_sms * per_sm * 8;
+  const int grid = (int)(batches < cap ? batches : cap);
+  schwarz_color_kernel<T, DIM, NCP, K1><<<grid, C::THREADS, smem, s>>>(a);
+  return cudaGetLastError() == cudaSuccess;
+}
+
+}  // namespace fd
+}  // namespace tpss

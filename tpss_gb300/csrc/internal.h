@@ -1,0 +1,274 @@
+// internal.h -- structures shared by the translation units of libtpss_gpu.so.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/tpss_gpu.h"
+
+namespace tpss
+{
+// ------------------------------------------------------------------------------------------
+// status handling: every C entry point catches tpss::Error and returns its code
+// ------------------------------------------------------------------------------------------
+struct Error
+{
+  int code;
+  std::string msg;
+};
+
+void set_last_error(const std::string &msg);
+
+[[noreturn]] inline void fail(int code, const std::string &msg) { throw Error{code, msg}; }
+
+#define TPSS_CUDA(call)                                                                     \
+  do                                                                                        \
+  {                                                                                         \
+    cudaError_t e_ = (call);                                                                \
+    if(e_ != cudaSuccess)                                                                   \
+      ::tpss::fail(e_ == cudaErrorMemoryAllocation ? TPSS_ERR_OUT_OF_MEMORY : TPSS_ERR_CUDA, \
+                   std::string(#call) + ": " + cudaGetErrorString(e_));                     \
+  } while(0)
+
+#define TPSS_REQUIRE(cond, msg)                                    \
+  do                                                               \
+  {                                                                \
+    if(!(cond)) ::tpss::fail(TPSS_ERR_INVALID_ARGUMENT, (msg));    \
+  } while(0)
+
+template<typename F>
+int guarded(F &&f)
+{
+  try
+  {
+    f();
+    return TPSS_OK;
+  }
+  catch(const Error &e)
+  {
+    set_last_error(e.msg);
+    return e.code;
+  }
+  catch(const std::bad_alloc &)
+  {
+    set_last_error("host allocation failed");
+    return TPSS_ERR_OUT_OF_MEMORY;
+  }
+  catch(const std::exception &e)
+  {
+    set_last_error(e.what());
+    return TPSS_ERR_STATE;
+  }
+}
+
+// device buffer with RAII
+template<typename T>
+struct DeviceBuffer
+{
+  T *ptr = nullptr;
+  size_t n = 0;
+  DeviceBuffer() = default;
+  explicit DeviceBuffer(size_t count) { resize(count); }
+  DeviceBuffer(const DeviceBuffer &) = delete;
+  DeviceBuffer &operator=(const DeviceBuffer &) = delete;
+  DeviceBuffer(DeviceBuffer &&o) noexcept : ptr(o.ptr), n(o.n)
+  {
+    o.ptr = nullptr;
+    o.n = 0;
+  }
+  DeviceBuffer &operator=(DeviceBuffer &&o) noexcept
+  {
+    if(this != &o)
+    {
+      release();
+      ptr = o.ptr;
+      n = o.n;
+      o.ptr = nullptr;
+      o.n = 0;
+    }
+    return *this;
+  }
+  ~DeviceBuffer() { release(); }
+  void resize(size_t count)
+  {
+    release();
+    if(count)
+    {
+      TPSS_CUDA(cudaMalloc(&ptr, count * sizeof(T)));
+      n = count;
+    }
+  }
+  void upload(const T *host, size_t count)
+  {
+    resize(count);
+    if(count) TPSS_CUDA(cudaMemcpy(ptr, host, count * sizeof(T), cudaMemcpyHostToDevice));
+  }
+  void release()
+  {
+    if(ptr) cudaFree(ptr);
+    ptr = nullptr;
+    n = 0;
+  }
+};
+
+inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
+
+inline int ipow(int b, int e)
+{
+  int r = 1;
+  while(e-- > 0) r *= b;
+  return r;
+}
+
+int num_sms();
+
+// ------------------------------------------------------------------------------------------
+// host-side 1-D finite element data (setup.cu)
+// ------------------------------------------------------------------------------------------
+struct Shape1D
+{
+  int k = 0, np = 1;
+  std::vector<double> qx, qw, nodes;
+  std::vector<double> val, grad;        // [i*np + q]
+  std::vector<double> fval[2], fgrad[2];  // at x=0 and x=1
+};
+Shape1D make_shape_1d(int k);
+// 1-D DG patch matrices of the FD local solver (ncp = 1 or 2 cells)
+void patch_matrices_1d(const Shape1D &s, int ncp, const double *h, bool bdry_lo, bool bdry_hi,
+                       double ip, double *M, double *A);
+// global 1-D SIPG blocks of one direction: mass[c][np^2], blk[c][3][np^2]
+void operator_blocks_1d(const Shape1D &s, int nc, const double *h, double ip,
+                        std::vector<double> &mass, std::vector<double> &blk);
+// child embedding E[s][i*np+j] = phi_j((z_i+s)/2)
+std::vector<double> embedding_1d(const Shape1D &s);
+
+// ------------------------------------------------------------------------------------------
+// layout
+// ------------------------------------------------------------------------------------------
+}  // namespace tpss
+
+struct tpss_layout
+{
+  int dim = 0, k = 0, np = 0, patch_variant = 0, smoother_variant = 0;
+  int ncp = 0;        // cells per patch per direction
+  int n = 0;          // 1-D patch size
+  int nloc = 0;       // n^dim
+  int npc = 0;        // cells per patch
+  int cell_dofs = 0;  // (k+1)^dim
+  int nc[3] = {1, 1, 1};
+  std::vector<double> h[3];
+  int64_t n_cells = 0, n_dofs = 0;
+  bool lexicographic = true;
+  std::vector<int64_t> cell_start;  // host
+  int64_t P = 0;
+  int n_colors = 0;
+  std::vector<int64_t> color_start;  // n_colors + 1
+  std::vector<int32_t> lower, color; // host, P*3 and P
+  std::vector<int32_t> patch_fd_key; // host: P*dim indices into fd_keys
+  struct FdKey
+  {
+    double h0, h1;
+    int lo, hi;
+  };
+  std::vector<FdKey> fd_keys;
+  std::vector<int32_t> cell_multiplicity;  // number of patches covering each cell
+  std::vector<int64_t> patch_first;           // host: P*npc first DoF of each patch cell
+  std::mutex device_mutex;
+  bool on_device = false;
+  tpss::DeviceBuffer<int64_t> d_patch_first;  // P*npc first DoF of each patch cell
+  tpss::DeviceBuffer<int32_t> d_patch_fd;     // P*dim
+  tpss::DeviceBuffer<int64_t> d_cell_start;   // n_cells (empty when lexicographic)
+};
+
+struct tpss_operator
+{
+  const tpss_layout *layout = nullptr;
+  double ip = 1.0;
+  tpss::DeviceBuffer<double> d_mass[3], d_blk[3];
+  int nblk_cells[3] = {0, 0, 0};
+};
+
+namespace tpss
+{
+// FD tables of a preconditioner (shared between shallow copies)
+struct FdTables
+{
+  const tpss_layout *layout = nullptr;
+  int n = 0, n_entries = 0;
+  int npad32 = 0, npad64 = 0;
+  DeviceBuffer<double> fd64;  // entries: [St n*npad][S n*npad][lam npad]
+  DeviceBuffer<float> fd32;
+  std::vector<double> S_host, lam_host;  // n_entries * n*n, n_entries * n (FP64 results)
+  double setup_seconds = 0.0;
+  DeviceBuffer<float> ras_w;  // P*npc weights (1/multiplicity) when RAS is used
+};
+
+struct TimerSlot
+{
+  double time = 0.0;
+  int64_t n_calls = 0;
+  const char *name = "";
+};
+
+struct PendingEvent
+{
+  cudaEvent_t start, stop;
+  int slot;
+};
+
+}  // namespace tpss
+
+struct tpss_precond
+{
+  std::shared_ptr<tpss::FdTables> tables;
+  tpss_operator *op = nullptr;
+  tpss_precond_desc desc{};
+  tpss::DeviceBuffer<double> residual;  // multiplicative scratch
+  tpss::DeviceBuffer<int> flag;         // finiteness check
+  std::vector<tpss::TimerSlot> timers;
+  std::vector<tpss::PendingEvent> pending;
+  std::vector<cudaEvent_t> event_pool;
+};
+
+namespace tpss
+{
+// FD kernel launch (fd_kernels_*.cu). Returns false when (dim, k, ncp) is not instantiated.
+struct FdLaunch
+{
+  const double *src;
+  double *dst;
+  const int64_t *patch_first;  // first patch of the range
+  const int32_t *patch_fd;     // first patch of the range
+  const void *fd;              // table of the precision
+  const float *ras_w;          // nullptr or first patch of the range
+  int64_t n_patches;
+  double omega;
+  int entry_stride;            // elements per table entry
+};
+bool launch_fd_f32(int dim, int k, int ncp, const FdLaunch &a, cudaStream_t s);
+bool launch_fd_f64(int dim, int k, int ncp, const FdLaunch &a, cudaStream_t s);
+
+// operator and transfer (operator.cu)
+void operator_apply(tpss_operator *op, double *dst, const double *src, cudaStream_t s);
+void transfer_apply(int dim, int k, const int *ncc, const double *E_dev, bool restrict_mode,
+                    double *coarse, double *fine, cudaStream_t s);
+
+// vector kernels (operator.cu)
+void vec_axpby(int64_t n, double a, const double *x, double b, double *y, cudaStream_t s);  // y = a x + b y
+void vec_sub(int64_t n, const double *a, double *y, cudaStream_t s);  // y = a - y
+// dot products: partial sums into `partial` (device, >= dot_partials()), final into out (device)
+int dot_partials();
+void vec_dot(int64_t n, const double *x, const double *y, double *partial, double *out,
+             cudaStream_t s);
+
+// upload the layout's index tables (layout.cu)
+void layout_to_device(const tpss_layout &L);
+
+// preconditioner internals (precond.cu)
+void precond_vmult(tpss_precond *p, double *dst, const double *src, cudaStream_t s);
+}  // namespace tpss

@@ -1,0 +1,534 @@
+// mg.cu -- geometric multigrid V-cycle and the preconditioned CG outer solver (FP64).
+//
+// Follows the solver stack the Schwarz smoother runs in (apps/poisson_problem.h:642-755,
+// apps/multigrid.h:137-399) with deal.II Multigrid::level_v_step semantics:
+//   level l > 0:  x_l = P_l b_l                          (pre-smoothing from zero:
+//                                                       SmootherRichardson::vmult with one step)
+//                 b_{l-1} = R (b_l - A_l x_l)
+//                 V-cycle on l-1
+//                 x_l += P x_{l-1}
+//                 x_l += P_l (b_l - A_l x_l)           (post-smoothing step)
+//   level 0:      coarse solve (CG to an absolute residual, or the dense inverse).
+// Outer solver: SolverCG with the V-cycle as preconditioner and ReductionControl
+// (stop at ||r|| <= max(abs_tol, rel_tol ||r_0||)).
+// The V-cycle can be captured in CUDA graphs: with the dense coarse solver the whole cycle is
+// one graph launch; with the CG coarse solver the down- and up-sweeps are two graphs around
+// the host-driven coarse iteration.
+#include <cmath>
+#include <cstring>
+
+#include "internal.h"
+
+namespace tpss
+{
+const double *embedding_table(int k);
+
+namespace
+{
+__global__ void cg_update_xr(int64_t n, double *__restrict__ x, double *__restrict__ r,
+                             const double *__restrict__ p, const double *__restrict__ Ap,
+                             const double *__restrict__ rz, const double *__restrict__ pAp)
+{
+  const double alpha = *rz / *pAp;
+  for(int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+  {
+    x[i] = fma(alpha, p[i], x[i]);
+    r[i] = fma(-alpha, Ap[i], r[i]);
+  }
+}
+
+__global__ void cg_update_p(int64_t n, double *__restrict__ p, const double *__restrict__ z,
+                            const double *__restrict__ rz_new, const double *__restrict__ rz_old)
+{
+  const double beta = *rz_new / *rz_old;
+  for(int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    p[i] = fma(beta, p[i], z[i]);
+}
+
+__global__ void dense_matvec(int n, const double *__restrict__ A, const double *__restrict__ x,
+                             double *__restrict__ y)
+{
+  // one warp per row
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) / 32, lane = threadIdx.x % 32;
+  if(warp >= n) return;
+  double s = 0.0;
+  for(int j = lane; j < n; j += 32) s = fma(A[(size_t)warp * n + j], x[j], s);
+  for(int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if(lane == 0) y[warp] = s;
+}
+
+int grid_for(int64_t n)
+{
+  const int64_t b = (n + 255) / 256, cap = (int64_t)num_sms() * 8;
+  return (int)(b < cap ? (b > 0 ? b : 1) : cap);
+}
+
+// Dense SIPG matrix of a small structured level (Kronecker sum of the global 1-D operators)
+// and its inverse by Cholesky, both FP64 on the host.
+std::vector<double> dense_inverse(const tpss_layout &L, double ip)
+{
+  const Shape1D s = make_shape_1d(L.k);
+  const int np = L.np, dim = L.dim;
+  std::vector<std::vector<double>> M1(dim), A1(dim);
+  std::vector<int> n1(dim);
+  for(int d = 0; d < dim; ++d)
+  {
+    std::vector<double> mass, blk;
+    operator_blocks_1d(s, L.nc[d], L.h[d].data(), ip, mass, blk);
+    const int n = L.nc[d] * np;
+    n1[d] = n;
+    M1[d].assign((size_t)n * n, 0.0);
+    A1[d].assign((size_t)n * n, 0.0);
+    for(int c = 0; c < L.nc[d]; ++c)
+      for(int i = 0; i < np; ++i)
+        for(int j = 0; j < np; ++j)
+        {
+          M1[d][(size_t)(c * np + i) * n + c * np + j] = mass[(size_t)c * np * np + i * np + j];
+          for(int o = -1; o <= 1; ++o)
+          {
+            const int cn = c + o;
+            if(cn < 0 || cn >= L.nc[d]) continue;
+            A1[d][(size_t)(c * np + i) * n + cn * np + j] =
+              blk[((size_t)c * 3 + o + 1) * np * np + i * np + j];
+          }
+        }
+  }
+  const int64_t N = L.n_dofs;
+  std::vector<double> A((size_t)N * N, 0.0);
+  // global index of (cell multi-index, dof multi-index) in the layout's numbering
+  auto gidx = [&](const int *pos) -> int64_t {
+    int c[3] = {0, 0, 0}, e = 0, stride = 1;
+    for(int d = 0; d < dim; ++d)
+    {
+      c[d] = pos[d] / np;
+      e += (pos[d] % np) * stride;
+      stride *= np;
+    }
+    const int64_t cell = c[0] + (int64_t)L.nc[0] * (c[1] + (int64_t)L.nc[1] * c[2]);
+    return L.cell_start[cell] + e;
+  };
+  int pr[3] = {0, 0, 0}, pc[3] = {0, 0, 0};
+  const int n0 = n1[0], n1d = dim > 1 ? n1[1] : 1, n2 = dim > 2 ? n1[2] : 1;
+  for(pr[2] = 0; pr[2] < n2; ++pr[2])
+    for(pr[1] = 0; pr[1] < n1d; ++pr[1])
+      for(pr[0] = 0; pr[0] < n0; ++pr[0])
+      {
+        const int64_t row = gidx(pr);
+        for(pc[2] = 0; pc[2] < n2; ++pc[2])
+          for(pc[1] = 0; pc[1] < n1d; ++pc[1])
+            for(pc[0] = 0; pc[0] < n0; ++pc[0])
+            {
+              double v = 0.0;
+              for(int d = 0; d < dim; ++d)
+              {
+                double t = 1.0;
+                for(int e = 0; e < dim; ++e)
+                {
+                  const auto &B = e == d ? A1[e] : M1[e];
+                  t *= B[(size_t)pr[e] * n1[e] + pc[e]];
+                  if(t == 0.0) break;
+                }
+                v += t;
+              }
+              if(v != 0.0) A[(size_t)row * N + gidx(pc)] = v;
+            }
+      }
+  // Cholesky A = G G^T (lower), then A^-1 = G^-T G^-1
+  std::vector<double> G(A);
+  for(int64_t j = 0; j < N; ++j)
+  {
+    double d = G[(size_t)j * N + j];
+    for(int64_t p = 0; p < j; ++p) d -= G[(size_t)j * N + p] * G[(size_t)j * N + p];
+    if(!(d > 0.0)) fail(TPSS_ERR_INVALID_ARGUMENT, "coarse matrix is not positive definite");
+    const double gjj = std::sqrt(d);
+    G[(size_t)j * N + j] = gjj;
+    for(int64_t i = j + 1; i < N; ++i)
+    {
+      double t = G[(size_t)i * N + j];
+      const double *gi = &G[(size_t)i * N], *gj = &G[(size_t)j * N];
+      for(int64_t p = 0; p < j; ++p) t -= gi[p] * gj[p];
+      G[(size_t)i * N + j] = t / gjj;
+    }
+  }
+  // Ginv (lower) by forward substitution, then Ainv = Ginv^T Ginv
+  std::vector<double> Gi((size_t)N * N, 0.0);
+  for(int64_t c = 0; c < N; ++c)
+    for(int64_t i = c; i < N; ++i)
+    {
+      double t = i == c ? 1.0 : 0.0;
+      for(int64_t p = c; p < i; ++p) t -= G[(size_t)i * N + p] * Gi[(size_t)p * N + c];
+      Gi[(size_t)i * N + c] = t / G[(size_t)i * N + i];
+    }
+  std::vector<double> Ainv((size_t)N * N, 0.0);
+  for(int64_t i = 0; i < N; ++i)
+    for(int64_t j = 0; j <= i; ++j)
+    {
+      double t = 0.0;
+      for(int64_t p = i; p < N; ++p) t += Gi[(size_t)p * N + i] * Gi[(size_t)p * N + j];
+      Ainv[(size_t)i * N + j] = t;
+      Ainv[(size_t)j * N + i] = t;
+    }
+  return Ainv;
+}
+}  // namespace
+}  // namespace tpss
+
+using namespace tpss;
+
+struct MgLevel
+{
+  tpss_layout *L = nullptr;
+  tpss_operator *op = nullptr;
+  tpss_precond *P = nullptr;
+  DeviceBuffer<double> x, b, t, r;
+};
+
+struct tpss_mg
+{
+  tpss_mg_desc desc{};
+  std::vector<MgLevel> lv;
+  DeviceBuffer<double> coarse_inv;
+  // coarse CG and outer CG work vectors and device scalars
+  DeviceBuffer<double> cp, cAp, partial, scal;  // scal: [rz, pAp, rz_new, rr, ...]
+  DeviceBuffer<double> r, p, Ap, z;
+  double *h_scal = nullptr;  // pinned
+  const double *E = nullptr;
+  cudaGraphExec_t g_full = nullptr, g_down = nullptr, g_up = nullptr;
+  // graphs are captured on and launched into a private stream (capture is not possible on
+  // the legacy default stream); events order it after / before the caller's stream
+  cudaStream_t gstream = nullptr;
+  cudaEvent_t ev_in = nullptr, ev_out = nullptr;
+  int coarse_iters_last = 0;
+  ~tpss_mg()
+  {
+    if(gstream) cudaStreamDestroy(gstream);
+    if(ev_in) cudaEventDestroy(ev_in);
+    if(ev_out) cudaEventDestroy(ev_out);
+    if(g_full) cudaGraphExecDestroy(g_full);
+    if(g_down) cudaGraphExecDestroy(g_down);
+    if(g_up) cudaGraphExecDestroy(g_up);
+    for(auto &l : lv)
+    {
+      tpss_precond_destroy(l.P);
+      tpss_operator_destroy(l.op);
+      tpss_layout_destroy(l.L);
+    }
+    if(h_scal) cudaFreeHost(h_scal);
+  }
+};
+
+namespace
+{
+void down_sweep(tpss_mg *mg, cudaStream_t s)
+{
+  const int top = (int)mg->lv.size() - 1;
+  for(int l = top; l >= 1; --l)
+  {
+    MgLevel &c = mg->lv[l], &f = mg->lv[l - 1];
+    precond_vmult(c.P, c.x.ptr, c.b.ptr, s);
+    operator_apply(c.op, c.t.ptr, c.x.ptr, s);
+    vec_sub(c.L->n_dofs, c.b.ptr, c.t.ptr, s);
+    TPSS_CUDA(cudaMemsetAsync(f.b.ptr, 0, sizeof(double) * f.L->n_dofs, s));
+    transfer_apply(c.L->dim, c.L->k, f.L->nc, mg->E, true, f.b.ptr, c.t.ptr, s);
+  }
+}
+
+void up_sweep(tpss_mg *mg, cudaStream_t s)
+{
+  const int top = (int)mg->lv.size() - 1;
+  for(int l = 1; l <= top; ++l)
+  {
+    MgLevel &c = mg->lv[l], &f = mg->lv[l - 1];
+    transfer_apply(c.L->dim, c.L->k, f.L->nc, mg->E, false, f.x.ptr, c.x.ptr, s);
+    operator_apply(c.op, c.t.ptr, c.x.ptr, s);
+    vec_sub(c.L->n_dofs, c.b.ptr, c.t.ptr, s);
+    precond_vmult(c.P, c.r.ptr, c.t.ptr, s);
+    vec_axpby(c.L->n_dofs, 1.0, c.r.ptr, 1.0, c.x.ptr, s);
+  }
+}
+
+void coarse_dense(tpss_mg *mg, cudaStream_t s)
+{
+  MgLevel &c = mg->lv[0];
+  const int n = (int)c.L->n_dofs;
+  dense_matvec<<<(n * 32 + 255) / 256, 256, 0, s>>>(n, mg->coarse_inv.ptr, c.b.ptr, c.x.ptr);
+  TPSS_CUDA(cudaGetLastError());
+}
+
+// Unpreconditioned CG from zero to ||r|| <= coarse_tol (deal.II SolverCG with
+// SolverControl(n, tol), as MGCoarseGridIterativeSolver).
+void coarse_cg(tpss_mg *mg, cudaStream_t s)
+{
+  MgLevel &c = mg->lv[0];
+  const int64_t n = c.L->n_dofs;
+  double *x = c.x.ptr, *r = c.r.ptr, *p = mg->cp.ptr, *Ap = mg->cAp.ptr;
+  double *rz = mg->scal.ptr + 0, *pAp = mg->scal.ptr + 1, *rz_new = mg->scal.ptr + 2;
+  TPSS_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * n, s));
+  TPSS_CUDA(cudaMemcpyAsync(r, c.b.ptr, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+  TPSS_CUDA(cudaMemcpyAsync(p, r, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+  vec_dot(n, r, r, mg->partial.ptr, rz, s);
+  TPSS_CUDA(cudaMemcpyAsync(mg->h_scal, rz, sizeof(double), cudaMemcpyDeviceToHost, s));
+  TPSS_CUDA(cudaStreamSynchronize(s));
+  const double tol = mg->desc.coarse_tol;
+  int it = 0;
+  if(std::sqrt(mg->h_scal[0]) > tol)
+  {
+    for(it = 1; it <= n; ++it)
+    {
+      operator_apply(c.op, Ap, p, s);
+      vec_dot(n, p, Ap, mg->partial.ptr, pAp, s);
+      cg_update_xr<<<grid_for(n), 256, 0, s>>>(n, x, r, p, Ap, rz, pAp);
+      vec_dot(n, r, r, mg->partial.ptr, rz_new, s);
+      TPSS_CUDA(cudaMemcpyAsync(mg->h_scal, rz_new, sizeof(double), cudaMemcpyDeviceToHost, s));
+      TPSS_CUDA(cudaStreamSynchronize(s));
+      if(std::sqrt(mg->h_scal[0]) <= tol) break;
+      cg_update_p<<<grid_for(n), 256, 0, s>>>(n, p, r, rz_new, rz);
+      TPSS_CUDA(cudaMemcpyAsync(rz, rz_new, sizeof(double), cudaMemcpyDeviceToDevice, s));
+    }
+    if(it > n) fail(TPSS_ERR_NOT_CONVERGED, "coarse grid CG did not converge");
+  }
+  mg->coarse_iters_last = it;
+}
+
+void capture(tpss_mg *mg, void (*fn)(tpss_mg *, cudaStream_t), cudaGraphExec_t *out)
+{
+  cudaGraph_t g = nullptr;
+  cudaStream_t s = mg->gstream;
+  TPSS_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  try
+  {
+    fn(mg, s);
+  }
+  catch(...)
+  {
+    cudaStreamEndCapture(s, &g);
+    if(g) cudaGraphDestroy(g);
+    throw;
+  }
+  TPSS_CUDA(cudaStreamEndCapture(s, &g));
+  cudaError_t e = cudaGraphInstantiate(out, g, 0);
+  cudaGraphDestroy(g);
+  TPSS_CUDA(e);
+}
+
+void full_cycle(tpss_mg *mg, cudaStream_t s)
+{
+  down_sweep(mg, s);
+  coarse_dense(mg, s);
+  up_sweep(mg, s);
+}
+
+void launch_graph(tpss_mg *mg, cudaGraphExec_t g, cudaStream_t s)
+{
+  TPSS_CUDA(cudaEventRecord(mg->ev_in, s));
+  TPSS_CUDA(cudaStreamWaitEvent(mg->gstream, mg->ev_in, 0));
+  TPSS_CUDA(cudaGraphLaunch(g, mg->gstream));
+  TPSS_CUDA(cudaEventRecord(mg->ev_out, mg->gstream));
+  TPSS_CUDA(cudaStreamWaitEvent(s, mg->ev_out, 0));
+}
+
+// x_top = V-cycle(b_top)
+void vcycle(tpss_mg *mg, cudaStream_t s)
+{
+  const bool dense = mg->desc.coarse_solver == 1;
+  if(mg->desc.use_graph)
+  {
+    if(dense)
+    {
+      if(!mg->g_full)
+      {
+        full_cycle(mg, s);  // eager warm-up: scratch allocations happen outside the capture
+        TPSS_CUDA(cudaStreamSynchronize(s));
+        capture(mg, full_cycle, &mg->g_full);
+      }
+      launch_graph(mg, mg->g_full, s);
+      return;
+    }
+    if(!mg->g_down)
+    {
+      down_sweep(mg, s);
+      coarse_cg(mg, s);
+      up_sweep(mg, s);
+      TPSS_CUDA(cudaStreamSynchronize(s));
+      capture(mg, down_sweep, &mg->g_down);
+      capture(mg, up_sweep, &mg->g_up);
+    }
+    launch_graph(mg, mg->g_down, s);
+    coarse_cg(mg, s);
+    launch_graph(mg, mg->g_up, s);
+    return;
+  }
+  down_sweep(mg, s);
+  if(dense)
+    coarse_dense(mg, s);
+  else
+    coarse_cg(mg, s);
+  up_sweep(mg, s);
+}
+}  // namespace
+
+extern "C" int tpss_mg_create(const tpss_mg_desc *d, tpss_mg **out)
+{
+  return guarded([&] {
+    TPSS_REQUIRE(d && out, "null argument");
+    *out = nullptr;
+    TPSS_REQUIRE(d->dim == 2 || d->dim == 3, "dim must be 2 or 3");
+    TPSS_REQUIRE(d->n_rep >= 1 && d->n_cells_fine >= d->n_rep, "invalid mesh sizes");
+    int nl = 0;
+    for(int nc = d->n_rep; nc <= d->n_cells_fine; nc *= 2) ++nl;
+    TPSS_REQUIRE((d->n_rep << (nl - 1)) == d->n_cells_fine, "n_cells_fine must be n_rep * 2^L");
+    TPSS_REQUIRE(nl >= 2, "at least two levels are needed");
+    auto mg = std::make_unique<tpss_mg>();
+    mg->desc = *d;
+    mg->lv.resize(nl);
+    for(int l = 0; l < nl; ++l)
+    {
+      MgLevel &lv = mg->lv[l];
+      tpss_layout_desc ld{};
+      ld.dim = d->dim;
+      ld.degree = d->degree;
+      ld.dof_layout = TPSS_DOF_DGQ;
+      ld.patch_variant = d->patch_variant;
+      ld.smoother_variant = d->smoother_variant;
+      for(int dd = 0; dd < 3; ++dd) ld.n_cells[dd] = dd < d->dim ? (d->n_rep << l) : 1;
+      int rc = tpss_layout_create(&ld, &lv.L);
+      if(rc) fail(rc, tpss_last_error());
+      rc = tpss_operator_create(lv.L, d->ip_factor, &lv.op);
+      if(rc) fail(rc, tpss_last_error());
+      if(l > 0)
+      {
+        tpss_precond_desc pd{};
+        pd.relaxation = d->relaxation;
+        pd.precision = d->precision;
+        pd.ip_factor = d->ip_factor;
+        rc = tpss_precond_create(lv.L, lv.op, &pd, &lv.P);
+        if(rc) fail(rc, tpss_last_error());
+      }
+      const int64_t n = lv.L->n_dofs;
+      lv.x.resize(n);
+      lv.b.resize(n);
+      lv.t.resize(n);
+      lv.r.resize(n);
+    }
+    const int64_t n0 = mg->lv[0].L->n_dofs, nt = mg->lv[nl - 1].L->n_dofs;
+    if(d->coarse_solver == 1)
+    {
+      TPSS_REQUIRE(n0 <= 4096, "dense coarse solver limited to 4096 coarse DoFs");
+      std::vector<double> inv = dense_inverse(*mg->lv[0].L, d->ip_factor);
+      mg->coarse_inv.upload(inv.data(), inv.size());
+    }
+    mg->cp.resize(n0);
+    mg->cAp.resize(n0);
+    mg->partial.resize(dot_partials());
+    mg->scal.resize(16);
+    mg->r.resize(nt);
+    mg->p.resize(nt);
+    mg->Ap.resize(nt);
+    mg->z.resize(nt);
+    TPSS_CUDA(cudaMallocHost(&mg->h_scal, 16 * sizeof(double)));
+    TPSS_CUDA(cudaStreamCreateWithFlags(&mg->gstream, cudaStreamNonBlocking));
+    TPSS_CUDA(cudaEventCreateWithFlags(&mg->ev_in, cudaEventDisableTiming));
+    TPSS_CUDA(cudaEventCreateWithFlags(&mg->ev_out, cudaEventDisableTiming));
+    mg->E = embedding_table(d->degree);
+    *out = mg.release();
+  });
+}
+
+extern "C" int tpss_mg_n_dofs(const tpss_mg *mg, int64_t *n)
+{
+  return guarded([&] {
+    TPSS_REQUIRE(mg && n, "null argument");
+    *n = mg->lv.back().L->n_dofs;
+  });
+}
+
+extern "C" int tpss_mg_n_levels(const tpss_mg *mg, int *n)
+{
+  return guarded([&] {
+    TPSS_REQUIRE(mg && n, "null argument");
+    *n = (int)mg->lv.size();
+  });
+}
+
+extern "C" int tpss_mg_level(tpss_mg *mg, int level, tpss_layout **layout, tpss_operator **op,
+                             tpss_precond **precond)
+{
+  return guarded([&] {
+    TPSS_REQUIRE(mg && level >= 0 && level < (int)mg->lv.size(), "invalid level");
+    if(layout) *layout = mg->lv[level].L;
+    if(op) *op = mg->lv[level].op;
+    if(precond) *precond = mg->lv[level].P;
+  });
+}
+
+extern "C" int tpss_mg_vmult(tpss_mg *mg, double *dst, const double *src, void *stream)
+{
+  return guarded([&] {
+    TPSS_REQUIRE(mg && dst && src, "null argument");
+    cudaStream_t s = as_stream(stream);
+    MgLevel &top = mg->lv.back();
+    const int64_t n = top.L->n_dofs;
+    TPSS_CUDA(cudaMemcpyAsync(top.b.ptr, src, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+    vcycle(mg, s);
+    TPSS_CUDA(cudaMemcpyAsync(dst, top.x.ptr, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+  });
+}
+
+extern "C" int tpss_mg_cg_solve(tpss_mg *mg, double *u, const double *f, double rel_tol,
+                                double abs_tol, int max_iter, int *iterations,
+                                double *res_history, void *stream)
+{
+  return guarded([&] {
+    TPSS_REQUIRE(mg && u && f && iterations, "null argument");
+    TPSS_REQUIRE(max_iter >= 0, "max_iter must be non-negative");
+    cudaStream_t s = as_stream(stream);
+    MgLevel &top = mg->lv.back();
+    const int64_t n = top.L->n_dofs;
+    double *r = mg->r.ptr, *p = mg->p.ptr, *Ap = mg->Ap.ptr;
+    double *d_rz = mg->scal.ptr + 8, *d_pAp = mg->scal.ptr + 9, *d_rr = mg->scal.ptr + 10,
+           *d_rz_new = mg->scal.ptr + 11;
+    TPSS_CUDA(cudaMemsetAsync(u, 0, sizeof(double) * n, s));
+    TPSS_CUDA(cudaMemcpyAsync(r, f, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+    vec_dot(n, r, r, mg->partial.ptr, d_rr, s);
+    TPSS_CUDA(cudaMemcpyAsync(mg->h_scal + 4, d_rr, sizeof(double), cudaMemcpyDeviceToHost, s));
+    TPSS_CUDA(cudaStreamSynchronize(s));
+    double res = std::sqrt(mg->h_scal[4]);
+    if(res_history) res_history[0] = res;
+    const double tol = std::max(abs_tol, rel_tol * res);
+    int it = 0;
+    bool converged = res <= tol;
+    if(!converged)
+    {
+      // z = V(r); p = z; rz = r.z
+      TPSS_CUDA(cudaMemcpyAsync(top.b.ptr, r, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+      vcycle(mg, s);
+      TPSS_CUDA(cudaMemcpyAsync(p, top.x.ptr, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+      vec_dot(n, r, top.x.ptr, mg->partial.ptr, d_rz, s);
+      for(it = 1; it <= max_iter; ++it)
+      {
+        operator_apply(top.op, Ap, p, s);
+        vec_dot(n, p, Ap, mg->partial.ptr, d_pAp, s);
+        cg_update_xr<<<grid_for(n), 256, 0, s>>>(n, u, r, p, Ap, d_rz, d_pAp);
+        vec_dot(n, r, r, mg->partial.ptr, d_rr, s);
+        TPSS_CUDA(cudaMemcpyAsync(mg->h_scal + 4, d_rr, sizeof(double), cudaMemcpyDeviceToHost, s));
+        TPSS_CUDA(cudaStreamSynchronize(s));
+        res = std::sqrt(mg->h_scal[4]);
+        if(res_history) res_history[it] = res;
+        if(res <= tol)
+        {
+          converged = true;
+          break;
+        }
+        TPSS_CUDA(cudaMemcpyAsync(top.b.ptr, r, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+        vcycle(mg, s);
+        vec_dot(n, r, top.x.ptr, mg->partial.ptr, d_rz_new, s);
+        cg_update_p<<<grid_for(n), 256, 0, s>>>(n, p, top.x.ptr, d_rz_new, d_rz);
+        TPSS_CUDA(cudaMemcpyAsync(d_rz, d_rz_new, sizeof(double), cudaMemcpyDeviceToDevice, s));
+      }
+    }
+    *iterations = converged ? it : -1;
+    if(!converged) fail(TPSS_ERR_NOT_CONVERGED, "CG did not reach the tolerance within max_iter");
+  });
+}
+
+extern "C" void tpss_mg_destroy(tpss_mg *mg) { delete mg; }

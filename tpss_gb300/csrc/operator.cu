@@ -1,0 +1,481 @@
+// operator.cu -- FP64 matrix-free SIPG operator, DG level transfer and vector kernels.
+//
+// Operator: MF::Operator::vmult (apps/laplace_integrator.h:578-743) on a Cartesian level.
+// With Gauss quadrature of k+1 points per direction the cell and face integrals are exact,
+// and on a tensor-product (Cartesian) mesh the SIPG bilinear form is the Kronecker sum
+//   A = sum_d M_{dim-1} x .. x A_d x .. x M_0
+// of global 1-D operators: block-diagonal cell mass matrices M_e and block-tridiagonal 1-D
+// SIPG matrices A_d (cell Laplace, Dirichlet boundary faces with sigma = 2 ip gamma / h,
+// interior faces with sigma = ip gamma (1/h_l + 1/h_r)/2, gamma = k(k+1);
+// apps/common_integrator.h:30-37).  Each output cell therefore gathers 3*dim neighbour terms
+// (left, self, right per direction), each a dim-fold sum-factorized contraction.
+//
+// Transfer: MGTransferMatrixFree for FE_DGQ -- prolongation embeds the coarse polynomial in
+// the 2^dim children (1-D embedding matrices E_0, E_1), restriction is its transpose.
+#include <mutex>
+
+#include "internal.h"
+
+namespace tpss
+{
+namespace
+{
+__host__ __device__ constexpr int cpow(int b, int e) { return e == 0 ? 1 : b * cpow(b, e - 1); }
+
+// in-place pencil contraction along DIR of one (NP)^DIM block: x <- (I x..x B x..x I) x,
+// B row-major NP x NP (TRANS: B^T)
+template<int DIM, int NP, int DIR, bool TRANS>
+__device__ __forceinline__ void pencil(double *x, const double *B, int p)
+{
+  constexpr int stride = cpow(NP, DIR);
+  const int base = (p % stride) + (p / stride) * stride * NP;
+  double r[NP], o[NP];
+#pragma unroll
+  for(int m = 0; m < NP; ++m) r[m] = x[base + m * stride];
+#pragma unroll
+  for(int i = 0; i < NP; ++i)
+  {
+    double acc = 0.0;
+#pragma unroll
+    for(int m = 0; m < NP; ++m) acc = fma(TRANS ? B[m * NP + i] : B[i * NP + m], r[m], acc);
+    o[i] = acc;
+  }
+#pragma unroll
+  for(int i = 0; i < NP; ++i) x[base + i * stride] = o[i];
+}
+
+template<int DIM, int NP, bool TRANS>
+__device__ __forceinline__ void pencil_dir(int dir, double *x, const double *B, int p)
+{
+  if(dir == 0) pencil<DIM, NP, 0, TRANS>(x, B, p);
+  else if(dir == 1) pencil<DIM, NP, 1, TRANS>(x, B, p);
+  else if constexpr(DIM == 3) pencil<DIM, NP, 2, TRANS>(x, B, p);
+}
+
+struct OpArgs
+{
+  const double *__restrict__ src;
+  double *__restrict__ dst;
+  const int64_t *__restrict__ cell_start;  // nullptr = lexicographic
+  const double *__restrict__ mass[3];      // [nc[d]][NP*NP]
+  const double *__restrict__ blk[3];       // [nc[d]][3][NP*NP]
+  int nc[3];
+  int64_t n_cells;
+};
+
+template<int DIM, int NP>
+struct OpCfg
+{
+  static constexpr int ND = cpow(NP, DIM);
+  static constexpr int NPENC = ND / NP;
+  static constexpr int CPB = NPENC >= 64 ? 1 : (64 + NPENC - 1) / NPENC;  // cells per block
+  static constexpr int THREADS = ((CPB * NPENC + 31) / 32) * 32;
+};
+
+template<int DIM, int NP>
+__global__ void __launch_bounds__(OpCfg<DIM, NP>::THREADS) sipg_kernel(OpArgs a)
+{
+  using C = OpCfg<DIM, NP>;
+  constexpr int ND = C::ND, CPB = C::CPB, NPENC = C::NPENC;
+  __shared__ double s_buf[CPB * ND];
+  __shared__ double s_acc[CPB * ND];
+  __shared__ double s_mat[CPB * DIM * NP * NP];
+  __shared__ int64_t s_src[CPB];
+  const int tid = threadIdx.x, slot = tid / NPENC, p = tid % NPENC;
+  for(int64_t c0 = (int64_t)blockIdx.x * CPB; c0 < a.n_cells; c0 += (int64_t)gridDim.x * CPB)
+  {
+    for(int i = tid; i < CPB * ND; i += C::THREADS) s_acc[i] = 0.0;
+    for(int term = 0; term < 3 * DIM; ++term)
+    {
+      const int d = term / 3, o = term % 3 - 1;
+      __syncthreads();
+      if(tid < CPB)
+      {
+        const int64_t cell = c0 + tid;
+        int64_t src_first = -1;
+        if(cell < a.n_cells)
+        {
+          int c[3] = {(int)(cell % a.nc[0]), (int)((cell / a.nc[0]) % a.nc[1]),
+                      (int)(cell / ((int64_t)a.nc[0] * a.nc[1]))};
+          const int cn = c[d] + o;
+          if(cn >= 0 && cn < a.nc[d])
+          {
+            c[d] = cn;
+            const int64_t nb = c[0] + (int64_t)a.nc[0] * (c[1] + (int64_t)a.nc[1] * c[2]);
+            src_first = a.cell_start ? a.cell_start[nb] : nb * ND;
+          }
+        }
+        s_src[tid] = src_first;
+      }
+      // matrices of this term: direction e uses the 1-D SIPG block (e == d) or the mass
+      for(int i = tid; i < CPB * DIM * NP * NP; i += C::THREADS)
+      {
+        const int s = i / (DIM * NP * NP), e = (i / (NP * NP)) % DIM, q = i % (NP * NP);
+        const int64_t cell = c0 + s;
+        double v = 0.0;
+        if(cell < a.n_cells)
+        {
+          const int ce = e == 0 ? (int)(cell % a.nc[0])
+                       : e == 1 ? (int)((cell / a.nc[0]) % a.nc[1])
+                                : (int)(cell / ((int64_t)a.nc[0] * a.nc[1]));
+          v = e == d ? a.blk[e][((size_t)ce * 3 + (o + 1)) * NP * NP + q]
+                     : a.mass[e][(size_t)ce * NP * NP + q];
+        }
+        s_mat[i] = v;
+      }
+      __syncthreads();
+      for(int i = tid; i < CPB * ND; i += C::THREADS)
+      {
+        const int s = i / ND;
+        const int64_t f = s_src[s];
+        s_buf[i] = f >= 0 ? a.src[f + (i % ND)] : 0.0;
+      }
+      __syncthreads();
+      const bool active = slot < CPB && s_src[slot < CPB ? slot : 0] >= 0;
+      for(int e = 0; e < DIM; ++e)
+      {
+        if(active) pencil_dir<DIM, NP, false>(e, s_buf + slot * ND, s_mat + (slot * DIM + e) * NP * NP, p);
+        __syncthreads();
+      }
+      for(int i = tid; i < CPB * ND; i += C::THREADS)
+        if(s_src[i / ND] >= 0) s_acc[i] += s_buf[i];
+    }
+    __syncthreads();
+    for(int i = tid; i < CPB * ND; i += C::THREADS)
+    {
+      const int64_t cell = c0 + i / ND;
+      if(cell < a.n_cells)
+      {
+        const int64_t f = a.cell_start ? a.cell_start[cell] : cell * ND;
+        a.dst[f + i % ND] = s_acc[i];
+      }
+    }
+    __syncthreads();
+  }
+}
+
+template<int DIM, int NP>
+void launch_sipg(const OpArgs &a, cudaStream_t s)
+{
+  using C = OpCfg<DIM, NP>;
+  const int64_t blocks = (a.n_cells + C::CPB - 1) / C::CPB;
+  const int64_t cap = (int64_t)num_sms() * 16;
+  const int grid = (int)(blocks < cap ? blocks : cap);
+  sipg_kernel<DIM, NP><<<grid, C::THREADS, 0, s>>>(a);
+  TPSS_CUDA(cudaGetLastError());
+}
+
+// ---- transfer: one coarse cell per slot
+struct TrArgs
+{
+  double *coarse;
+  double *fine;
+  const double *E;  // [2][NP*NP]
+  int ncc[3];
+  int64_t n_coarse;
+};
+
+template<int DIM, int NP, bool RESTRICT>
+__global__ void __launch_bounds__(OpCfg<DIM, NP>::THREADS) transfer_kernel(TrArgs a)
+{
+  using C = OpCfg<DIM, NP>;
+  constexpr int ND = C::ND, CPB = C::CPB, NPENC = C::NPENC, NCH = 1 << DIM;
+  __shared__ double s_buf[CPB * ND];
+  __shared__ double s_acc[CPB * ND];
+  __shared__ double s_E[2 * NP * NP];
+  const int tid = threadIdx.x, slot = tid / NPENC, p = tid % NPENC;
+  for(int i = tid; i < 2 * NP * NP; i += C::THREADS) s_E[i] = a.E[i];
+  const int nf0 = 2 * a.ncc[0], nf1 = DIM > 1 ? 2 * a.ncc[1] : 1;
+  for(int64_t c0 = (int64_t)blockIdx.x * CPB; c0 < a.n_coarse; c0 += (int64_t)gridDim.x * CPB)
+  {
+    for(int i = tid; i < CPB * ND; i += C::THREADS) s_acc[i] = 0.0;
+    for(int ch = 0; ch < NCH; ++ch)
+    {
+      __syncthreads();
+      for(int i = tid; i < CPB * ND; i += C::THREADS)
+      {
+        const int64_t cell = c0 + i / ND;
+        double v = 0.0;
+        if(cell < a.n_coarse)
+        {
+          if(RESTRICT)
+          {
+            const int c[3] = {(int)(cell % a.ncc[0]), (int)((cell / a.ncc[0]) % a.ncc[1]),
+                              (int)(cell / ((int64_t)a.ncc[0] * a.ncc[1]))};
+            const int f[3] = {2 * c[0] + (ch & 1), 2 * c[1] + ((ch >> 1) & 1),
+                              DIM == 3 ? 2 * c[2] + ((ch >> 2) & 1) : 0};
+            const int64_t fc = f[0] + (int64_t)nf0 * (f[1] + (int64_t)nf1 * f[2]);
+            v = a.fine[fc * ND + i % ND];
+          }
+          else
+            v = a.coarse[cell * ND + i % ND];
+        }
+        s_buf[i] = v;
+      }
+      __syncthreads();
+      const bool active = slot < CPB && c0 + (slot < CPB ? slot : 0) < a.n_coarse;
+#pragma unroll
+      for(int e = 0; e < DIM; ++e)
+      {
+        if(active) pencil_dir<DIM, NP, RESTRICT>(e, s_buf + slot * ND, s_E + ((ch >> e) & 1) * NP * NP, p);
+        __syncthreads();
+      }
+      for(int i = tid; i < CPB * ND; i += C::THREADS)
+      {
+        const int64_t cell = c0 + i / ND;
+        if(cell >= a.n_coarse) continue;
+        if(RESTRICT)
+          s_acc[i] += s_buf[i];
+        else
+        {
+          const int c[3] = {(int)(cell % a.ncc[0]), (int)((cell / a.ncc[0]) % a.ncc[1]),
+                            (int)(cell / ((int64_t)a.ncc[0] * a.ncc[1]))};
+          const int f[3] = {2 * c[0] + (ch & 1), 2 * c[1] + ((ch >> 1) & 1),
+                            DIM == 3 ? 2 * c[2] + ((ch >> 2) & 1) : 0};
+          const int64_t fc = f[0] + (int64_t)nf0 * (f[1] + (int64_t)nf1 * f[2]);
+          a.fine[fc * ND + i % ND] += s_buf[i];
+        }
+      }
+    }
+    __syncthreads();
+    if(RESTRICT)
+      for(int i = tid; i < CPB * ND; i += C::THREADS)
+      {
+        const int64_t cell = c0 + i / ND;
+        if(cell < a.n_coarse) a.coarse[cell * ND + i % ND] += s_acc[i];
+      }
+    __syncthreads();
+  }
+}
+
+template<int DIM, int NP>
+void launch_transfer(const TrArgs &a, bool restrict_mode, cudaStream_t s)
+{
+  using C = OpCfg<DIM, NP>;
+  const int64_t blocks = (a.n_coarse + C::CPB - 1) / C::CPB;
+  const int64_t cap = (int64_t)num_sms() * 16;
+  const int grid = (int)(blocks < cap ? blocks : cap);
+  if(restrict_mode)
+    transfer_kernel<DIM, NP, true><<<grid, C::THREADS, 0, s>>>(a);
+  else
+    transfer_kernel<DIM, NP, false><<<grid, C::THREADS, 0, s>>>(a);
+  TPSS_CUDA(cudaGetLastError());
+}
+
+#define TPSS_DISPATCH_NP(dim, np, FN, ...)                                        \
+  do                                                                              \
+  {                                                                               \
+    switch((dim) * 16 + (np))                                                     \
+    {                                                                             \
+    case 2 * 16 + 2: FN<2, 2>(__VA_ARGS__); break;                                \
+    case 2 * 16 + 3: FN<2, 3>(__VA_ARGS__); break;                                \
+    case 2 * 16 + 4: FN<2, 4>(__VA_ARGS__); break;                                \
+    case 2 * 16 + 5: FN<2, 5>(__VA_ARGS__); break;                                \
+    case 2 * 16 + 6: FN<2, 6>(__VA_ARGS__); break;                                \
+    case 2 * 16 + 7: FN<2, 7>(__VA_ARGS__); break;                                \
+    case 2 * 16 + 8: FN<2, 8>(__VA_ARGS__); break;                                \
+    case 3 * 16 + 2: FN<3, 2>(__VA_ARGS__); break;                                \
+    case 3 * 16 + 3: FN<3, 3>(__VA_ARGS__); break;                                \
+    case 3 * 16 + 4: FN<3, 4>(__VA_ARGS__); break;                                \
+    case 3 * 16 + 5: FN<3, 5>(__VA_ARGS__); break;                                \
+    case 3 * 16 + 6: FN<3, 6>(__VA_ARGS__); break;                                \
+    case 3 * 16 + 7: FN<3, 7>(__VA_ARGS__); break;                                \
+    case 3 * 16 + 8: FN<3, 8>(__VA_ARGS__); break;                                \
+    default: fail(TPSS_ERR_NOT_IMPLEMENTED, "unsupported (dim, degree)");         \
+    }                                                                             \
+  } while(0)
+
+// ---- vector kernels
+__global__ void axpby_kernel(int64_t n, double a, const double *__restrict__ x, double b,
+                             double *__restrict__ y)
+{
+  for(int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    y[i] = a * x[i] + b * y[i];
+}
+
+__global__ void sub_kernel(int64_t n, const double *__restrict__ a, double *__restrict__ y)
+{
+  for(int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    y[i] = a[i] - y[i];
+}
+
+constexpr int kDotBlocks = 1024, kDotThreads = 256;
+
+__global__ void dot_partial_kernel(int64_t n, const double *__restrict__ x,
+                                   const double *__restrict__ y, double *__restrict__ part)
+{
+  __shared__ double sh[kDotThreads];
+  double s = 0.0;
+  for(int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    s = fma(x[i], y[i], s);
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for(int w = kDotThreads / 2; w > 0; w >>= 1)
+  {
+    if(threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+    __syncthreads();
+  }
+  if(threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+
+__global__ void dot_final_kernel(const double *__restrict__ part, int n, double *__restrict__ out)
+{
+  __shared__ double sh[kDotThreads];
+  double s = 0.0;
+  for(int i = threadIdx.x; i < n; i += blockDim.x) s += part[i];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for(int w = kDotThreads / 2; w > 0; w >>= 1)
+  {
+    if(threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+    __syncthreads();
+  }
+  if(threadIdx.x == 0) *out = sh[0];
+}
+
+int vec_grid(int64_t n)
+{
+  const int64_t b = (n + 255) / 256, cap = (int64_t)num_sms() * 8;
+  return (int)(b < cap ? (b > 0 ? b : 1) : cap);
+}
+}  // namespace
+
+void operator_apply(tpss_operator *op, double *dst, const double *src, cudaStream_t s)
+{
+  const tpss_layout &L = *op->layout;
+  TPSS_REQUIRE(dst && src && dst != src, "operator: invalid vectors");
+  OpArgs a;
+  a.src = src;
+  a.dst = dst;
+  a.cell_start = L.lexicographic ? nullptr : L.d_cell_start.ptr;
+  for(int d = 0; d < 3; ++d)
+  {
+    a.mass[d] = op->d_mass[d].ptr;
+    a.blk[d] = op->d_blk[d].ptr;
+    a.nc[d] = L.nc[d];
+  }
+  a.n_cells = L.n_cells;
+  TPSS_DISPATCH_NP(L.dim, L.np, launch_sipg, a, s);
+}
+
+void transfer_apply(int dim, int k, const int *ncc, const double *E_dev, bool restrict_mode,
+                    double *coarse, double *fine, cudaStream_t s)
+{
+  TrArgs a;
+  a.coarse = coarse;
+  a.fine = fine;
+  a.E = E_dev;
+  a.n_coarse = 1;
+  for(int d = 0; d < 3; ++d)
+  {
+    a.ncc[d] = d < dim ? ncc[d] : 1;
+    a.n_coarse *= a.ncc[d];
+  }
+  TPSS_DISPATCH_NP(dim, k + 1, launch_transfer, a, restrict_mode, s);
+}
+
+void vec_axpby(int64_t n, double a, const double *x, double b, double *y, cudaStream_t s)
+{
+  axpby_kernel<<<vec_grid(n), 256, 0, s>>>(n, a, x, b, y);
+  TPSS_CUDA(cudaGetLastError());
+}
+
+void vec_sub(int64_t n, const double *a, double *y, cudaStream_t s)
+{
+  sub_kernel<<<vec_grid(n), 256, 0, s>>>(n, a, y);
+  TPSS_CUDA(cudaGetLastError());
+}
+
+int dot_partials() { return kDotBlocks; }
+
+void vec_dot(int64_t n, const double *x, const double *y, double *partial, double *out,
+             cudaStream_t s)
+{
+  // fixed grid so the summation order (and the result) does not depend on the device
+  dot_partial_kernel<<<kDotBlocks, kDotThreads, 0, s>>>(n, x, y, partial);
+  dot_final_kernel<<<1, kDotThreads, 0, s>>>(partial, kDotBlocks, out);
+  TPSS_CUDA(cudaGetLastError());
+}
+}  // namespace tpss
+
+using namespace tpss;
+
+extern "C" int tpss_operator_create(const tpss_layout *layout, double ip_factor, tpss_operator **out)
+{
+  return guarded([&] {
+    TPSS_REQUIRE(layout && out, "null argument");
+    TPSS_REQUIRE(ip_factor > 0.0, "ip_factor must be positive");
+    *out = nullptr;
+    layout_to_device(*layout);
+    auto op = std::make_unique<tpss_operator>();
+    op->layout = layout;
+    op->ip = ip_factor;
+    const Shape1D s = make_shape_1d(layout->k);
+    for(int d = 0; d < layout->dim; ++d)
+    {
+      std::vector<double> mass, blk;
+      operator_blocks_1d(s, layout->nc[d], layout->h[d].data(), ip_factor, mass, blk);
+      op->d_mass[d].upload(mass.data(), mass.size());
+      op->d_blk[d].upload(blk.data(), blk.size());
+      op->nblk_cells[d] = layout->nc[d];
+    }
+    *out = op.release();
+  });
+}
+
+extern "C" int tpss_operator_vmult(tpss_operator *op, double *dst, const double *src, void *stream)
+{
+  return guarded([&] {
+    TPSS_REQUIRE(op, "null operator");
+    operator_apply(op, dst, src, as_stream(stream));
+  });
+}
+
+extern "C" void tpss_operator_destroy(tpss_operator *op) { delete op; }
+
+namespace
+{
+const double *embedding_device(int k)
+{
+  static std::mutex mu;
+  static double *tables[9] = {nullptr};
+  std::lock_guard<std::mutex> lock(mu);
+  if(!tables[k])
+  {
+    const Shape1D s = make_shape_1d(k);
+    const std::vector<double> E = embedding_1d(s);
+    double *d = nullptr;
+    TPSS_CUDA(cudaMalloc(&d, E.size() * sizeof(double)));
+    TPSS_CUDA(cudaMemcpy(d, E.data(), E.size() * sizeof(double), cudaMemcpyHostToDevice));
+    tables[k] = d;  // kept for the lifetime of the process
+  }
+  return tables[k];
+}
+}  // namespace
+
+namespace tpss
+{
+const double *embedding_table(int k) { return embedding_device(k); }
+}  // namespace tpss
+
+extern "C" int tpss_transfer_prolongate_add(int dim, int degree, const int *ncc, double *fine,
+                                            const double *coarse, void *stream)
+{
+  return guarded([&] {
+    TPSS_REQUIRE(ncc && fine && coarse, "null argument");
+    TPSS_REQUIRE((dim == 2 || dim == 3) && degree >= 1 && degree <= 7, "unsupported dim/degree");
+    transfer_apply(dim, degree, ncc, embedding_device(degree), false, const_cast<double *>(coarse),
+                   fine, as_stream(stream));
+  });
+}
+
+extern "C" int tpss_transfer_restrict_add(int dim, int degree, const int *ncc, double *coarse,
+                                          const double *fine, void *stream)
+{
+  return guarded([&] {
+    TPSS_REQUIRE(ncc && fine && coarse, "null argument");
+    TPSS_REQUIRE((dim == 2 || dim == 3) && degree >= 1 && degree <= 7, "unsupported dim/degree");
+    transfer_apply(dim, degree, ncc, embedding_device(degree), true, coarse,
+                   const_cast<double *>(fine), as_stream(stream));
+  });
+}

@@ -1,0 +1,474 @@
+// precond.cu -- SchwarzPreconditioner and SchwarzSmoother on the GPU.
+//
+// initialize (preconditioner/schwarz_preconditioner.templates.h:1-60): the 1-D SIPG
+// mass/Laplace matrices of every distinct (h_left, h_right, boundary flags) patch direction are
+// assembled on the host and their generalized eigenproblems are solved in FP64 on the GPU
+// (compute_inverses, templates:101-123); the FD tables are kept in FP64 and FP32.
+// vmult (templates:209-239): additive = dst := 0 then one fused kernel per color
+// (additive_schwarz_operation, templates:665-688); multiplicative = residual update with the
+// level operator between colors in the color sequence of get_color_sequence
+// (schwarz_preconditioner.h:532-567, templates:691-732).
+#include <chrono>
+#include <cmath>
+#include <cstring>
+
+#include "internal.h"
+
+namespace tpss
+{
+void gen_eig_batched(int n, int n_problems, const std::vector<double> &Ms,
+                     const std::vector<double> &As, std::vector<double> &S,
+                     std::vector<double> &lam);
+
+namespace
+{
+const char *kTimerNames[5] = {"[SchwarzPrecond] Update residuals:", "[SchwarzPrecond] Apply inverses:",
+                              "[SchwarzPrecond] Compute inverses:",
+                              "[SchwarzPrecond] Copy Locally Owned:", "[SchwarzPrecond] Step:"};
+
+int pad_to(int n, int w) { return (n + w - 1) / w * w; }
+
+std::shared_ptr<FdTables> build_tables(const tpss_layout &L, double ip, bool ras)
+{
+  auto t0 = std::chrono::steady_clock::now();
+  auto T = std::make_shared<FdTables>();
+  T->layout = &L;
+  T->n = L.n;
+  T->n_entries = (int)L.fd_keys.size();
+  T->npad32 = pad_to(L.n, 4);
+  T->npad64 = pad_to(L.n, 2);
+  const int n = L.n, nn = n * n;
+  const Shape1D shape = make_shape_1d(L.k);
+  std::vector<double> Ms((size_t)T->n_entries * nn), As((size_t)T->n_entries * nn);
+  for(int e = 0; e < T->n_entries; ++e)
+  {
+    const auto &key = L.fd_keys[e];
+    const double h[2] = {key.h0, key.h1};
+    patch_matrices_1d(shape, L.ncp, h, key.lo != 0, key.hi != 0, ip, &Ms[(size_t)e * nn],
+                      &As[(size_t)e * nn]);
+  }
+  gen_eig_batched(n, T->n_entries, Ms, As, T->S_host, T->lam_host);
+  // kernel tables: [S^T n x npad][S n x npad][lambda npad]
+  auto fill = [&](auto *dummy, int npad, std::vector<std::remove_pointer_t<decltype(dummy)>> &out) {
+    using V = std::remove_pointer_t<decltype(dummy)>;
+    const int es = (2 * n + 1) * npad;
+    out.assign((size_t)T->n_entries * es, V(0));
+    for(int e = 0; e < T->n_entries; ++e)
+    {
+      const double *S = &T->S_host[(size_t)e * nn], *lam = &T->lam_host[(size_t)e * n];
+      V *E = &out[(size_t)e * es];
+      for(int i = 0; i < n; ++i)
+        for(int m = 0; m < n; ++m)
+        {
+          E[i * npad + m] = V(S[m * n + i]);              // S^T
+          E[n * npad + i * npad + m] = V(S[i * n + m]);   // S
+        }
+      for(int i = 0; i < n; ++i) E[2 * n * npad + i] = V(lam[i]);
+    }
+  };
+  std::vector<double> t64;
+  std::vector<float> t32;
+  fill((double *)nullptr, T->npad64, t64);
+  fill((float *)nullptr, T->npad32, t32);
+  T->fd64.upload(t64.data(), t64.size());
+  T->fd32.upload(t32.data(), t32.size());
+  if(ras)
+  {
+    // RAS weights: 1 / (number of patches sharing the cell), the gathered "appearances" of
+    // compute_ras_weights (schwarz_preconditioner.templates.h:126-165); DG DoFs of a cell
+    // all have the same count.
+    std::vector<float> w((size_t)L.P * L.npc);
+    const std::vector<int64_t> &first = L.patch_first;
+    std::vector<int32_t> mult_by_block(L.n_cells);
+    for(int64_t c = 0; c < L.n_cells; ++c)
+      mult_by_block[L.cell_start[c] / L.cell_dofs] = L.cell_multiplicity[c];
+    for(size_t i = 0; i < w.size(); ++i) w[i] = 1.0f / float(mult_by_block[first[i] / L.cell_dofs]);
+    T->ras_w.upload(w.data(), w.size());
+  }
+  T->setup_seconds =
+    std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  return T;
+}
+
+void validate_desc(const tpss_precond_desc &d)
+{
+  TPSS_REQUIRE(d.relaxation > 0.0, "Invalid relaxation factor.");
+  TPSS_REQUIRE(d.precision == TPSS_FP64 || d.precision == TPSS_FP32, "invalid precision");
+  if(d.use_ras_weights && d.use_ras_boolean_weights)
+    fail(TPSS_ERR_INVALID_ARGUMENT, "It isn't possible to use more than one RAS option.");
+  if(d.use_ras_boolean_weights)
+    fail(TPSS_ERR_NOT_IMPLEMENTED, "RAS boolean weights (rscatter_add) are not implemented");
+}
+
+cudaEvent_t get_event(tpss_precond *p)
+{
+  if(!p->event_pool.empty())
+  {
+    cudaEvent_t e = p->event_pool.back();
+    p->event_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e;
+  TPSS_CUDA(cudaEventCreate(&e));
+  return e;
+}
+
+// Timers are read lazily: start/stop events are recorded on the stream and resolved when
+// the caller asks for the time data (or when too many are pending).
+void harvest(tpss_precond *p, bool all)
+{
+  size_t keep_from = 0;
+  for(size_t i = 0; i < p->pending.size(); ++i)
+  {
+    auto &pe = p->pending[i];
+    if(!all && cudaEventQuery(pe.stop) != cudaSuccess)
+    {
+      keep_from = i;
+      break;
+    }
+    TPSS_CUDA(cudaEventSynchronize(pe.stop));
+    float ms = 0.f;
+    TPSS_CUDA(cudaEventElapsedTime(&ms, pe.start, pe.stop));
+    p->timers[pe.slot].time += ms * 1e-3;
+    p->timers[pe.slot].n_calls += 1;
+    p->event_pool.push_back(pe.start);
+    p->event_pool.push_back(pe.stop);
+    keep_from = i + 1;
+  }
+  p->pending.erase(p->pending.begin(), p->pending.begin() + keep_from);
+}
+
+struct ScopedTimer
+{
+  tpss_precond *p;
+  int slot;
+  cudaStream_t s;
+  cudaEvent_t start = nullptr;
+  bool enabled;
+  ScopedTimer(tpss_precond *p_, int slot_, cudaStream_t s_) : p(p_), slot(slot_), s(s_)
+  {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaStreamIsCapturing(s, &cs);
+    enabled = cs == cudaStreamCaptureStatusNone;  // no event timing inside graph capture
+    if(enabled)
+    {
+      start = get_event(p);
+      TPSS_CUDA(cudaEventRecord(start, s));
+    }
+  }
+  ~ScopedTimer()
+  {
+    if(!enabled) return;
+    cudaEvent_t stop = nullptr;
+    try
+    {
+      stop = get_event(p);
+    }
+    catch(...)
+    {
+      return;
+    }
+    cudaEventRecord(stop, s);
+    p->pending.push_back({start, stop, slot});
+    if(p->pending.size() > 256)
+    {
+      try
+      {
+        harvest(p, false);
+      }
+      catch(...)
+      {
+      }
+    }
+  }
+};
+
+__global__ void finite_check_kernel(const double *__restrict__ x, int64_t n, int *flag)
+{
+  int bad = 0;
+  for(int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+      i += (int64_t)gridDim.x * blockDim.x)
+    bad |= !isfinite(x[i]);
+  if(__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(flag, 1);
+}
+
+void apply_color(tpss_precond *p, int color, double *dst, const double *src, cudaStream_t s)
+{
+  const tpss_layout &L = *p->tables->layout;
+  const int64_t b = L.color_start[color], e = L.color_start[color + 1];
+  if(e <= b) return;
+  FdLaunch a;
+  a.src = src;
+  a.dst = dst;
+  a.patch_first = L.d_patch_first.ptr + b * L.npc;
+  a.patch_fd = L.d_patch_fd.ptr + b * L.dim;
+  const bool ras = p->desc.use_ras_weights && L.smoother_variant == TPSS_ADDITIVE;
+  a.ras_w = ras ? p->tables->ras_w.ptr + b * L.npc : nullptr;
+  a.n_patches = e - b;
+  a.omega = p->desc.relaxation;
+  bool ok;
+  if(p->desc.precision == TPSS_FP32)
+  {
+    a.fd = p->tables->fd32.ptr;
+    a.entry_stride = (2 * L.n + 1) * p->tables->npad32;
+    ok = launch_fd_f32(L.dim, L.k, L.ncp, a, s);
+  }
+  else
+  {
+    a.fd = p->tables->fd64.ptr;
+    a.entry_stride = (2 * L.n + 1) * p->tables->npad64;
+    ok = launch_fd_f64(L.dim, L.k, L.ncp, a, s);
+  }
+  if(!ok)
+  {
+    cudaError_t err = cudaGetLastError();
+    fail(TPSS_ERR_CUDA, std::string("Schwarz color kernel launch failed: ") + cudaGetErrorString(err));
+  }
+}
+}  // namespace
+
+bool launch_fd_float_2(int k, int ncp, const FdLaunch &a, cudaStream_t s);
+bool launch_fd_float_3(int k, int ncp, const FdLaunch &a, cudaStream_t s);
+bool launch_fd_double_2(int k, int ncp, const FdLaunch &a, cudaStream_t s);
+bool launch_fd_double_3(int k, int ncp, const FdLaunch &a, cudaStream_t s);
+
+bool launch_fd_f32(int dim, int k, int ncp, const FdLaunch &a, cudaStream_t s)
+{
+  return dim == 2 ? launch_fd_float_2(k, ncp, a, s) : launch_fd_float_3(k, ncp, a, s);
+}
+
+bool launch_fd_f64(int dim, int k, int ncp, const FdLaunch &a, cudaStream_t s)
+{
+  return dim == 2 ? launch_fd_double_2(k, ncp, a, s) : launch_fd_double_3(k, ncp, a, s);
+}
+
+void precond_vmult(tpss_precond *p, double *dst, const double *src, cudaStream_t s)
+{
+  const tpss_layout &L = *p->tables->layout;
+  TPSS_REQUIRE(dst && src, "null vector");
+  TPSS_REQUIRE(dst != src, "dst and src must not alias");
+  ScopedTimer step(p, 4, s);
+  TPSS_CUDA(cudaMemsetAsync(dst, 0, sizeof(double) * L.n_dofs, s));
+  if(L.smoother_variant == TPSS_ADDITIVE)
+  {
+    ScopedTimer t(p, 1, s);
+    for(int c = 0; c < L.n_colors; ++c) apply_color(p, c, dst, src, s);
+  }
+  else
+  {
+    TPSS_REQUIRE(p->op, "the multiplicative smoother needs the level operator");
+    std::vector<int> seq;
+    for(int c = 0; c < L.n_colors; ++c) seq.push_back(p->desc.reverse ? L.n_colors - 1 - c : c);
+    if(p->desc.symmetrized)
+      for(int i = L.n_colors - 2; i >= 0; --i) seq.push_back(seq[i]);
+    if(p->residual.n < (size_t)L.n_dofs) p->residual.resize(L.n_dofs);
+    double *res = p->residual.ptr;
+    {
+      ScopedTimer t(p, 1, s);
+      apply_color(p, seq[0], dst, src, s);
+    }
+    for(size_t i = 1; i < seq.size(); ++i)
+    {
+      {
+        ScopedTimer t(p, 0, s);
+        operator_apply(p->op, res, dst, s);
+        vec_sub(L.n_dofs, src, res, s);  // res = src - A dst
+      }
+      ScopedTimer t(p, 1, s);
+      apply_color(p, seq[i], dst, res, s);
+    }
+  }
+  if(p->desc.check_finite)
+  {
+    if(p->flag.n == 0) p->flag.resize(1);
+    TPSS_CUDA(cudaMemsetAsync(p->flag.ptr, 0, sizeof(int), s));
+    finite_check_kernel<<<num_sms() * 4, 256, 0, s>>>(dst, L.n_dofs, p->flag.ptr);
+    TPSS_CUDA(cudaGetLastError());
+    int h = 0;
+    TPSS_CUDA(cudaMemcpyAsync(&h, p->flag.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
+    TPSS_CUDA(cudaStreamSynchronize(s));
+    if(h) fail(TPSS_ERR_NOT_FINITE, "vmult produced a non-finite value");
+  }
+}
+}  // namespace tpss
+
+using namespace tpss;
+
+struct tpss_smoother
+{
+  tpss_operator *op = nullptr;
+  tpss_precond *p = nullptr;
+  int n_steps = 1;
+  double damping = 1.0;
+  DeviceBuffer<double> residual, tmp;
+};
+
+extern "C" int tpss_precond_create(const tpss_layout *layout, tpss_operator *op,
+                                   const tpss_precond_desc *desc, tpss_precond **out)
+{
+  return guarded([&] {
+    TPSS_REQUIRE(layout && desc && out, "null argument");
+    *out = nullptr;
+    validate_desc(*desc);
+    if(layout->smoother_variant == TPSS_MULTIPLICATIVE)
+    {
+      TPSS_REQUIRE(op, "the multiplicative smoother needs the level operator");
+      TPSS_REQUIRE(op->layout->n_dofs == layout->n_dofs, "operator does not match the layout");
+    }
+    layout_to_device(*layout);
+    auto p = std::make_unique<tpss_precond>();
+    p->desc = *desc;
+    p->op = op;
+    p->tables = build_tables(*layout, desc->ip_factor, desc->use_ras_weights != 0);
+    p->timers.resize(5);
+    for(int i = 0; i < 5; ++i) p->timers[i].name = kTimerNames[i];
+    p->timers[2].time = p->tables->setup_seconds;
+    p->timers[2].n_calls = 1;
+    *out = p.release();
+  });
+}
+
+extern "C" int tpss_precond_create_shallow(const tpss_precond *other, const tpss_precond_desc *desc,
+                                           tpss_precond **out)
+{
+  return guarded([&] {
+    TPSS_REQUIRE(other && desc && out, "null argument");
+    *out = nullptr;
+    validate_desc(*desc);
+    TPSS_REQUIRE(desc->ip_factor == other->desc.ip_factor,
+                 "shallow copies share the local solvers: ip_factor must match");
+    auto p = std::make_unique<tpss_precond>();
+    p->desc = *desc;
+    p->op = other->op;
+    p->tables = other->tables;
+    if(desc->use_ras_weights && p->tables->ras_w.n == 0)
+      fail(TPSS_ERR_INVALID_ARGUMENT, "shallow copy cannot add RAS weights");
+    p->timers = other->timers;
+    *out = p.release();
+  });
+}
+
+extern "C" int tpss_precond_vmult(tpss_precond *p, double *dst, const double *src, void *stream)
+{
+  return guarded([&] {
+    TPSS_REQUIRE(p, "null preconditioner");
+    precond_vmult(p, dst, src, as_stream(stream));
+  });
+}
+
+extern "C" int tpss_precond_vmult_add(tpss_precond *p, double *dst, const double *src, void *stream)
+{
+  return guarded([&] {
+    TPSS_REQUIRE(p, "null preconditioner");
+    const int64_t n = p->tables->layout->n_dofs;
+    if(p->residual.n < (size_t)n) p->residual.resize(n);
+    // vmult into the scratch vector, then dst += scratch (multiplicative also uses the
+    // scratch for its residual, so it gets its own temporary)
+    if(p->tables->layout->smoother_variant == TPSS_MULTIPLICATIVE)
+    {
+      DeviceBuffer<double> tmp(n);
+      precond_vmult(p, tmp.ptr, src, as_stream(stream));
+      vec_axpby(n, 1.0, tmp.ptr, 1.0, dst, as_stream(stream));
+      TPSS_CUDA(cudaStreamSynchronize(as_stream(stream)));
+    }
+    else
+    {
+      precond_vmult(p, p->residual.ptr, src, as_stream(stream));
+      vec_axpby(n, 1.0, p->residual.ptr, 1.0, dst, as_stream(stream));
+    }
+  });
+}
+
+extern "C" int tpss_precond_Tvmult(tpss_precond *p, double *, const double *, void *)
+{
+  return guarded([&] {
+    TPSS_REQUIRE(p, "null preconditioner");
+    fail(TPSS_ERR_NOT_IMPLEMENTED, "TODO transpose operation is not implemented.");
+  });
+}
+
+extern "C" int tpss_precond_time_info(tpss_precond *p, tpss_time_info *out, int *n_inout)
+{
+  return guarded([&] {
+    TPSS_REQUIRE(p && n_inout, "null argument");
+    harvest(p, true);
+    const int n = (int)p->timers.size();
+    if(out)
+    {
+      const int m = std::min(n, *n_inout);
+      for(int i = 0; i < m; ++i)
+      {
+        out[i].time = p->timers[i].time;
+        out[i].n_calls = p->timers[i].n_calls;
+        std::snprintf(out[i].description, sizeof(out[i].description), "%s", p->timers[i].name);
+      }
+    }
+    *n_inout = n;
+  });
+}
+
+extern "C" void tpss_precond_destroy(tpss_precond *p)
+{
+  if(!p) return;
+  for(auto &pe : p->pending)
+  {
+    cudaEventSynchronize(pe.stop);
+    cudaEventDestroy(pe.start);
+    cudaEventDestroy(pe.stop);
+  }
+  for(auto e : p->event_pool) cudaEventDestroy(e);
+  delete p;
+}
+
+extern "C" int tpss_smoother_create(tpss_operator *op, tpss_precond *p, int n_steps,
+                                    double damping, tpss_smoother **out)
+{
+  return guarded([&] {
+    TPSS_REQUIRE(op && p && out, "null argument");
+    TPSS_REQUIRE(n_steps >= 1, "n_steps must be positive");
+    TPSS_REQUIRE(op->layout->n_dofs == p->tables->layout->n_dofs, "operator/preconditioner mismatch");
+    auto s = std::make_unique<tpss_smoother>();
+    s->op = op;
+    s->p = p;
+    s->n_steps = n_steps;
+    s->damping = damping;
+    *out = s.release();
+  });
+}
+
+namespace
+{
+void smoother_steps(tpss_smoother *sm, double *x, const double *b, cudaStream_t s)
+{
+  const int64_t n = sm->p->tables->layout->n_dofs;
+  if(sm->residual.n < (size_t)n) sm->residual.resize(n);
+  if(sm->tmp.n < (size_t)n) sm->tmp.resize(n);
+  for(int k = 0; k < sm->n_steps; ++k)
+  {
+    operator_apply(sm->op, sm->residual.ptr, x, s);  // r = A x
+    vec_sub(n, b, sm->residual.ptr, s);              // r = b - A x
+    precond_vmult(sm->p, sm->tmp.ptr, sm->residual.ptr, s);
+    vec_axpby(n, sm->damping, sm->tmp.ptr, 1.0, x, s);  // x += damping P r
+  }
+}
+}  // namespace
+
+extern "C" int tpss_smoother_step(tpss_smoother *sm, double *x, const double *b, void *stream)
+{
+  return guarded([&] {
+    TPSS_REQUIRE(sm && x && b, "null argument");
+    smoother_steps(sm, x, b, as_stream(stream));
+  });
+}
+
+extern "C" int tpss_smoother_vmult(tpss_smoother *sm, double *x, const double *b, void *stream)
+{
+  return guarded([&] {
+    TPSS_REQUIRE(sm && x && b, "null argument");
+    TPSS_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * sm->p->tables->layout->n_dofs,
+                              as_stream(stream)));
+    smoother_steps(sm, x, b, as_stream(stream));
+  });
+}
+
+extern "C" void tpss_smoother_destroy(tpss_smoother *s) { delete s; }
