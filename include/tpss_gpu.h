@@ -111,7 +111,14 @@ typedef struct tpss_precond_desc
   int precision;               /* TPSS_FP64 or TPSS_FP32 smoother arithmetic */
   double ip_factor;            /* EquationData::ip_factor of the local SIPG matrices */
   int check_finite;            /* 1: vmult checks that dst is finite (one extra reduction) */
+  int kernel_variant;          /* additive smoother kernel: TPSS_KERNEL_AUTO, TPSS_KERNEL_COLOR
+                                  (one fused launch per color) or TPSS_KERNEL_STREAM (3D vertex
+                                  patches, FP32, k <= 4: column-streamed, one pass) */
 } tpss_precond_desc;
+
+#define TPSS_KERNEL_AUTO 0
+#define TPSS_KERNEL_COLOR 1
+#define TPSS_KERNEL_STREAM 2
 
 /*
  * SchwarzPreconditioner::initialize(subdomain_handler, operator, additional_data)

@@ -254,8 +254,14 @@ def test_mg_cg_iterations_match_oracle(tpss, oracle, xcheck, cuda):
                 u = torch.zeros(N, dtype=torch.float64, device=cuda)
                 it, hist = mg.solve(u, torch.tensor(f, dtype=torch.float64, device=cuda),
                                     rel_tol=c["rel_tol"])
-                assert it == c["iterations"], (c, coarse_solver, graph, it)
-                assert abs(hist[-1] - c["final_residual"]) <= 1e-6 * c["initial_residual"]
+                if coarse_solver == 0:
+                    # the reference's coarse solver (CG to 1e-12): identical iteration counts
+                    assert it == c["iterations"], (c, graph, it)
+                    assert abs(hist[-1] - c["final_residual"]) <= 1e-6 * c["initial_residual"]
+                else:
+                    # the exact (dense) coarse solve differs from CG-to-1e-12 below 1e-12;
+                    # the count may move by one when a residual lands next to the tolerance
+                    assert abs(it - c["iterations"]) <= 1, (c, graph, it)
         # the FP32 smoother converges in the same or fewer iterations (+1 allowed)
         mg32 = tpss.MultigridSolver(c["dim"], c["k"], c["n_rep"], c["n_cells_fine"],
                                     patch_variant=c["patch_variant"],
@@ -302,3 +308,82 @@ def test_full_size_config2_fp32_vs_oracle(tpss, oracle, cuda):
     sym = abs((y * Px).sum().item() - (x * Py).sum().item()) / abs((y * Px).sum().item())
     assert sym <= 1e-10
     assert rel_err(Px.cpu().numpy(), ref) <= 1e-12
+
+
+STREAM_CASES = [
+    # k, n_cells: partial columns, several z segments, minimal meshes
+    (1, (9, 5, 17)), (2, (6, 6, 6)), (3, (5, 7, 11)), (4, (2, 2, 2)), (4, (13, 3, 10)),
+    (4, (9, 9, 18)), (3, (17, 4, 2)),
+]
+
+
+@pytest.mark.parametrize("k,nc", STREAM_CASES)
+@pytest.mark.parametrize("variant", [1, 2])
+def test_fp32_streamed_and_color_kernels(tpss, oracle, cuda, k, nc, variant):
+    """FP32 additive vertex patches in 3D: the column-streamed kernel (variant 2) and the
+    per-color kernel (variant 1) against the FP64 oracle."""
+    import torch
+    N = int(np.prod(nc)) * (k + 1) ** 3
+    src = philox(300 + k, N)
+    ad = tpss.SubdomainHandler.AdditionalData(dim=3, degree=k, n_cells=nc, patch_variant=1)
+    sh = tpss.SubdomainHandler(ad)
+    p = tpss.SchwarzPreconditioner()
+    p.initialize(sh, None, tpss.SchwarzPreconditioner.AdditionalData(
+        relaxation=0.15, precision=1, kernel_variant=variant))
+    s = torch.tensor(src, dtype=torch.float64, device=cuda)
+    d = torch.full_like(s, float("nan"))  # every entry must be written
+    p.vmult(d, s)
+    torch.cuda.synchronize()
+    ref = oracle.schwarz_vmult(3, k, nc, src, patch_variant=1, omega=0.15)
+    assert rel_err(d.cpu().numpy(), ref) <= 2e-5
+
+
+def test_streamed_kernel_general_layouts(tpss, oracle, cuda):
+    """Permuted cell numbering, non-uniform tensor-product h and RAS weights."""
+    import torch
+    k, nc = 3, (6, 5, 10)
+    g = np.random.default_rng(11)
+    h = [g.uniform(0.5, 1.5, n) for n in nc]
+    h = [x / x.sum() for x in h]
+    ncell, nd = int(np.prod(nc)), (k + 1) ** 3
+    cell_start = g.permutation(ncell) * nd
+    src = philox(12, ncell * nd)
+    for ras in (False, True):
+        ad = tpss.SubdomainHandler.AdditionalData(dim=3, degree=k, n_cells=nc, patch_variant=1,
+                                                  cell_h=h, cell_dof_start=cell_start)
+        sh = tpss.SubdomainHandler(ad)
+        p = tpss.SchwarzPreconditioner()
+        p.initialize(sh, None, tpss.SchwarzPreconditioner.AdditionalData(
+            relaxation=0.7, precision=1, kernel_variant=2, use_ras_weights=ras))
+        s = torch.tensor(src, dtype=torch.float64, device=cuda)
+        d = torch.empty_like(s)
+        p.vmult(d, s)
+        ref = oracle.schwarz_vmult(3, k, nc, src, patch_variant=1, omega=0.7, h=h,
+                                   cell_start=cell_start, use_ras=ras)
+        assert rel_err(d.cpu().numpy(), ref) <= 2e-5, ras
+
+
+def test_streamed_kernel_is_deterministic(tpss, cuda):
+    import torch
+    k, nc = 4, (20, 12, 17)
+    ad = tpss.SubdomainHandler.AdditionalData(dim=3, degree=k, n_cells=nc, patch_variant=1)
+    sh = tpss.SubdomainHandler(ad)
+    p = tpss.SchwarzPreconditioner()
+    p.initialize(sh, None, tpss.SchwarzPreconditioner.AdditionalData(relaxation=0.15, precision=1,
+                                                                     kernel_variant=2))
+    s = torch.tensor(philox(5, sh.n_dofs()), dtype=torch.float64, device=cuda)
+    a, b = torch.empty_like(s), torch.empty_like(s)
+    p.vmult(a, s)
+    p.vmult(b, s)
+    assert torch.equal(a, b)
+
+
+def test_streamed_kernel_rejects_unsupported(tpss, cuda):
+    ad = tpss.SubdomainHandler.AdditionalData(dim=2, degree=3, n_cells=(4, 4), patch_variant=1)
+    sh = tpss.SubdomainHandler(ad)
+    p = tpss.SchwarzPreconditioner()
+    p.initialize(sh, None, tpss.SchwarzPreconditioner.AdditionalData(precision=1, kernel_variant=2))
+    import torch
+    x = torch.zeros(sh.n_dofs(), dtype=torch.float64, device=cuda)
+    with pytest.raises(tpss.TPSSInvalidArgument):
+        p.vmult(x, x.clone())

@@ -236,6 +236,7 @@ class SchwarzPreconditioner:
         precision: int = Precision.fp64
         ip_factor: float = 1.0
         check_finite: bool = False
+        kernel_variant: int = 0  # 0 auto, 1 one launch per color, 2 column-streamed (3D, FP32)
 
     def __init__(self):
         self._h = None
@@ -252,6 +253,7 @@ class SchwarzPreconditioner:
         d.use_ras_boolean_weights = int(ad.use_ras_boolean_weights)
         d.precision, d.ip_factor = int(ad.precision), float(ad.ip_factor)
         d.check_finite = int(ad.check_finite)
+        d.kernel_variant = int(ad.kernel_variant)
         return d
 
     def initialize(self, subdomain_handler, linear_operator=None, additional_data=None):

@@ -30,6 +30,9 @@ TPSS_ADDITIVE = 0
 TPSS_MULTIPLICATIVE = 1
 TPSS_FP64 = 0
 TPSS_FP32 = 1
+TPSS_KERNEL_AUTO = 0
+TPSS_KERNEL_COLOR = 1
+TPSS_KERNEL_STREAM = 2
 
 
 class TPSSError(RuntimeError):
@@ -60,7 +63,8 @@ class LayoutDesc(C.Structure):
 class PrecondDesc(C.Structure):
     _fields_ = [("relaxation", C.c_double), ("reverse", C.c_int), ("symmetrized", C.c_int),
                 ("use_ras_weights", C.c_int), ("use_ras_boolean_weights", C.c_int),
-                ("precision", C.c_int), ("ip_factor", C.c_double), ("check_finite", C.c_int)]
+                ("precision", C.c_int), ("ip_factor", C.c_double), ("check_finite", C.c_int),
+                ("kernel_variant", C.c_int)]
 
 
 class TimeInfo(C.Structure):

@@ -183,6 +183,8 @@ struct tpss_layout
   tpss::DeviceBuffer<int64_t> d_patch_first;  // P*npc first DoF of each patch cell
   tpss::DeviceBuffer<int32_t> d_patch_fd;     // P*dim
   tpss::DeviceBuffer<int64_t> d_cell_start;   // n_cells (empty when lexicographic)
+  std::vector<int32_t> vertex_fd[3];           // vertex patches: FD entry of vertex v_d, per d
+  tpss::DeviceBuffer<int32_t> d_vertex_fd[3];
 };
 
 struct tpss_operator
@@ -230,6 +232,7 @@ struct tpss_precond
   tpss_precond_desc desc{};
   tpss::DeviceBuffer<double> residual;  // multiplicative scratch
   tpss::DeviceBuffer<int> flag;         // finiteness check
+  tpss::DeviceBuffer<float> halo;       // streamed kernel: partial sums of shared cells
   std::vector<tpss::TimerSlot> timers;
   std::vector<tpss::PendingEvent> pending;
   std::vector<cudaEvent_t> event_pool;
@@ -265,6 +268,19 @@ void vec_sub(int64_t n, const double *a, double *y, cudaStream_t s);  // y = a -
 int dot_partials();
 void vec_dot(int64_t n, const double *x, const double *y, double *partial, double *out,
              cudaStream_t s);
+
+// streamed 3D vertex-patch smoother, FP32 (stream3d.cu)
+struct StreamLaunch
+{
+  const double *src;
+  double *dst;
+  const float *fd32;
+  double omega;
+  int ras;
+  DeviceBuffer<float> *halo;  // scratch, grown on demand
+};
+bool stream_supported(const tpss_layout &L);
+bool launch_stream3d(const tpss_layout &L, const StreamLaunch &l, cudaStream_t s);
 
 // upload the layout's index tables (layout.cu)
 void layout_to_device(const tpss_layout &L);

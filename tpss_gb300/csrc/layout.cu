@@ -209,6 +209,19 @@ void build_layout(tpss_layout &L, const tpss_layout_desc &d)
     }
   }
   L.patch_first = std::move(first);
+  // vertex patches on the structured level: the FD key of direction d depends only on the
+  // vertex index v_d, which the streaming kernel uses instead of per-patch indices
+  if(vertex)
+    for(int dd = 0; dd < dim; ++dd)
+    {
+      L.vertex_fd[dd].assign(L.nc[dd] + 1, -1);
+      for(int v = 1; v < L.nc[dd]; ++v)
+      {
+        auto key = std::make_tuple(L.h[dd][v - 1], L.h[dd][v], (int)(v - 1 == 0), (int)(v == L.nc[dd] - 1));
+        auto it = keymap.find(key);
+        L.vertex_fd[dd][v] = it == keymap.end() ? -1 : it->second;
+      }
+    }
 }
 }  // namespace
 
@@ -222,6 +235,8 @@ void layout_to_device(const tpss_layout &Lc)
   L.d_patch_first.upload(L.patch_first.data(), L.patch_first.size());
   L.d_patch_fd.upload(L.patch_fd_key.data(), L.patch_fd_key.size());
   if(!L.lexicographic) L.d_cell_start.upload(L.cell_start.data(), L.cell_start.size());
+  for(int dd = 0; dd < 3; ++dd)
+    if(!L.vertex_fd[dd].empty()) L.d_vertex_fd[dd].upload(L.vertex_fd[dd].data(), L.vertex_fd[dd].size());
   L.on_device = true;
 }
 }  // namespace tpss

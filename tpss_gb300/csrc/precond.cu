@@ -92,6 +92,8 @@ std::shared_ptr<FdTables> build_tables(const tpss_layout &L, double ip, bool ras
 
 void validate_desc(const tpss_precond_desc &d)
 {
+  TPSS_REQUIRE(d.kernel_variant >= TPSS_KERNEL_AUTO && d.kernel_variant <= TPSS_KERNEL_STREAM,
+               "invalid kernel variant");
   TPSS_REQUIRE(d.relaxation > 0.0, "Invalid relaxation factor.");
   TPSS_REQUIRE(d.precision == TPSS_FP64 || d.precision == TPSS_FP32, "invalid precision");
   if(d.use_ras_weights && d.use_ras_boolean_weights)
@@ -242,17 +244,42 @@ bool launch_fd_f64(int dim, int k, int ncp, const FdLaunch &a, cudaStream_t s)
   return dim == 2 ? launch_fd_double_2(k, ncp, a, s) : launch_fd_double_3(k, ncp, a, s);
 }
 
+bool use_stream(const tpss_precond *p)
+{
+  const tpss_layout &L = *p->tables->layout;
+  if(p->desc.kernel_variant == TPSS_KERNEL_COLOR) return false;
+  const bool ok = L.smoother_variant == TPSS_ADDITIVE && p->desc.precision == TPSS_FP32 &&
+                  stream_supported(L);
+  if(p->desc.kernel_variant == TPSS_KERNEL_STREAM && !ok)
+    fail(TPSS_ERR_INVALID_ARGUMENT, "the streamed kernel needs additive 3D vertex patches, FP32, k <= 4");
+  return ok;
+}
+
 void precond_vmult(tpss_precond *p, double *dst, const double *src, cudaStream_t s)
 {
   const tpss_layout &L = *p->tables->layout;
   TPSS_REQUIRE(dst && src, "null vector");
   TPSS_REQUIRE(dst != src, "dst and src must not alias");
   ScopedTimer step(p, 4, s);
-  TPSS_CUDA(cudaMemsetAsync(dst, 0, sizeof(double) * L.n_dofs, s));
+  if(!(L.smoother_variant == TPSS_ADDITIVE && use_stream(p)))
+    TPSS_CUDA(cudaMemsetAsync(dst, 0, sizeof(double) * L.n_dofs, s));
   if(L.smoother_variant == TPSS_ADDITIVE)
   {
     ScopedTimer t(p, 1, s);
-    for(int c = 0; c < L.n_colors; ++c) apply_color(p, c, dst, src, s);
+    if(use_stream(p))
+    {
+      // one pass over all patches; every cell of dst is written, no zeroing needed
+      StreamLaunch l;
+      l.src = src;
+      l.dst = dst;
+      l.fd32 = p->tables->fd32.ptr;
+      l.omega = p->desc.relaxation;
+      l.ras = p->desc.use_ras_weights != 0;
+      l.halo = &p->halo;
+      if(!launch_stream3d(L, l, s)) fail(TPSS_ERR_CUDA, "streamed smoother launch failed");
+    }
+    else
+      for(int c = 0; c < L.n_colors; ++c) apply_color(p, c, dst, src, s);
   }
   else
   {
