@@ -1,0 +1,324 @@
+// tpss_gpu.hpp -- C++ host interface over the C ABI of tpss_gpu.h.
+//
+// Mirrors the reference's smoother-path classes with the same names, AdditionalData fields
+// and error behaviour (deal.II's AssertThrow throws; here every non-zero status throws
+// tpss_gpu::Error):
+//   SubdomainHandler           TPSS/subdomain_handler.h:33-262
+//   LaplaceOperator            apps/laplace_integrator.h:396-786 (MF::Operator)
+//   SchwarzPreconditioner      preconditioner/schwarz_preconditioner.h:88-588
+//   SchwarzSmoother            smoother/schwarz_smoother.h:16-52, smoother_richardson.h:14-163
+//   MultigridSolver            apps/poisson_problem.h:642-755 (GMG + CG)
+// Vectors are device pointers to FP64 arrays; streams are cudaStream_t passed as void*.
+// Header-only; link with libtpss_gpu.so.
+#pragma once
+
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "tpss_gpu.h"
+
+namespace tpss_gpu
+{
+struct Error : std::runtime_error
+{
+  int code;
+  Error(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+
+inline void check(int rc)
+{
+  if(rc != TPSS_OK)
+  {
+    const char *m = tpss_last_error();
+    throw Error(rc, m ? m : "tpss_gpu error");
+  }
+}
+
+enum class PatchVariant { cell = TPSS_PATCH_CELL, vertex = TPSS_PATCH_VERTEX };
+enum class SmootherVariant { additive = TPSS_ADDITIVE, multiplicative = TPSS_MULTIPLICATIVE };
+enum class Precision { fp64 = TPSS_FP64, fp32 = TPSS_FP32 };
+
+/* TPSS::lookup_damping_factor (TPSS/TPSS.h:121-163) */
+inline double lookup_damping_factor(PatchVariant pv, SmootherVariant sv, int dim)
+{
+  if(sv == SmootherVariant::multiplicative) return 1.;
+  if(pv == PatchVariant::cell) return 0.7;
+  if(dim == 2) return 0.25;
+  if(dim == 3) return 0.15;
+  throw Error(TPSS_ERR_INVALID_ARGUMENT, "This case is not listed!");
+}
+
+class SubdomainHandler
+{
+public:
+  struct AdditionalData
+  {
+    int dim = 2, degree = 1;
+    std::vector<int> n_cells = {2, 2};
+    PatchVariant patch_variant = PatchVariant::vertex;
+    SmootherVariant smoother_variant = SmootherVariant::additive;
+    unsigned int level = 0;
+    std::vector<std::vector<double>> cell_h;  // empty: uniform 1/n per direction
+    std::vector<int64_t> cell_dof_start;      // empty: lexicographic cell blocks
+    std::vector<int32_t> coloring;            // empty: default coloring
+  };
+
+  SubdomainHandler() = default;
+  explicit SubdomainHandler(const AdditionalData &ad) { reinit(ad); }
+  SubdomainHandler(const SubdomainHandler &) = delete;
+  SubdomainHandler &operator=(const SubdomainHandler &) = delete;
+  ~SubdomainHandler() { clear(); }
+
+  void reinit(const AdditionalData &ad)
+  {
+    clear();
+    tpss_layout_desc d{};
+    d.dim = ad.dim;
+    d.degree = ad.degree;
+    d.dof_layout = TPSS_DOF_DGQ;
+    d.patch_variant = static_cast<int>(ad.patch_variant);
+    d.smoother_variant = static_cast<int>(ad.smoother_variant);
+    for(int i = 0; i < 3; ++i) d.n_cells[i] = i < (int)ad.n_cells.size() ? ad.n_cells[i] : 1;
+    for(int i = 0; i < 3 && i < (int)ad.cell_h.size(); ++i)
+      d.cell_h[i] = ad.cell_h[i].empty() ? nullptr : ad.cell_h[i].data();
+    d.cell_dof_start = ad.cell_dof_start.empty() ? nullptr : ad.cell_dof_start.data();
+    d.patch_color = ad.coloring.empty() ? nullptr : ad.coloring.data();
+    check(tpss_layout_create(&d, &handle_));
+    additional_data_ = ad;
+  }
+
+  void clear()
+  {
+    if(handle_) tpss_layout_destroy(handle_);
+    handle_ = nullptr;
+  }
+
+  int64_t n_dofs() const
+  {
+    int64_t n = 0;
+    check(tpss_layout_info(handle_, &n, nullptr, nullptr));
+    return n;
+  }
+  int64_t n_subdomains() const
+  {
+    int64_t p = 0;
+    check(tpss_layout_info(handle_, nullptr, &p, nullptr));
+    return p;
+  }
+  int n_colors() const
+  {
+    int c = 0;
+    check(tpss_layout_info(handle_, nullptr, nullptr, &c));
+    return c;
+  }
+  const AdditionalData &get_additional_data() const { return additional_data_; }
+  tpss_layout *handle() const { return handle_; }
+
+private:
+  tpss_layout *handle_ = nullptr;
+  AdditionalData additional_data_;
+};
+
+class LaplaceOperator
+{
+public:
+  LaplaceOperator(std::shared_ptr<const SubdomainHandler> sh, double ip_factor = 1.)
+    : sh_(std::move(sh))
+  {
+    check(tpss_operator_create(sh_->handle(), ip_factor, &handle_));
+  }
+  LaplaceOperator(const LaplaceOperator &) = delete;
+  ~LaplaceOperator() { tpss_operator_destroy(handle_); }
+  int64_t m() const { return sh_->n_dofs(); }
+  int64_t n() const { return m(); }
+  void vmult(double *dst, const double *src, void *stream = nullptr) const
+  {
+    check(tpss_operator_vmult(handle_, dst, src, stream));
+  }
+  void Tvmult(double *dst, const double *src, void *stream = nullptr) const { vmult(dst, src, stream); }
+  tpss_operator *handle() const { return handle_; }
+
+private:
+  std::shared_ptr<const SubdomainHandler> sh_;
+  tpss_operator *handle_ = nullptr;
+};
+
+struct TimeInfo
+{
+  double time;
+  std::string description;
+  std::string unit = "[s]";
+  int64_t n_calls;
+};
+
+class SchwarzPreconditioner
+{
+public:
+  struct AdditionalData
+  {
+    double relaxation = 1.;
+    bool reverse = false;
+    bool symmetrized = false;
+    bool use_ras_weights = false;
+    bool use_ras_boolean_weights = false;
+    Precision precision = Precision::fp64;
+    double ip_factor = 1.;
+    bool check_finite = false;
+    int kernel_variant = TPSS_KERNEL_AUTO;
+  };
+
+  SchwarzPreconditioner() = default;
+  SchwarzPreconditioner(const SchwarzPreconditioner &) = delete;
+  SchwarzPreconditioner &operator=(const SchwarzPreconditioner &) = delete;
+  ~SchwarzPreconditioner() { clear(); }
+
+  void clear()
+  {
+    if(handle_) tpss_precond_destroy(handle_);
+    handle_ = nullptr;
+  }
+
+  void initialize(std::shared_ptr<const SubdomainHandler> sh, LaplaceOperator *op,
+                  const AdditionalData &ad)
+  {
+    clear();
+    const tpss_precond_desc d = desc(ad);
+    check(tpss_precond_create(sh->handle(), op ? op->handle() : nullptr, &d, &handle_));
+    sh_ = std::move(sh);
+    additional_data_ = ad;
+  }
+
+  /* shallow copy sharing the local solvers (schwarz_preconditioner.templates.h:63-86) */
+  void initialize(const SchwarzPreconditioner &other, const AdditionalData &ad)
+  {
+    clear();
+    const tpss_precond_desc d = desc(ad);
+    check(tpss_precond_create_shallow(other.handle_, &d, &handle_));
+    sh_ = other.sh_;
+    additional_data_ = ad;
+  }
+
+  void vmult(double *dst, const double *src, void *stream = nullptr) const
+  {
+    check(tpss_precond_vmult(handle_, dst, src, stream));
+  }
+  void vmult_add(double *dst, const double *src, void *stream = nullptr) const
+  {
+    check(tpss_precond_vmult_add(handle_, dst, src, stream));
+  }
+  void Tvmult(double *dst, const double *src, void *stream = nullptr) const
+  {
+    check(tpss_precond_Tvmult(handle_, dst, src, stream));
+  }
+
+  std::vector<TimeInfo> get_time_data() const
+  {
+    int n = 0;
+    check(tpss_precond_time_info(handle_, nullptr, &n));
+    std::vector<tpss_time_info> raw(n);
+    check(tpss_precond_time_info(handle_, raw.data(), &n));
+    std::vector<TimeInfo> out;
+    for(const auto &r : raw) out.push_back({r.time, r.description, "[s]", r.n_calls});
+    return out;
+  }
+
+  std::shared_ptr<const SubdomainHandler> get_subdomain_handler() const { return sh_; }
+  const AdditionalData &get_additional_data() const { return additional_data_; }
+  int64_t m() const { return sh_->n_dofs(); }
+  int64_t n() const { return m(); }
+  tpss_precond *handle() const { return handle_; }
+
+private:
+  static tpss_precond_desc desc(const AdditionalData &ad)
+  {
+    tpss_precond_desc d{};
+    d.relaxation = ad.relaxation;
+    d.reverse = ad.reverse;
+    d.symmetrized = ad.symmetrized;
+    d.use_ras_weights = ad.use_ras_weights;
+    d.use_ras_boolean_weights = ad.use_ras_boolean_weights;
+    d.precision = static_cast<int>(ad.precision);
+    d.ip_factor = ad.ip_factor;
+    d.check_finite = ad.check_finite;
+    d.kernel_variant = ad.kernel_variant;
+    return d;
+  }
+
+  tpss_precond *handle_ = nullptr;
+  std::shared_ptr<const SubdomainHandler> sh_;
+  AdditionalData additional_data_;
+};
+
+class SchwarzSmoother
+{
+public:
+  struct AdditionalData
+  {
+    unsigned int number_of_smoothing_steps = 1;
+    double damping_factor = 1.;
+  };
+
+  SchwarzSmoother() = default;
+  SchwarzSmoother(const SchwarzSmoother &) = delete;
+  ~SchwarzSmoother()
+  {
+    if(handle_) tpss_smoother_destroy(handle_);
+  }
+
+  void initialize(LaplaceOperator &op, std::shared_ptr<SchwarzPreconditioner> p,
+                  const AdditionalData &ad)
+  {
+    if(handle_) tpss_smoother_destroy(handle_);
+    handle_ = nullptr;
+    check(tpss_smoother_create(op.handle(), p->handle(), (int)ad.number_of_smoothing_steps,
+                               ad.damping_factor, &handle_));
+    precond_ = std::move(p);
+  }
+  void step(double *dst, const double *src, void *stream = nullptr) const
+  {
+    check(tpss_smoother_step(handle_, dst, src, stream));
+  }
+  void vmult(double *dst, const double *src, void *stream = nullptr) const
+  {
+    check(tpss_smoother_vmult(handle_, dst, src, stream));
+  }
+
+private:
+  tpss_smoother *handle_ = nullptr;
+  std::shared_ptr<SchwarzPreconditioner> precond_;
+};
+
+class MultigridSolver
+{
+public:
+  explicit MultigridSolver(const tpss_mg_desc &d) { check(tpss_mg_create(&d, &handle_)); }
+  MultigridSolver(const MultigridSolver &) = delete;
+  ~MultigridSolver() { tpss_mg_destroy(handle_); }
+  int64_t n_dofs() const
+  {
+    int64_t n = 0;
+    check(tpss_mg_n_dofs(handle_, &n));
+    return n;
+  }
+  void vmult(double *dst, const double *src, void *stream = nullptr) const
+  {
+    check(tpss_mg_vmult(handle_, dst, src, stream));
+  }
+  /* returns the CG iteration count; residual norms in `history` (max_iter + 1 entries) */
+  int solve(double *u, const double *f, double rel_tol, double abs_tol = 1e-14, int max_iter = 100,
+            std::vector<double> *history = nullptr, void *stream = nullptr) const
+  {
+    int it = 0;
+    std::vector<double> h(max_iter + 1);
+    check(tpss_mg_cg_solve(handle_, u, f, rel_tol, abs_tol, max_iter, &it, h.data(), stream));
+    if(history) *history = std::vector<double>(h.begin(), h.begin() + it + 1);
+    return it;
+  }
+
+private:
+  tpss_mg *handle_ = nullptr;
+};
+
+}  // namespace tpss_gpu

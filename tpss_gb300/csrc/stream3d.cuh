@@ -133,21 +133,20 @@ __device__ __forceinline__ void mpass(float *__restrict__ data, const float *__r
   }
 }
 
-// direction 2: S^T, divide by the eigenvalue sums, S
-template<int N, int NPAD, int ES, int NPT, int TPP>
-__device__ __forceinline__ void mpass_last(float *__restrict__ data, const float *__restrict__ ex,
-                                           const float *__restrict__ ey, const float *__restrict__ ez,
-                                           int q)
+// direction 2, forward: S^T along z, then division by the eigenvalue sums
+// lambda_x[i0] + lambda_y[i1] + lambda_z[i2]
+template<int N, int NPAD, int NPT, int TPP>
+__device__ __forceinline__ void mpass_divide(float *__restrict__ data, const float *__restrict__ ex,
+                                             const float *__restrict__ ey, const float *__restrict__ ez,
+                                             int q)
 {
   constexpr int stride = N * N;
-  float r[NPT][N], t[NPT][N];
-  int base[NPT];
+  float r[NPT][N];
   float lxy[NPT];
 #pragma unroll
   for(int j = 0; j < NPT; ++j)
   {
-    const int p = q + j * TPP;
-    base[j] = p;  // pencil along z: base = p (i0 + N i1)
+    const int p = q + j * TPP;  // pencil along z: i0 + N i1
     lxy[j] = ex[Entry<float, N>::LAM + p % N] + ey[Entry<float, N>::LAM + p / N];
 #pragma unroll
     for(int m = 0; m < N; ++m) r[j][m] = data[p + m * stride];
@@ -172,28 +171,7 @@ __device__ __forceinline__ void mpass_last(float *__restrict__ data, const float
     }
     const float lz = ez[Entry<float, N>::LAM + i];
 #pragma unroll
-    for(int j = 0; j < NPT; ++j) t[j][i] = acc[j] / (lxy[j] + lz);
-  }
-#pragma unroll
-  for(int i = 0; i < N; ++i)
-  {
-    const float4 *row = reinterpret_cast<const float4 *>(ez + Entry<float, N>::S + i * NPAD);
-    float acc[NPT];
-#pragma unroll
-    for(int j = 0; j < NPT; ++j) acc[j] = 0.f;
-#pragma unroll
-    for(int m4 = 0; m4 < NPAD / 4; ++m4)
-    {
-      const float4 v = row[m4];
-      const float vv[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-      for(int w = 0; w < 4; ++w)
-        if(m4 * 4 + w < N)
-#pragma unroll
-          for(int j = 0; j < NPT; ++j) acc[j] = fmaf(vv[w], t[j][m4 * 4 + w < N ? m4 * 4 + w : 0], acc[j]);
-    }
-#pragma unroll
-    for(int j = 0; j < NPT; ++j) data[base[j] + i * stride] = acc[j];
+    for(int j = 0; j < NPT; ++j) data[q + j * TPP + i * stride] = acc[j] / (lxy[j] + lz);
   }
 }
 
@@ -229,7 +207,7 @@ __device__ __forceinline__ void copy_layer_async(const StreamArgs &a, int x0, in
 __device__ __forceinline__ void wait_async_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
 template<class C>
-__global__ void __maxnreg__(C::THREADS <= 256 ? 224 : 160) stream_kernel(StreamArgs a)
+__global__ void __launch_bounds__(C::THREADS, 1) stream_kernel(StreamArgs a)
 {
   constexpr int K1 = C::K1, N = C::N, NLOC = C::NLOC, CD = C::CD, ES = C::ES, NPAD = C::NPAD;
   constexpr int BX = C::BX, BY = C::BY, BZ = C::BZ, TPP = C::TPP, NPT = C::NPT;
@@ -294,7 +272,9 @@ __global__ void __maxnreg__(C::THREADS <= 256 ? 224 : 160) stream_kernel(StreamA
       __syncthreads();
       if(active) mpass<N, NPAD, 1, NPT, TPP>(my, ey + Entry<float, N>::ST, q, 1.f);
       __syncthreads();
-      if(active) mpass_last<N, NPAD, ES, NPT, TPP>(my, ex, ey, ez, q);
+      if(active) mpass_divide<N, NPAD, NPT, TPP>(my, ex, ey, ez, q);
+      __syncthreads();
+      if(active) mpass<N, NPAD, 2, NPT, TPP>(my, ez + Entry<float, N>::S, q, 1.f);
       __syncthreads();
       if(active) mpass<N, NPAD, 1, NPT, TPP>(my, ey + Entry<float, N>::S, q, 1.f);
       __syncthreads();
