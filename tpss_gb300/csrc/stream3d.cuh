@@ -48,12 +48,20 @@ struct SCfg
   static constexpr int LAYER = LCELLS * CD;
   static constexpr int ES = Entry<float, N>::size;
   static constexpr int NPAD = Entry<float, N>::NPAD;
+  // padded patch layout (x + SX y + SXY z): chosen so that the pencils of a warp fall into
+  // distinct shared-memory banks in all three directions (at most 2-way conflicts)
+  static constexpr int SX = N == 10 ? 13 : N == 8 ? 9 : N == 6 ? 6 : N == 4 ? 5 : N;
+  static constexpr int SXY = N == 10 ? 137 : N == 8 ? 72 : N == 6 ? 39 : N == 4 ? 21 : N * N;
+  static constexpr int PSTRIDE = SXY * N;  // floats per patch work buffer
+  // element loops give every thread one fixed cell-local DoF e (no div/mod per element)
+  static constexpr int G = THREADS / CD;   // thread groups sharing an e
+  static_assert(G >= 1, "need at least one thread per cell DoF");
   // shared memory carve-up (in floats; the staged FP64 cell layers take two floats per value)
   static constexpr int OFF_FD = 0;                                   // (BX + BY + BZ) entries
   static constexpr int OFF_RAW = ((OFF_FD + (BX + BY + BZ) * ES + 3) / 4) * 4;  // 3 FP64 layers
   static constexpr int OFF_ACC = OFF_RAW + 3 * 2 * LAYER;            // 2 FP32 layers
   static constexpr int OFF_WORK = OFF_ACC + 2 * LAYER;               // NPATCH patches
-  static constexpr int FLOATS = OFF_WORK + NPATCH * NLOC;
+  static constexpr int FLOATS = OFF_WORK + NPATCH * PSTRIDE;
   static constexpr size_t smem_bytes() { return (size_t)FLOATS * 4; }
 };
 
@@ -96,17 +104,25 @@ __device__ __forceinline__ float multiplicity(int c, int n)
   return float((c >= 1 ? 1 : 0) + (c + 1 <= n - 1 ? 1 : 0));
 }
 
-template<int N, int NPAD, int DIR, int NPT, int TPP>
+// base offset of pencil p along DIR in the padded layout x + SX y + SXY z
+template<int N, int SX, int SXY, int DIR>
+__device__ __forceinline__ int pbase(int p)
+{
+  const int a = p % N, b = p / N;
+  return DIR == 0 ? SX * a + SXY * b : DIR == 1 ? a + SXY * b : a + SX * b;
+}
+
+template<int N, int SX, int SXY, int NPAD, int DIR, int NPT, int TPP>
 __device__ __forceinline__ void mpass(float *__restrict__ data, const float *__restrict__ B, int q,
                                       float scale)
 {
-  constexpr int stride = cpow(N, DIR);
+  constexpr int stride = DIR == 0 ? 1 : DIR == 1 ? SX : SXY;
   float r[NPT][N];
   int base[NPT];
 #pragma unroll
   for(int j = 0; j < NPT; ++j)
   {
-    base[j] = fd::pencil_base<3, N, DIR>(q + j * TPP);
+    base[j] = pbase<N, SX, SXY, DIR>(q + j * TPP);
 #pragma unroll
     for(int m = 0; m < N; ++m) r[j][m] = data[base[j] + m * stride];
   }
@@ -135,21 +151,23 @@ __device__ __forceinline__ void mpass(float *__restrict__ data, const float *__r
 
 // direction 2, forward: S^T along z, then division by the eigenvalue sums
 // lambda_x[i0] + lambda_y[i1] + lambda_z[i2]
-template<int N, int NPAD, int NPT, int TPP>
+template<int N, int SX, int SXY, int NPAD, int NPT, int TPP>
 __device__ __forceinline__ void mpass_divide(float *__restrict__ data, const float *__restrict__ ex,
                                              const float *__restrict__ ey, const float *__restrict__ ez,
                                              int q)
 {
-  constexpr int stride = N * N;
+  constexpr int stride = SXY;
   float r[NPT][N];
   float lxy[NPT];
+  int base[NPT];
 #pragma unroll
   for(int j = 0; j < NPT; ++j)
   {
     const int p = q + j * TPP;  // pencil along z: i0 + N i1
+    base[j] = pbase<N, SX, SXY, 2>(p);
     lxy[j] = ex[Entry<float, N>::LAM + p % N] + ey[Entry<float, N>::LAM + p / N];
 #pragma unroll
-    for(int m = 0; m < N; ++m) r[j][m] = data[p + m * stride];
+    for(int m = 0; m < N; ++m) r[j][m] = data[base[j] + m * stride];
   }
 #pragma unroll
   for(int i = 0; i < N; ++i)
@@ -171,7 +189,7 @@ __device__ __forceinline__ void mpass_divide(float *__restrict__ data, const flo
     }
     const float lz = ez[Entry<float, N>::LAM + i];
 #pragma unroll
-    for(int j = 0; j < NPT; ++j) data[q + j * TPP + i * stride] = acc[j] / (lxy[j] + lz);
+    for(int j = 0; j < NPT; ++j) data[base[j] + i * stride] = acc[j] / (lxy[j] + lz);
   }
 }
 
@@ -186,39 +204,72 @@ __device__ __forceinline__ int64_t cell_first(const StreamArgs &a, int cx, int c
 // [x0, x0+bx], y in [y0, y0+by]) into the FP64 staging buffer; cells outside are zero-filled
 template<class C>
 __device__ __forceinline__ void copy_layer_async(const StreamArgs &a, int x0, int y0, int bx, int by,
-                                                 int cz, double *raw)
+                                                 int cz, double *raw, int e, int g)
 {
-  for(int i = threadIdx.x; i < C::LAYER; i += C::THREADS)
-  {
-    const int cell = i / C::CD, e = i % C::CD;
-    const int lx = cell % C::CX, ly = cell / C::CX;
-    if(lx <= bx && ly <= by)
+  if(g < C::G)
+    for(int cell = g; cell < C::LCELLS; cell += C::G)
     {
-      const double *g = a.src + cell_first<C>(a, x0 + lx, y0 + ly, cz) + e;
-      const unsigned saddr = (unsigned)__cvta_generic_to_shared(raw + i);
-      asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(saddr), "l"(g) : "memory");
+      const int lx = cell % C::CX, ly = cell / C::CX;
+      const int i = cell * C::CD + e;
+      if(lx <= bx && ly <= by)
+      {
+        const double *src = a.src + cell_first<C>(a, x0 + lx, y0 + ly, cz) + e;
+        const unsigned saddr = (unsigned)__cvta_generic_to_shared(raw + i);
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(saddr), "l"(src) : "memory");
+      }
+      else
+        raw[i] = 0.0;
     }
-    else
-      raw[i] = 0.0;
-  }
   asm volatile("cp.async.commit_group;\n" ::: "memory");
 }
 
 __device__ __forceinline__ void wait_async_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
+// write one completed cell layer: cells owned by the item to dst, shared cells to the halo
+template<class C>
+__device__ __forceinline__ void write_layer(const StreamArgs &a, float *accl, int item, int lz, int cz,
+                                            bool zshared, int tx, int ty, int x0, int y0, int bx,
+                                            int by, int e, int g, bool clear)
+{
+  if(g >= C::G) return;
+  for(int cell = g; cell < C::LCELLS; cell += C::G)
+  {
+    const int lx = cell % C::CX, ly = cell / C::CX;
+    if(lx > bx || ly > by) continue;
+    const int i = cell * C::CD + e;
+    const bool xs = (lx == 0 && tx > 0) || (lx == bx && tx < a.T[0] - 1);
+    const bool ys = (ly == 0 && ty > 0) || (ly == by && ty < a.T[1] - 1);
+    float v = accl[i];
+    if(xs || ys || zshared)
+      a.halo[((size_t)item * (C::BZ + 1) * C::LCELLS + (size_t)lz * C::LCELLS + cell) * C::CD + e] = v;
+    else
+    {
+      const int cx = x0 + lx, cy = y0 + ly;
+      if(a.ras)
+        v /= multiplicity(cx, a.nc[0]) * multiplicity(cy, a.nc[1]) * multiplicity(cz, a.nc[2]);
+      a.dst[cell_first<C>(a, cx, cy, cz) + e] = double(v);
+    }
+    if(clear) accl[i] = 0.f;
+  }
+}
+
 template<class C>
 __global__ void __launch_bounds__(C::THREADS, 1) stream_kernel(StreamArgs a)
 {
-  constexpr int K1 = C::K1, N = C::N, NLOC = C::NLOC, CD = C::CD, ES = C::ES, NPAD = C::NPAD;
+  constexpr int K1 = C::K1, N = C::N, CD = C::CD, ES = C::ES, NPAD = C::NPAD;
   constexpr int BX = C::BX, BY = C::BY, BZ = C::BZ, TPP = C::TPP, NPT = C::NPT;
+  constexpr int SX = C::SX, SXY = C::SXY, PS = C::PSTRIDE;
   extern __shared__ __align__(16) float sm[];
   float *s_fd = sm + C::OFF_FD;
   double *s_raw = reinterpret_cast<double *>(sm + C::OFF_RAW);
   float *s_acc = sm + C::OFF_ACC;
   float *s_work = sm + C::OFF_WORK;
   const int tid = threadIdx.x;
-  const int slot = tid / TPP, q = tid % TPP;  // patch slot (px + BX py) and pencil group
+  const int slot = tid / TPP, q = tid % TPP;  // FD passes: patch slot (px + BX py), pencil group
   const int px = slot % BX, py = slot / BX;
+  // element loops: fixed cell-local DoF e and its patch-local offset
+  const int e = tid % CD, g = tid / CD;
+  const int e_patch = (e % K1) + SX * ((e / K1) % K1) + SXY * (e / (K1 * K1));
   const int n_items = a.T[0] * a.T[1] * a.T[2];
 
   for(int item = blockIdx.x; item < n_items; item += gridDim.x)
@@ -228,133 +279,83 @@ __global__ void __launch_bounds__(C::THREADS, 1) stream_kernel(StreamArgs a)
     const int bx = min(BX, a.nc[0] - 1 - BX * tx), by = min(BY, a.nc[1] - 1 - BY * ty);
     const int bz = min(BZ, a.nc[2] - 1 - BZ * tz);
     const int x0 = BX * tx, y0 = BY * ty, z0 = BZ * tz;  // first cell of the item
-    __syncthreads();  // previous item done with shared memory
-    // FD entries: x vertices, y vertices, z vertices of the item
+    __syncthreads();  // the previous item is done with shared memory
     for(int i = tid; i < (BX + BY + BZ) * ES; i += C::THREADS)
     {
-      const int s = i / ES, o = i % ES;
-      int e = -1;
-      if(s < BX) { if(s < bx) e = a.vfd[0][x0 + 1 + s]; }
-      else if(s < BX + BY) { if(s - BX < by) e = a.vfd[1][y0 + 1 + (s - BX)]; }
-      else if(s - BX - BY < bz) e = a.vfd[2][z0 + 1 + (s - BX - BY)];
-      s_fd[i] = e >= 0 ? a.fd[(size_t)e * ES + o] : 0.f;
+      const int sl = i / ES, o = i % ES;
+      int en = -1;
+      if(sl < BX) { if(sl < bx) en = a.vfd[0][x0 + 1 + sl]; }
+      else if(sl < BX + BY) { if(sl - BX < by) en = a.vfd[1][y0 + 1 + (sl - BX)]; }
+      else if(sl - BX - BY < bz) en = a.vfd[2][z0 + 1 + (sl - BX - BY)];
+      s_fd[i] = en >= 0 ? a.fd[(size_t)en * ES + o] : 0.f;
     }
-    // cell layers 0 and 1 of the item, zero accumulators
-    copy_layer_async<C>(a, x0, y0, bx, by, z0, s_raw);
-    copy_layer_async<C>(a, x0, y0, bx, by, z0 + 1, s_raw + C::LAYER);
+    copy_layer_async<C>(a, x0, y0, bx, by, z0, s_raw, e, g);
+    copy_layer_async<C>(a, x0, y0, bx, by, z0 + 1, s_raw + C::LAYER, e, g);
     for(int i = tid; i < 2 * C::LAYER; i += C::THREADS) s_acc[i] = 0.f;
     wait_async_all();
     __syncthreads();
 
     for(int j = 0; j < bz; ++j)
     {
-      // vertex layer j: cell layers j (ring slot j%3 / acc j%2) and j+1
       // layer j+2 streams in while this vertex layer is solved (its ring slot held layer j-1)
       const bool more = j + 2 <= bz;
-      if(more) copy_layer_async<C>(a, x0, y0, bx, by, z0 + j + 2, s_raw + ((j + 2) % 3) * C::LAYER);
+      if(more) copy_layer_async<C>(a, x0, y0, bx, by, z0 + j + 2, s_raw + ((j + 2) % 3) * C::LAYER, e, g);
       const double *lo = s_raw + (j % 3) * C::LAYER, *hi = s_raw + ((j + 1) % 3) * C::LAYER;
-      // gather the BX x BY patches of this layer into the work buffers
-      for(int i = tid; i < C::NPATCH * NLOC; i += C::THREADS)
-      {
-        const int s = i / NLOC, r = i % NLOC;
-        const int sx = s % BX, sy = s / BX;
-        const int ix = r % N, iy = (r / N) % N, iz = r / (N * N);
-        const int ox = ix / K1, oy = iy / K1, oz = iz / K1;
-        const int e = (ix % K1) + K1 * ((iy % K1) + K1 * (iz % K1));
-        const double *layer = oz ? hi : lo;
-        s_work[i] = (sx < bx && sy < by) ? float(layer[((sx + ox) + C::CX * (sy + oy)) * CD + e]) : 0.f;
-      }
+      // gather: (patch, cell offset) combos, fixed e per thread
+      if(g < C::G)
+        for(int c = g; c < C::NPATCH * 8; c += C::G)
+        {
+          const int sl = c >> 3, ox = c & 1, oy = (c >> 1) & 1, oz = (c >> 2) & 1;
+          const int sx = sl % BX, sy = sl / BX;
+          if(sx >= bx || sy >= by) continue;
+          const double *layer = oz ? hi : lo;
+          s_work[sl * PS + e_patch + K1 * (ox + SX * oy + SXY * oz)] =
+            float(layer[((sx + ox) + C::CX * (sy + oy)) * CD + e]);
+        }
       __syncthreads();
       const bool active = px < bx && py < by;
-      float *my = s_work + slot * NLOC;
+      float *my = s_work + slot * PS;
       const float *ex = s_fd + px * ES, *ey = s_fd + (BX + py) * ES, *ez = s_fd + (BX + BY + j) * ES;
-      if(active) mpass<N, NPAD, 0, NPT, TPP>(my, ex + Entry<float, N>::ST, q, 1.f);
+      if(active) mpass<N, SX, SXY, NPAD, 0, NPT, TPP>(my, ex + Entry<float, N>::ST, q, 1.f);
       __syncthreads();
-      if(active) mpass<N, NPAD, 1, NPT, TPP>(my, ey + Entry<float, N>::ST, q, 1.f);
+      if(active) mpass<N, SX, SXY, NPAD, 1, NPT, TPP>(my, ey + Entry<float, N>::ST, q, 1.f);
       __syncthreads();
-      if(active) mpass_divide<N, NPAD, NPT, TPP>(my, ex, ey, ez, q);
+      if(active) mpass_divide<N, SX, SXY, NPAD, NPT, TPP>(my, ex, ey, ez, q);
       __syncthreads();
-      if(active) mpass<N, NPAD, 2, NPT, TPP>(my, ez + Entry<float, N>::S, q, 1.f);
+      if(active) mpass<N, SX, SXY, NPAD, 2, NPT, TPP>(my, ez + Entry<float, N>::S, q, 1.f);
       __syncthreads();
-      if(active) mpass<N, NPAD, 1, NPT, TPP>(my, ey + Entry<float, N>::S, q, 1.f);
+      if(active) mpass<N, SX, SXY, NPAD, 1, NPT, TPP>(my, ey + Entry<float, N>::S, q, 1.f);
       __syncthreads();
-      if(active) mpass<N, NPAD, 0, NPT, TPP>(my, ex + Entry<float, N>::S, q, a.omega);
+      if(active) mpass<N, SX, SXY, NPAD, 0, NPT, TPP>(my, ex + Entry<float, N>::S, q, a.omega);
       __syncthreads();
-      // accumulate: four x/y parity classes, patches within a class do not share cells
+      // accumulate per cell: the (up to) 4 patches of this layer touching the cell, fixed order
       float *alo = s_acc + (j % 2) * C::LAYER, *ahi = s_acc + ((j + 1) % 2) * C::LAYER;
-#pragma unroll 1
-      for(int par = 0; par < 4; ++par)
-      {
-        for(int i = tid; i < C::NPATCH * NLOC; i += C::THREADS)
+      if(g < C::G)
+        for(int cl = g; cl < 2 * C::LCELLS; cl += C::G)
         {
-          const int s = i / NLOC, r = i % NLOC;
-          const int sx = s % BX, sy = s / BX;
-          if((sx & 1) + 2 * (sy & 1) != par || sx >= bx || sy >= by) continue;
-          const int ix = r % N, iy = (r / N) % N, iz = r / (N * N);
-          const int ox = ix / K1, oy = iy / K1, oz = iz / K1;
-          const int e = (ix % K1) + K1 * ((iy % K1) + K1 * (iz % K1));
-          float *layer = oz ? ahi : alo;
-          layer[((sx + ox) + C::CX * (sy + oy)) * CD + e] += s_work[i];
-        }
-        __syncthreads();
-      }
-      // cell layer j is complete: write it out, clear its accumulator for layer j+2
-      {
-        const int lz = j, cz = z0 + j;
-        const bool zshared = (lz == 0 && tz > 0);  // lz == bz handled after the loop
-        for(int i = tid; i < C::LAYER; i += C::THREADS)
-        {
-          const int cell = i / CD, e = i % CD;
+          const int L = cl >= C::LCELLS, cell = cl - L * C::LCELLS;
           const int lx = cell % C::CX, ly = cell / C::CX;
-          if(lx > bx || ly > by) continue;
-          const bool xs = (lx == 0 && tx > 0) || (lx == bx && tx < a.T[0] - 1);
-          const bool ys = (ly == 0 && ty > 0) || (ly == by && ty < a.T[1] - 1);
-          float v = alo[i];
-          if(xs || ys || zshared)
-          {
-            float *h = a.halo + ((size_t)item * (BZ + 1) * C::LCELLS + (size_t)lz * C::LCELLS + cell) * CD;
-            h[e] = v;
-          }
-          else
-          {
-            const int cx = x0 + lx, cy = y0 + ly;
-            if(a.ras)
-              v /= multiplicity(cx, a.nc[0]) * multiplicity(cy, a.nc[1]) * multiplicity(cz, a.nc[2]);
-            a.dst[cell_first<C>(a, cx, cy, cz) + e] = double(v);
-          }
-          alo[i] = 0.f;
+          float sum = 0.f;
+#pragma unroll
+          for(int oy = 1; oy >= 0; --oy)
+#pragma unroll
+            for(int ox = 1; ox >= 0; --ox)
+            {
+              const int sx = lx - ox, sy = ly - oy;
+              if(sx >= 0 && sx < bx && sy >= 0 && sy < by)
+                sum += s_work[(sx + BX * sy) * PS + e_patch + K1 * (ox + SX * oy + SXY * L)];
+            }
+          (L ? ahi : alo)[cell * CD + e] += sum;
         }
-      }
+      __syncthreads();
+      // cell layer j is complete: write it, clear its accumulator for layer j+2
+      write_layer<C>(a, alo, item, j, z0 + j, j == 0 && tz > 0, tx, ty, x0, y0, bx, by, e, g, true);
       if(more) wait_async_all();
       __syncthreads();
     }
-    // last cell layer bz
-    {
-      const int lz = bz, cz = z0 + bz;
-      const bool zshared = tz < a.T[2] - 1;
-      const float *alast = s_acc + (bz % 2) * C::LAYER;
-      for(int i = tid; i < C::LAYER; i += C::THREADS)
-      {
-        const int cell = i / CD, e = i % CD;
-        const int lx = cell % C::CX, ly = cell / C::CX;
-        if(lx > bx || ly > by) continue;
-        const bool xs = (lx == 0 && tx > 0) || (lx == bx && tx < a.T[0] - 1);
-        const bool ys = (ly == 0 && ty > 0) || (ly == by && ty < a.T[1] - 1);
-        float v = alast[i];
-        if(xs || ys || zshared)
-        {
-          float *h = a.halo + ((size_t)item * (BZ + 1) * C::LCELLS + (size_t)lz * C::LCELLS + cell) * CD;
-          h[e] = v;
-        }
-        else
-        {
-          const int cx = x0 + lx, cy = y0 + ly;
-          if(a.ras)
-            v /= multiplicity(cx, a.nc[0]) * multiplicity(cy, a.nc[1]) * multiplicity(cz, a.nc[2]);
-          a.dst[cell_first<C>(a, cx, cy, cz) + e] = double(v);
-        }
-      }
-    }
+    // last cell layer of the item
+    write_layer<C>(a, s_acc + (bz % 2) * C::LAYER, item, bz, z0 + bz, tz < a.T[2] - 1, tx, ty, x0,
+                   y0, bx, by, e, g, false);
   }
 }
 
