@@ -335,6 +335,7 @@ def run_ours(args):
     if not args.no_e2e:
         out["e2e"] = e2e(tpss, p, src_h, args, W, world, dist)
     if not args.no_solve:
+        out["operator"] = operator_time(tpss, sh, src, W)
         out["solve"] = solve_times(tpss, args)
     if rank == 0 and not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline(args, W)
@@ -385,6 +386,29 @@ def e2e(tpss, p, src_h, args, W, world, dist):
         ms = float(t.item())
     return {"value": world * N / (ms * 1e-3), "unit": "DoF/s", "h2d_bytes_per_step": N * 8,
             "d2h_bytes_per_step": N * 8, "ms_per_step": ms, "steps": steps}
+
+
+def operator_time(tpss, sh, src, W):
+    """FP64 matrix-free SIPG operator (MF::Operator::vmult) on the same level: the residual
+    inside every smoothing step and CG iteration."""
+    import torch
+    op = tpss.LaplaceOperator(sh, 1.0)
+    dst = torch.empty_like(src)
+    for _ in range(3):
+        op.vmult(dst, src)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 10
+    e0.record()
+    for _ in range(reps):
+        op.vmult(dst, src)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    k, dim = sh.get_additional_data().degree, sh.get_additional_data().dim
+    cells = W["N"] // (k + 1) ** dim
+    fma_cell = 3 * dim * dim * (k + 1) ** (dim + 1)  # 3 dim neighbour terms x dim contractions
+    return {"ms": ms, "dof_per_s": W["N"] / (ms * 1e-3), "fp64_tflops": 2 * fma_cell * cells / (ms * 1e-3) / 1e12}
 
 
 def solve_times(tpss, args):

@@ -149,6 +149,48 @@ __device__ __forceinline__ void mpass(float *__restrict__ data, const float *__r
   }
 }
 
+// direction 0, forward, reading the patch straight from the two staged FP64 cell layers:
+// pencil (y, z) of patch (px, py) covers cells (px, px+1) of row (py + y/K1) in layer z/K1
+template<int K1, int N, int SX, int SXY, int NPAD, int NPT, int TPP, int CX, int CD>
+__device__ __forceinline__ void mpass_x_from_layers(float *__restrict__ data, const double *__restrict__ lo,
+                                                    const double *__restrict__ hi,
+                                                    const float *__restrict__ St, int px, int py, int q)
+{
+  float r[NPT][N];
+  int base[NPT];
+#pragma unroll
+  for(int j = 0; j < NPT; ++j)
+  {
+    const int p = q + j * TPP, y = p % N, z = p / N;
+    base[j] = SX * y + SXY * z;
+    const double *layer = z >= K1 ? hi : lo;
+    const int row = (px + CX * (py + y / K1)) * CD + K1 * (y % K1) + K1 * K1 * (z % K1);
+#pragma unroll
+    for(int m = 0; m < N; ++m) r[j][m] = float(layer[row + (m / K1) * CD + (m % K1)]);
+  }
+#pragma unroll
+  for(int i = 0; i < N; ++i)
+  {
+    const float4 *rw = reinterpret_cast<const float4 *>(St + i * NPAD);
+    float acc[NPT];
+#pragma unroll
+    for(int j = 0; j < NPT; ++j) acc[j] = 0.f;
+#pragma unroll
+    for(int m4 = 0; m4 < NPAD / 4; ++m4)
+    {
+      const float4 v = rw[m4];
+      const float vv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+      for(int w = 0; w < 4; ++w)
+        if(m4 * 4 + w < N)
+#pragma unroll
+          for(int j = 0; j < NPT; ++j) acc[j] = fmaf(vv[w], r[j][m4 * 4 + w < N ? m4 * 4 + w : 0], acc[j]);
+    }
+#pragma unroll
+    for(int j = 0; j < NPT; ++j) data[base[j] + i] = acc[j];
+  }
+}
+
 // direction 2, forward: S^T along z, then division by the eigenvalue sums
 // lambda_x[i0] + lambda_y[i1] + lambda_z[i2]
 template<int N, int SX, int SXY, int NPAD, int NPT, int TPP>
@@ -189,7 +231,7 @@ __device__ __forceinline__ void mpass_divide(float *__restrict__ data, const flo
     }
     const float lz = ez[Entry<float, N>::LAM + i];
 #pragma unroll
-    for(int j = 0; j < NPT; ++j) data[base[j] + i * stride] = acc[j] / (lxy[j] + lz);
+    for(int j = 0; j < NPT; ++j) data[base[j] + i * stride] = __fdividef(acc[j], lxy[j] + lz);
   }
 }
 
@@ -301,22 +343,12 @@ __global__ void __launch_bounds__(C::THREADS, 1) stream_kernel(StreamArgs a)
       const bool more = j + 2 <= bz;
       if(more) copy_layer_async<C>(a, x0, y0, bx, by, z0 + j + 2, s_raw + ((j + 2) % 3) * C::LAYER, e, g);
       const double *lo = s_raw + (j % 3) * C::LAYER, *hi = s_raw + ((j + 1) % 3) * C::LAYER;
-      // gather: (patch, cell offset) combos, fixed e per thread
-      if(g < C::G)
-        for(int c = g; c < C::NPATCH * 8; c += C::G)
-        {
-          const int sl = c >> 3, ox = c & 1, oy = (c >> 1) & 1, oz = (c >> 2) & 1;
-          const int sx = sl % BX, sy = sl / BX;
-          if(sx >= bx || sy >= by) continue;
-          const double *layer = oz ? hi : lo;
-          s_work[sl * PS + e_patch + K1 * (ox + SX * oy + SXY * oz)] =
-            float(layer[((sx + ox) + C::CX * (sy + oy)) * CD + e]);
-        }
-      __syncthreads();
       const bool active = px < bx && py < by;
       float *my = s_work + slot * PS;
       const float *ex = s_fd + px * ES, *ey = s_fd + (BX + py) * ES, *ez = s_fd + (BX + BY + j) * ES;
-      if(active) mpass<N, SX, SXY, NPAD, 0, NPT, TPP>(my, ex + Entry<float, N>::ST, q, 1.f);
+      if(active)
+        mpass_x_from_layers<K1, N, SX, SXY, NPAD, NPT, TPP, C::CX, CD>(my, lo, hi, ex + Entry<float, N>::ST,
+                                                                      px, py, q);
       __syncthreads();
       if(active) mpass<N, SX, SXY, NPAD, 1, NPT, TPP>(my, ey + Entry<float, N>::ST, q, 1.f);
       __syncthreads();
