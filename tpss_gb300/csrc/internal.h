@@ -144,6 +144,8 @@ void patch_matrices_1d(const Shape1D &s, int ncp, const double *h, bool bdry_lo,
 // global 1-D SIPG blocks of one direction: mass[c][np^2], blk[c][3][np^2]
 void operator_blocks_1d(const Shape1D &s, int nc, const double *h, double ip,
                         std::vector<double> &mass, std::vector<double> &blk);
+// per-cell 1-D factors of the operator: mass, own block, rank-2 neighbour couplings
+std::vector<double> operator_factors_1d(const Shape1D &s, int nc, const double *h, double ip);
 // child embedding E[s][i*np+j] = phi_j((z_i+s)/2)
 std::vector<double> embedding_1d(const Shape1D &s);
 
@@ -192,6 +194,7 @@ struct tpss_operator
   const tpss_layout *layout = nullptr;
   double ip = 1.0;
   tpss::DeviceBuffer<double> d_mass[3], d_blk[3];
+  tpss::DeviceBuffer<double> d_fac[3];  // operator_factors_1d per direction
   int nblk_cells[3] = {0, 0, 0};
 };
 

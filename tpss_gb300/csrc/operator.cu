@@ -57,8 +57,7 @@ struct OpArgs
   const double *__restrict__ src;
   double *__restrict__ dst;
   const int64_t *__restrict__ cell_start;  // nullptr = lexicographic
-  const double *__restrict__ mass[3];      // [nc[d]][NP*NP]
-  const double *__restrict__ blk[3];       // [nc[d]][3][NP*NP]
+  const double *__restrict__ fac[3];       // operator_factors_1d per direction
   int nc[3];
   int64_t n_cells;
 };
@@ -68,89 +67,144 @@ struct OpCfg
 {
   static constexpr int ND = cpow(NP, DIM);
   static constexpr int NPENC = ND / NP;
-  static constexpr int CPB = NPENC >= 64 ? 1 : (64 + NPENC - 1) / NPENC;  // cells per block
+  static constexpr int CPB = NPENC >= 128 ? 1 : 128 / NPENC;  // cells per block
   static constexpr int THREADS = ((CPB * NPENC + 31) / 32) * 32;
+  static constexpr int FS = 2 * NP * NP + 8 * NP;  // factor stride per cell and direction
 };
 
+// Kronecker-sum application per direction d:
+//   X_d = C_d u_c + sum_{r<2} aR_r (bR_r . u_{c+e_d}) + sum_{r<2} aL_r (bL_r . u_{c-e_d})   (along d)
+//   out += (mass along the other directions) X_d
+// The neighbour couplings are rank two, so a neighbour costs two dot products per pencil
+// instead of a full n x n contraction.
 template<int DIM, int NP>
 __global__ void __launch_bounds__(OpCfg<DIM, NP>::THREADS) sipg_kernel(OpArgs a)
 {
   using C = OpCfg<DIM, NP>;
-  constexpr int ND = C::ND, CPB = C::CPB, NPENC = C::NPENC;
-  __shared__ double s_buf[CPB * ND];
-  __shared__ double s_acc[CPB * ND];
-  __shared__ double s_mat[CPB * DIM * NP * NP];
-  __shared__ int64_t s_src[CPB];
+  constexpr int ND = C::ND, CPB = C::CPB, NPENC = C::NPENC, FS = C::FS;
+  __shared__ double s_x[CPB * ND];
+  __shared__ double s_out[CPB * ND];
+  __shared__ double s_fac[CPB * DIM * FS];
+  __shared__ int64_t s_first[CPB][3][3];  // [cell][direction][left, self, right]
   const int tid = threadIdx.x, slot = tid / NPENC, p = tid % NPENC;
   for(int64_t c0 = (int64_t)blockIdx.x * CPB; c0 < a.n_cells; c0 += (int64_t)gridDim.x * CPB)
   {
-    for(int i = tid; i < CPB * ND; i += C::THREADS) s_acc[i] = 0.0;
-    for(int term = 0; term < 3 * DIM; ++term)
-    {
-      const int d = term / 3, o = term % 3 - 1;
-      __syncthreads();
-      if(tid < CPB)
-      {
-        const int64_t cell = c0 + tid;
-        int64_t src_first = -1;
-        if(cell < a.n_cells)
-        {
-          int c[3] = {(int)(cell % a.nc[0]), (int)((cell / a.nc[0]) % a.nc[1]),
-                      (int)(cell / ((int64_t)a.nc[0] * a.nc[1]))};
-          const int cn = c[d] + o;
-          if(cn >= 0 && cn < a.nc[d])
-          {
-            c[d] = cn;
-            const int64_t nb = c[0] + (int64_t)a.nc[0] * (c[1] + (int64_t)a.nc[1] * c[2]);
-            src_first = a.cell_start ? a.cell_start[nb] : nb * ND;
-          }
-        }
-        s_src[tid] = src_first;
-      }
-      // matrices of this term: direction e uses the 1-D SIPG block (e == d) or the mass
-      for(int i = tid; i < CPB * DIM * NP * NP; i += C::THREADS)
-      {
-        const int s = i / (DIM * NP * NP), e = (i / (NP * NP)) % DIM, q = i % (NP * NP);
-        const int64_t cell = c0 + s;
-        double v = 0.0;
-        if(cell < a.n_cells)
-        {
-          const int ce = e == 0 ? (int)(cell % a.nc[0])
-                       : e == 1 ? (int)((cell / a.nc[0]) % a.nc[1])
-                                : (int)(cell / ((int64_t)a.nc[0] * a.nc[1]));
-          v = e == d ? a.blk[e][((size_t)ce * 3 + (o + 1)) * NP * NP + q]
-                     : a.mass[e][(size_t)ce * NP * NP + q];
-        }
-        s_mat[i] = v;
-      }
-      __syncthreads();
-      for(int i = tid; i < CPB * ND; i += C::THREADS)
-      {
-        const int s = i / ND;
-        const int64_t f = s_src[s];
-        s_buf[i] = f >= 0 ? a.src[f + (i % ND)] : 0.0;
-      }
-      __syncthreads();
-      const bool active = slot < CPB && s_src[slot < CPB ? slot : 0] >= 0;
-      for(int e = 0; e < DIM; ++e)
-      {
-        if(active) pencil_dir<DIM, NP, false>(e, s_buf + slot * ND, s_mat + (slot * DIM + e) * NP * NP, p);
-        __syncthreads();
-      }
-      for(int i = tid; i < CPB * ND; i += C::THREADS)
-        if(s_src[i / ND] >= 0) s_acc[i] += s_buf[i];
-    }
     __syncthreads();
-    for(int i = tid; i < CPB * ND; i += C::THREADS)
+    for(int i = tid; i < CPB * DIM * FS; i += C::THREADS)
     {
-      const int64_t cell = c0 + i / ND;
+      const int s = i / (DIM * FS), d = (i / FS) % DIM, o = i % FS;
+      const int64_t cell = c0 + s;
+      double v = 0.0;
       if(cell < a.n_cells)
       {
-        const int64_t f = a.cell_start ? a.cell_start[cell] : cell * ND;
-        a.dst[f + i % ND] = s_acc[i];
+        const int cd = d == 0 ? (int)(cell % a.nc[0]) : d == 1 ? (int)((cell / a.nc[0]) % a.nc[1])
+                                                               : (int)(cell / ((int64_t)a.nc[0] * a.nc[1]));
+        v = a.fac[d][(size_t)cd * FS + o];
+      }
+      s_fac[i] = v;
+    }
+    for(int i3 = tid; i3 < CPB * DIM * 3; i3 += C::THREADS)
+    {
+      const int s = i3 / (DIM * 3), d = (i3 / 3) % DIM, o = i3 % 3 - 1;
+      const int64_t cell = c0 + s;
+      int64_t f = -1;
+      if(cell < a.n_cells)
+      {
+        int c[3] = {(int)(cell % a.nc[0]), (int)((cell / a.nc[0]) % a.nc[1]),
+                    (int)(cell / ((int64_t)a.nc[0] * a.nc[1]))};
+        c[d] += o;
+        if(c[d] >= 0 && c[d] < a.nc[d])
+        {
+          const int64_t nb = c[0] + (int64_t)a.nc[0] * (c[1] + (int64_t)a.nc[1] * c[2]);
+          f = a.cell_start ? a.cell_start[nb] : nb * ND;
+        }
+      }
+      s_first[s][d][o + 1] = f;
+    }
+    for(int i = tid; i < CPB * ND; i += C::THREADS) s_out[i] = 0.0;
+    __syncthreads();
+    const bool active = slot < CPB && c0 + (slot < CPB ? slot : 0) < a.n_cells;
+#pragma unroll
+    for(int d = 0; d < DIM; ++d)
+    {
+      if(active)
+      {
+        const int stride = d == 0 ? 1 : d == 1 ? NP : NP * NP;
+        const int base = (p % stride) + (p / stride) * stride * NP;
+        const double *F = s_fac + (slot * DIM + d) * FS;
+        const double *Cm = F + NP * NP, *aL = F + 2 * NP * NP, *bL = aL + 2 * NP, *aR = bL + 2 * NP,
+                     *bR = aR + 2 * NP;
+        double u[NP], x[NP];
+        const double *uc = a.src + s_first[slot][d][1] + base;
+#pragma unroll
+        for(int m = 0; m < NP; ++m) u[m] = uc[m * stride];
+#pragma unroll
+        for(int i = 0; i < NP; ++i)
+        {
+          double acc = 0.0;
+#pragma unroll
+          for(int m = 0; m < NP; ++m) acc = fma(Cm[i * NP + m], u[m], acc);
+          x[i] = acc;
+        }
+#pragma unroll
+        for(int side = 0; side < 2; ++side)
+        {
+          const int64_t f = s_first[slot][d][side == 0 ? 0 : 2];
+          if(f < 0) continue;
+          const double *an = side == 0 ? aL : aR, *bn = side == 0 ? bL : bR;
+          const double *un = a.src + f + base;
+          double t0 = 0.0, t1 = 0.0;
+#pragma unroll
+          for(int m = 0; m < NP; ++m)
+          {
+            const double v = un[m * stride];
+            t0 = fma(bn[m], v, t0);
+            t1 = fma(bn[NP + m], v, t1);
+          }
+#pragma unroll
+          for(int i = 0; i < NP; ++i) x[i] = fma(an[i], t0, fma(an[NP + i], t1, x[i]));
+        }
+#pragma unroll
+        for(int i = 0; i < NP; ++i) s_x[slot * ND + base + i * stride] = x[i];
+      }
+      __syncthreads();
+      // masses along the other directions; the last one accumulates into out
+      int done = 0;
+#pragma unroll
+      for(int e = 0; e < DIM; ++e)
+      {
+        if(e == d) continue;
+        ++done;
+        const bool last = done == DIM - 1;
+        if(active)
+        {
+          const int stride = e == 0 ? 1 : e == 1 ? NP : NP * NP;
+          const int base = (p % stride) + (p / stride) * stride * NP;
+          const double *M = s_fac + (slot * DIM + e) * FS;
+          double r[NP];
+#pragma unroll
+          for(int m = 0; m < NP; ++m) r[m] = s_x[slot * ND + base + m * stride];
+#pragma unroll
+          for(int i = 0; i < NP; ++i)
+          {
+            double acc = 0.0;
+#pragma unroll
+            for(int m = 0; m < NP; ++m) acc = fma(M[i * NP + m], r[m], acc);
+            if(last)
+              s_out[slot * ND + base + i * stride] += acc;
+            else
+              s_x[slot * ND + base + i * stride] = acc;
+          }
+        }
+        __syncthreads();
       }
     }
-    __syncthreads();
+    for(int i = tid; i < CPB * ND; i += C::THREADS)
+    {
+      const int s = i / ND;
+      const int64_t cell = c0 + s;
+      if(cell < a.n_cells) a.dst[s_first[s][0][1] + i % ND] = s_out[i];
+    }
   }
 }
 
@@ -350,8 +404,7 @@ void operator_apply(tpss_operator *op, double *dst, const double *src, cudaStrea
   a.cell_start = L.lexicographic ? nullptr : L.d_cell_start.ptr;
   for(int d = 0; d < 3; ++d)
   {
-    a.mass[d] = op->d_mass[d].ptr;
-    a.blk[d] = op->d_blk[d].ptr;
+    a.fac[d] = op->d_fac[d].ptr;
     a.nc[d] = L.nc[d];
   }
   a.n_cells = L.n_cells;
@@ -413,10 +466,8 @@ extern "C" int tpss_operator_create(const tpss_layout *layout, double ip_factor,
     const Shape1D s = make_shape_1d(layout->k);
     for(int d = 0; d < layout->dim; ++d)
     {
-      std::vector<double> mass, blk;
-      operator_blocks_1d(s, layout->nc[d], layout->h[d].data(), ip_factor, mass, blk);
-      op->d_mass[d].upload(mass.data(), mass.size());
-      op->d_blk[d].upload(blk.data(), blk.size());
+      const std::vector<double> fac = operator_factors_1d(s, layout->nc[d], layout->h[d].data(), ip_factor);
+      op->d_fac[d].upload(fac.data(), fac.size());
       op->nblk_cells[d] = layout->nc[d];
     }
     *out = op.release();

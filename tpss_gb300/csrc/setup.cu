@@ -264,3 +264,56 @@ std::vector<double> embedding_1d(const Shape1D &s)
 }
 
 }  // namespace tpss
+
+namespace tpss
+{
+// Per cell of one direction: [M np*np][C np*np][aL 2*np][bL 2*np][aR 2*np][bR 2*np].
+// C is the cell's own block of the global 1-D SIPG matrix; the couplings to the neighbours are
+// rank two (only face values and normal derivatives meet):
+//   block(c, c+1) = aR_0 bR_0^T + aR_1 bR_1^T,  block(c, c-1) = aL_0 bL_0^T + aL_1 bL_1^T
+// (zero at the physical boundary), from the interior-face terms
+// sigma [u][v] - {u'}[v] - [u]{v'} with sigma = ip gamma (1/h_l + 1/h_r)/2.
+std::vector<double> operator_factors_1d(const Shape1D &s, int nc, const double *h, double ip)
+{
+  const int np = s.np, q2 = np * np, stride = 2 * q2 + 8 * np;
+  const double gamma = s.k == 0 ? 1.0 : double(s.k) * (s.k + 1);
+  std::vector<double> mass, blk;
+  operator_blocks_1d(s, nc, h, ip, mass, blk);
+  std::vector<double> out((size_t)nc * stride, 0.0);
+  for(int c = 0; c < nc; ++c)
+  {
+    double *o = &out[(size_t)c * stride];
+    for(int i = 0; i < q2; ++i)
+    {
+      o[i] = mass[(size_t)c * q2 + i];
+      o[q2 + i] = blk[((size_t)c * 3 + 1) * q2 + i];
+    }
+    double *aL = o + 2 * q2, *bL = aL + 2 * np, *aR = bL + 2 * np, *bR = aR + 2 * np;
+    if(c > 0)
+    {
+      const double hl = h[c - 1], hc = h[c];
+      const double sigma = ip * 0.5 * gamma * (1.0 / hl + 1.0 / hc);
+      for(int i = 0; i < np; ++i)
+      {
+        aL[i] = s.fval[0][i];                // test value at the cell's left face
+        aL[np + i] = s.fgrad[0][i] / hc;     // test derivative there
+        bL[i] = -sigma * s.fval[1][i] + 0.5 * s.fgrad[1][i] / hl;  // trial side of cell c-1
+        bL[np + i] = -0.5 * s.fval[1][i];
+      }
+    }
+    if(c + 1 < nc)
+    {
+      const double hc = h[c], hr = h[c + 1];
+      const double sigma = ip * 0.5 * gamma * (1.0 / hc + 1.0 / hr);
+      for(int i = 0; i < np; ++i)
+      {
+        aR[i] = s.fval[1][i];
+        aR[np + i] = s.fgrad[1][i] / hc;
+        bR[i] = -sigma * s.fval[0][i] - 0.5 * s.fgrad[0][i] / hr;
+        bR[np + i] = 0.5 * s.fval[0][i];
+      }
+    }
+  }
+  return out;
+}
+}  // namespace tpss
