@@ -211,6 +211,12 @@ struct FdTables
   std::vector<double> S_host, lam_host;  // n_entries * n*n, n_entries * n (FP64 results)
   double setup_seconds = 0.0;
   DeviceBuffer<float> ras_w;  // P*npc weights (1/multiplicity) when RAS is used
+  // Even/odd split of mirror-symmetric entries (vertex patches with equal cells and equal
+  // boundary flags): per entry [Se^T h x hpad][So^T][Se][So][lambda: even then odd, npad],
+  // Se = S_even / sqrt(2); sym[e] = 1 when entry e has this form.
+  int hpad32 = 0;
+  DeviceBuffer<float> fd32_eo;
+  DeviceBuffer<int32_t> sym;
 };
 
 struct TimerSlot
@@ -278,6 +284,9 @@ struct StreamLaunch
   const double *src;
   double *dst;
   const float *fd32;
+  const float *fd32_eo;
+  const int32_t *sym;
+  int es_eo;
   double omega;
   int ras;
   DeviceBuffer<float> *halo;  // scratch, grown on demand

@@ -28,6 +28,77 @@ const char *kTimerNames[5] = {"[SchwarzPrecond] Update residuals:", "[SchwarzPre
 
 int pad_to(int n, int w) { return (n + w - 1) / w * w; }
 
+// Mirror-symmetric 1-D problems (two equal cells, equal boundary flags) commute with the flip
+// J: i -> n-1-i.  Their generalized eigenproblem splits into an even and an odd half problem
+// in the bases e_j = (delta_j + delta_{n-1-j})/sqrt(2) and o_j = (delta_j - delta_{n-1-j})/sqrt(2),
+// which lets the kernels contract with two h x h matrices (h = n/2) instead of one n x n.
+// The resulting inverse is the same operator; only the rounding differs.
+void build_even_odd(const tpss_layout &L, FdTables &T, const std::vector<double> &Ms,
+                    const std::vector<double> &As)
+{
+  const int n = L.n, nn = n * n;
+  std::vector<int32_t> sym(T.n_entries, 0);
+  if(L.ncp == 2 && n % 2 == 0)
+    for(int e = 0; e < T.n_entries; ++e)
+    {
+      const auto &k = L.fd_keys[e];
+      sym[e] = k.h0 == k.h1 && k.lo == k.hi;
+    }
+  const int h = n / 2;
+  T.hpad32 = pad_to(h, 4);
+  const int npad = T.npad32, hp = T.hpad32;
+  const int es = 4 * h * hp + npad;
+  std::vector<int> ids;
+  for(int e = 0; e < T.n_entries; ++e)
+    if(sym[e]) ids.push_back(e);
+  std::vector<float> tab((size_t)std::max<size_t>(1, (size_t)T.n_entries) * es, 0.f);
+  if(!ids.empty())
+  {
+    const double r2 = 1.0 / std::sqrt(2.0);
+    const int hh = h * h;
+    std::vector<double> Mh(2 * ids.size() * hh), Ah(2 * ids.size() * hh);
+    for(size_t u = 0; u < ids.size(); ++u)
+    {
+      const double *M = &Ms[(size_t)ids[u] * nn], *A = &As[(size_t)ids[u] * nn];
+      for(int par = 0; par < 2; ++par)  // 0: even, 1: odd
+      {
+        const double sg = par == 0 ? 1.0 : -1.0;
+        double *Mo = &Mh[(2 * u + par) * hh], *Ao = &Ah[(2 * u + par) * hh];
+        for(int a = 0; a < h; ++a)
+          for(int b = 0; b < h; ++b)
+          {
+            // x_a^T X x_b with x_a = (delta_a + sg delta_{n-1-a})/sqrt(2)
+            auto proj = [&](const double *X) {
+              const int a2 = n - 1 - a, b2 = n - 1 - b;
+              return 0.5 * (X[a * n + b] + sg * X[a * n + b2] + sg * X[a2 * n + b] + X[a2 * n + b2]);
+            };
+            Mo[a * h + b] = proj(M);
+            Ao[a * h + b] = proj(A);
+          }
+      }
+    }
+    std::vector<double> Sh, lamh;
+    gen_eig_batched(h, (int)(2 * ids.size()), Mh, Ah, Sh, lamh);
+    for(size_t u = 0; u < ids.size(); ++u)
+    {
+      float *E = &tab[(size_t)ids[u] * es];
+      for(int par = 0; par < 2; ++par)
+      {
+        const double *S = &Sh[(2 * u + par) * hh];
+        for(int i = 0; i < h; ++i)
+          for(int k = 0; k < h; ++k)
+          {
+            E[(par * h + k) * hp + i] = float(S[i * h + k] * r2);          // Se^T / So^T rows
+            E[(2 * h + par * h + i) * hp + k] = float(S[i * h + k] * r2);  // Se / So rows
+          }
+        for(int k = 0; k < h; ++k) E[4 * h * hp + par * h + k] = float(lamh[(2 * u + par) * h + k]);
+      }
+    }
+  }
+  T.fd32_eo.upload(tab.data(), tab.size());
+  T.sym.upload(sym.data(), sym.size());
+}
+
 std::shared_ptr<FdTables> build_tables(const tpss_layout &L, double ip, bool ras)
 {
   auto t0 = std::chrono::steady_clock::now();
@@ -72,6 +143,7 @@ std::shared_ptr<FdTables> build_tables(const tpss_layout &L, double ip, bool ras
   fill((float *)nullptr, T->npad32, t32);
   T->fd64.upload(t64.data(), t64.size());
   T->fd32.upload(t32.data(), t32.size());
+  build_even_odd(L, *T, Ms, As);
   if(ras)
   {
     // RAS weights: 1 / (number of patches sharing the cell), the gathered "appearances" of
@@ -273,6 +345,9 @@ void precond_vmult(tpss_precond *p, double *dst, const double *src, cudaStream_t
       l.src = src;
       l.dst = dst;
       l.fd32 = p->tables->fd32.ptr;
+      l.fd32_eo = p->tables->fd32_eo.ptr;
+      l.sym = p->tables->sym.ptr;
+      l.es_eo = 4 * (L.n / 2) * p->tables->hpad32 + p->tables->npad32;
       l.omega = p->desc.relaxation;
       l.ras = p->desc.use_ras_weights != 0;
       l.halo = &p->halo;

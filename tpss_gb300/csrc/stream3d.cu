@@ -17,6 +17,9 @@ bool launch_stream(const tpss_layout &L, const StreamLaunch &l, cudaStream_t s)
   a.dst = l.dst;
   a.cell_start = L.lexicographic ? nullptr : L.d_cell_start.ptr;
   a.fd = l.fd32;
+  a.fd_eo = l.fd32_eo;
+  a.sym = l.sym;
+  a.es_eo = l.es_eo;
   for(int d = 0; d < 3; ++d)
   {
     a.vfd[d] = L.d_vertex_fd[d].ptr;

@@ -48,6 +48,13 @@ struct SCfg
   static constexpr int LAYER = LCELLS * CD;
   static constexpr int ES = Entry<float, N>::size;
   static constexpr int NPAD = Entry<float, N>::NPAD;
+  // even/odd entries of mirror-symmetric 1-D problems: [Se^T][So^T][Se][So] (h x hpad) + lambda
+  static constexpr int H = N / 2;
+  static constexpr int HPAD = ((H + 3) / 4) * 4;
+  static constexpr int EO_SOT = H * HPAD, EO_SE = 2 * H * HPAD, EO_SO = 3 * H * HPAD;
+  static constexpr int EO_LAM = 4 * H * HPAD;
+  static constexpr int ES_EO = EO_LAM + NPAD;
+  static constexpr int ESLOT = ((ES > ES_EO ? ES : ES_EO) + 3) / 4 * 4;  // shared slot size
   // padded patch layout (x + SX y + SXY z): chosen so that the pencils of a warp fall into
   // distinct shared-memory banks in all three directions (at most 2-way conflicts)
   static constexpr int SX = N == 10 ? 13 : N == 8 ? 9 : N == 6 ? 6 : N == 4 ? 5 : N;
@@ -58,7 +65,8 @@ struct SCfg
   static_assert(G >= 1, "need at least one thread per cell DoF");
   // shared memory carve-up (in floats; the staged FP64 cell layers take two floats per value)
   static constexpr int OFF_FD = 0;                                   // (BX + BY + BZ) entries
-  static constexpr int OFF_RAW = ((OFF_FD + (BX + BY + BZ) * ES + 3) / 4) * 4;  // 3 FP64 layers
+  static constexpr int OFF_SYM = OFF_FD + (BX + BY + BZ) * ESLOT;          // int flags
+  static constexpr int OFF_RAW = ((OFF_SYM + (BX + BY + BZ) + 3) / 4) * 4;  // 3 FP64 layers
   static constexpr int OFF_ACC = OFF_RAW + 3 * 2 * LAYER;            // 2 FP32 layers
   static constexpr int OFF_WORK = OFF_ACC + 2 * LAYER;               // NPATCH patches
   static constexpr int FLOATS = OFF_WORK + NPATCH * PSTRIDE;
@@ -72,6 +80,9 @@ struct StreamArgs
   float *__restrict__ halo;
   const int64_t *__restrict__ cell_start;  // nullptr: lexicographic cells
   const float *__restrict__ fd;            // FP32 FD table
+  const float *__restrict__ fd_eo;         // even/odd table (valid where sym[e])
+  const int32_t *__restrict__ sym;         // entry is mirror-symmetric
+  int es_eo;                               // elements per even/odd entry
   const int32_t *__restrict__ vfd[3];      // FD entry of vertex v per direction
   int nc[3];                               // cells per direction
   int T[3];                                // items per direction
@@ -149,9 +160,126 @@ __device__ __forceinline__ void mpass(float *__restrict__ data, const float *__r
   }
 }
 
+// Even/odd passes of mirror-symmetric directions (n = 2h): forward t_e = Se^T (r_i + r_{n-1-i}),
+// t_o = So^T (r_i - r_{n-1-i}) stored at transformed positions [0,h) and [h,n); backward
+// u_i = Se t_e + So t_o, u_{n-1-i} = Se t_e - So t_o.  Half the FMAs of a full n x n pass.
+template<int H, int HPAD, int NPT>
+__device__ __forceinline__ void eo_forward(float (&r)[NPT][2 * H], const float *__restrict__ eo,
+                                           float (&t)[NPT][2 * H])
+{
+#pragma unroll
+  for(int j = 0; j < NPT; ++j)
+#pragma unroll
+    for(int i = 0; i < H; ++i)
+    {
+      const float a = r[j][i], b = r[j][2 * H - 1 - i];
+      r[j][i] = a + b;
+      r[j][2 * H - 1 - i] = a - b;  // odd part stored mirrored
+    }
+#pragma unroll
+  for(int par = 0; par < 2; ++par)
+#pragma unroll
+    for(int k = 0; k < H; ++k)
+    {
+      const float4 *row = reinterpret_cast<const float4 *>(eo + (par * H + k) * HPAD);
+      float acc[NPT];
+#pragma unroll
+      for(int j = 0; j < NPT; ++j) acc[j] = 0.f;
+#pragma unroll
+      for(int m4 = 0; m4 < HPAD / 4; ++m4)
+      {
+        const float4 v = row[m4];
+        const float vv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+        for(int w = 0; w < 4; ++w)
+          if(m4 * 4 + w < H)
+          {
+            constexpr int dummy = 0;
+            (void)dummy;
+            const int i = m4 * 4 + w < H ? m4 * 4 + w : 0;
+#pragma unroll
+            for(int j = 0; j < NPT; ++j)
+              acc[j] = fmaf(vv[w], par == 0 ? r[j][i] : r[j][2 * H - 1 - i], acc[j]);
+          }
+      }
+#pragma unroll
+      for(int j = 0; j < NPT; ++j) t[j][par * H + k] = acc[j];
+    }
+}
+
+template<int H, int HPAD, int NPT>
+__device__ __forceinline__ void eo_backward(const float (&t)[NPT][2 * H], const float *__restrict__ eo,
+                                            float (&u)[NPT][2 * H])
+{
+#pragma unroll
+  for(int i = 0; i < H; ++i)
+  {
+    const float4 *re = reinterpret_cast<const float4 *>(eo + (2 * H + i) * HPAD);
+    const float4 *ro = reinterpret_cast<const float4 *>(eo + (3 * H + i) * HPAD);
+    float E[NPT], O[NPT];
+#pragma unroll
+    for(int j = 0; j < NPT; ++j) E[j] = O[j] = 0.f;
+#pragma unroll
+    for(int m4 = 0; m4 < HPAD / 4; ++m4)
+    {
+      const float4 ve = re[m4], vo = ro[m4];
+      const float ee[4] = {ve.x, ve.y, ve.z, ve.w}, oo[4] = {vo.x, vo.y, vo.z, vo.w};
+#pragma unroll
+      for(int w = 0; w < 4; ++w)
+        if(m4 * 4 + w < H)
+        {
+          const int k = m4 * 4 + w < H ? m4 * 4 + w : 0;
+#pragma unroll
+          for(int j = 0; j < NPT; ++j)
+          {
+            E[j] = fmaf(ee[w], t[j][k], E[j]);
+            O[j] = fmaf(oo[w], t[j][H + k], O[j]);
+          }
+        }
+    }
+#pragma unroll
+    for(int j = 0; j < NPT; ++j)
+    {
+      u[j][i] = E[j] + O[j];
+      u[j][2 * H - 1 - i] = E[j] - O[j];
+    }
+  }
+}
+
+// full or even/odd pass along DIR (in place in the padded patch layout)
+template<bool SYM, bool FWD, int N, int SX, int SXY, int NPAD, int HPAD, int DIR, int NPT, int TPP>
+__device__ __forceinline__ void spass(float *__restrict__ data, const float *__restrict__ ent, int q,
+                                      float scale)
+{
+  if constexpr(!SYM)
+    mpass<N, SX, SXY, NPAD, DIR, NPT, TPP>(data, ent + (FWD ? Entry<float, N>::ST : Entry<float, N>::S), q, scale);
+  else
+  {
+    constexpr int H = N / 2;
+    constexpr int stride = DIR == 0 ? 1 : DIR == 1 ? SX : SXY;
+    float r[NPT][N], o[NPT][N];
+    int base[NPT];
+#pragma unroll
+    for(int j = 0; j < NPT; ++j)
+    {
+      base[j] = pbase<N, SX, SXY, DIR>(q + j * TPP);
+#pragma unroll
+      for(int m = 0; m < N; ++m) r[j][m] = data[base[j] + m * stride];
+    }
+    if constexpr(FWD)
+      eo_forward<H, HPAD, NPT>(r, ent, o);
+    else
+      eo_backward<H, HPAD, NPT>(r, ent, o);
+#pragma unroll
+    for(int j = 0; j < NPT; ++j)
+#pragma unroll
+      for(int i = 0; i < N; ++i) data[base[j] + i * stride] = o[j][i] * scale;
+  }
+}
+
 // direction 0, forward, reading the patch straight from the two staged FP64 cell layers:
 // pencil (y, z) of patch (px, py) covers cells (px, px+1) of row (py + y/K1) in layer z/K1
-template<int K1, int N, int SX, int SXY, int NPAD, int NPT, int TPP, int CX, int CD>
+template<bool SYM, int K1, int N, int SX, int SXY, int NPAD, int HPAD, int NPT, int TPP, int CX, int CD>
 __device__ __forceinline__ void mpass_x_from_layers(float *__restrict__ data, const double *__restrict__ lo,
                                                     const double *__restrict__ hi,
                                                     const float *__restrict__ St, int px, int py, int q)
@@ -167,6 +295,16 @@ __device__ __forceinline__ void mpass_x_from_layers(float *__restrict__ data, co
     const int row = (px + CX * (py + y / K1)) * CD + K1 * (y % K1) + K1 * K1 * (z % K1);
 #pragma unroll
     for(int m = 0; m < N; ++m) r[j][m] = float(layer[row + (m / K1) * CD + (m % K1)]);
+  }
+  if constexpr(SYM)
+  {
+    float t[NPT][N];
+    eo_forward<N / 2, HPAD, NPT>(r, St, t);
+#pragma unroll
+    for(int j = 0; j < NPT; ++j)
+#pragma unroll
+      for(int i = 0; i < N; ++i) data[base[j] + i] = t[j][i];
+    return;
   }
 #pragma unroll
   for(int i = 0; i < N; ++i)
@@ -193,10 +331,10 @@ __device__ __forceinline__ void mpass_x_from_layers(float *__restrict__ data, co
 
 // direction 2, forward: S^T along z, then division by the eigenvalue sums
 // lambda_x[i0] + lambda_y[i1] + lambda_z[i2]
-template<int N, int SX, int SXY, int NPAD, int NPT, int TPP>
-__device__ __forceinline__ void mpass_divide(float *__restrict__ data, const float *__restrict__ ex,
-                                             const float *__restrict__ ey, const float *__restrict__ ez,
-                                             int q)
+template<bool SYM, int N, int SX, int SXY, int NPAD, int HPAD, int NPT, int TPP>
+__device__ __forceinline__ void mpass_divide(float *__restrict__ data, const float *__restrict__ lamx,
+                                             const float *__restrict__ lamy, const float *__restrict__ ez,
+                                             const float *__restrict__ lamz, int q)
 {
   constexpr int stride = SXY;
   float r[NPT][N];
@@ -207,9 +345,22 @@ __device__ __forceinline__ void mpass_divide(float *__restrict__ data, const flo
   {
     const int p = q + j * TPP;  // pencil along z: i0 + N i1
     base[j] = pbase<N, SX, SXY, 2>(p);
-    lxy[j] = ex[Entry<float, N>::LAM + p % N] + ey[Entry<float, N>::LAM + p / N];
+    lxy[j] = lamx[p % N] + lamy[p / N];
 #pragma unroll
     for(int m = 0; m < N; ++m) r[j][m] = data[base[j] + m * stride];
+  }
+  if constexpr(SYM)
+  {
+    float t[NPT][N];
+    eo_forward<N / 2, HPAD, NPT>(r, ez, t);
+#pragma unroll
+    for(int i = 0; i < N; ++i)
+    {
+      const float lz = lamz[i];
+#pragma unroll
+      for(int j = 0; j < NPT; ++j) data[base[j] + i * stride] = __fdividef(t[j][i], lxy[j] + lz);
+    }
+    return;
   }
 #pragma unroll
   for(int i = 0; i < N; ++i)
@@ -229,7 +380,7 @@ __device__ __forceinline__ void mpass_divide(float *__restrict__ data, const flo
 #pragma unroll
           for(int j = 0; j < NPT; ++j) acc[j] = fmaf(vv[w], r[j][m4 * 4 + w < N ? m4 * 4 + w : 0], acc[j]);
     }
-    const float lz = ez[Entry<float, N>::LAM + i];
+    const float lz = lamz[i];
 #pragma unroll
     for(int j = 0; j < NPT; ++j) data[base[j] + i * stride] = __fdividef(acc[j], lxy[j] + lz);
   }
@@ -303,6 +454,7 @@ __global__ void __launch_bounds__(C::THREADS, 1) stream_kernel(StreamArgs a)
   constexpr int SX = C::SX, SXY = C::SXY, PS = C::PSTRIDE;
   extern __shared__ __align__(16) float sm[];
   float *s_fd = sm + C::OFF_FD;
+  int *s_sym = reinterpret_cast<int *>(sm + C::OFF_SYM);
   double *s_raw = reinterpret_cast<double *>(sm + C::OFF_RAW);
   float *s_acc = sm + C::OFF_ACC;
   float *s_work = sm + C::OFF_WORK;
@@ -322,14 +474,22 @@ __global__ void __launch_bounds__(C::THREADS, 1) stream_kernel(StreamArgs a)
     const int bz = min(BZ, a.nc[2] - 1 - BZ * tz);
     const int x0 = BX * tx, y0 = BY * ty, z0 = BZ * tz;  // first cell of the item
     __syncthreads();  // the previous item is done with shared memory
-    for(int i = tid; i < (BX + BY + BZ) * ES; i += C::THREADS)
+    // 1-D eigenbases of the item's x, y and z vertices: full entry or even/odd split
+    for(int i = tid; i < (BX + BY + BZ) * C::ESLOT; i += C::THREADS)
     {
-      const int sl = i / ES, o = i % ES;
+      const int sl = i / C::ESLOT, o = i % C::ESLOT;
       int en = -1;
       if(sl < BX) { if(sl < bx) en = a.vfd[0][x0 + 1 + sl]; }
       else if(sl < BX + BY) { if(sl - BX < by) en = a.vfd[1][y0 + 1 + (sl - BX)]; }
       else if(sl - BX - BY < bz) en = a.vfd[2][z0 + 1 + (sl - BX - BY)];
-      s_fd[i] = en >= 0 ? a.fd[(size_t)en * ES + o] : 0.f;
+      float v = 0.f;
+      if(en >= 0)
+      {
+        if(a.sym[en]) { if(o < C::ES_EO) v = a.fd_eo[(size_t)en * a.es_eo + o]; }
+        else if(o < ES) v = a.fd[(size_t)en * ES + o];
+      }
+      s_fd[i] = v;
+      if(o == 0) s_sym[sl] = en >= 0 ? a.sym[en] : 0;
     }
     copy_layer_async<C>(a, x0, y0, bx, by, z0, s_raw, e, g);
     copy_layer_async<C>(a, x0, y0, bx, by, z0 + 1, s_raw + C::LAYER, e, g);
@@ -345,20 +505,49 @@ __global__ void __launch_bounds__(C::THREADS, 1) stream_kernel(StreamArgs a)
       const double *lo = s_raw + (j % 3) * C::LAYER, *hi = s_raw + ((j + 1) % 3) * C::LAYER;
       const bool active = px < bx && py < by;
       float *my = s_work + slot * PS;
-      const float *ex = s_fd + px * ES, *ey = s_fd + (BX + py) * ES, *ez = s_fd + (BX + BY + j) * ES;
+      constexpr int ESL = C::ESLOT, HP = C::HPAD;
+      const float *ex = s_fd + px * ESL, *ey = s_fd + (BX + py) * ESL, *ez = s_fd + (BX + BY + j) * ESL;
+      const bool sx = s_sym[px], sy = s_sym[BX + py], sz = s_sym[BX + BY + j];
+      const float *lamx = ex + (sx ? C::EO_LAM : Entry<float, N>::LAM);
+      const float *lamy = ey + (sy ? C::EO_LAM : Entry<float, N>::LAM);
+      const float *lamz = ez + (sz ? C::EO_LAM : Entry<float, N>::LAM);
       if(active)
-        mpass_x_from_layers<K1, N, SX, SXY, NPAD, NPT, TPP, C::CX, CD>(my, lo, hi, ex + Entry<float, N>::ST,
-                                                                      px, py, q);
+      {
+        if(sx)
+          mpass_x_from_layers<true, K1, N, SX, SXY, NPAD, HP, NPT, TPP, C::CX, CD>(my, lo, hi, ex, px, py, q);
+        else
+          mpass_x_from_layers<false, K1, N, SX, SXY, NPAD, HP, NPT, TPP, C::CX, CD>(my, lo, hi, ex, px, py, q);
+      }
       __syncthreads();
-      if(active) mpass<N, SX, SXY, NPAD, 1, NPT, TPP>(my, ey + Entry<float, N>::ST, q, 1.f);
+      if(active)
+      {
+        if(sy) spass<true, true, N, SX, SXY, NPAD, HP, 1, NPT, TPP>(my, ey, q, 1.f);
+        else spass<false, true, N, SX, SXY, NPAD, HP, 1, NPT, TPP>(my, ey, q, 1.f);
+      }
       __syncthreads();
-      if(active) mpass_divide<N, SX, SXY, NPAD, NPT, TPP>(my, ex, ey, ez, q);
+      if(active)
+      {
+        if(sz) mpass_divide<true, N, SX, SXY, NPAD, HP, NPT, TPP>(my, lamx, lamy, ez, lamz, q);
+        else mpass_divide<false, N, SX, SXY, NPAD, HP, NPT, TPP>(my, lamx, lamy, ez, lamz, q);
+      }
       __syncthreads();
-      if(active) mpass<N, SX, SXY, NPAD, 2, NPT, TPP>(my, ez + Entry<float, N>::S, q, 1.f);
+      if(active)
+      {
+        if(sz) spass<true, false, N, SX, SXY, NPAD, HP, 2, NPT, TPP>(my, ez, q, 1.f);
+        else spass<false, false, N, SX, SXY, NPAD, HP, 2, NPT, TPP>(my, ez, q, 1.f);
+      }
       __syncthreads();
-      if(active) mpass<N, SX, SXY, NPAD, 1, NPT, TPP>(my, ey + Entry<float, N>::S, q, 1.f);
+      if(active)
+      {
+        if(sy) spass<true, false, N, SX, SXY, NPAD, HP, 1, NPT, TPP>(my, ey, q, 1.f);
+        else spass<false, false, N, SX, SXY, NPAD, HP, 1, NPT, TPP>(my, ey, q, 1.f);
+      }
       __syncthreads();
-      if(active) mpass<N, SX, SXY, NPAD, 0, NPT, TPP>(my, ex + Entry<float, N>::S, q, a.omega);
+      if(active)
+      {
+        if(sx) spass<true, false, N, SX, SXY, NPAD, HP, 0, NPT, TPP>(my, ex, q, a.omega);
+        else spass<false, false, N, SX, SXY, NPAD, HP, 0, NPT, TPP>(my, ex, q, a.omega);
+      }
       __syncthreads();
       // accumulate per cell: the (up to) 4 patches of this layer touching the cell, fixed order
       float *alo = s_acc + (j % 2) * C::LAYER, *ahi = s_acc + ((j + 1) % 2) * C::LAYER;
