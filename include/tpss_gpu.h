@@ -77,6 +77,13 @@ typedef struct tpss_layout_desc
                                      NULL = cell index * (k+1)^dim */
   const int32_t *patch_color;     /* host: optional user coloring, one entry per patch in the
                                      default patch order (tpss_layout_patches); NULL = default */
+  const double *vertex_coords;    /* host, optional: coordinates of the (n_cells[d]+1) vertices per
+                                     direction (lexicographic, x fastest, dim values each) of a
+                                     distorted mesh with trilinear cells.  Vertex patches then use
+                                     surrogate Cartesian widths: the average arc length between
+                                     opposite faces (MappingInfo, TPSS/mapping_info.templates.h:42-240,
+                                     use_arc_length = true, no volume normalization) */
+  int surrogate_n_q;              /* Gauss-Lobatto points per direction for the arc lengths; 0 = 5 */
 } tpss_layout_desc;
 
 /* Replaces SubdomainHandler<dim,Number>::reinit (TPSS/subdomain_handler.h:33-225). */

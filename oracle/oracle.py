@@ -280,3 +280,67 @@ def num_threads():
 
 def set_num_threads(n):
     lib().or_set_num_threads(int(n))
+
+
+def _lib_ext():
+    L = lib()
+    if not getattr(L, "_ext_ready", False):
+        L.or_ksvd.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, _dp, C.c_int, _dp, _dp]
+        L.or_ksvd_diag.argtypes = [C.c_int, C.c_int, _dp, C.c_int, _dp, _dp]
+        L.or_surrogate_h.argtypes = [C.c_int, _ip, _dp, C.c_int, _dp]
+        L.or_schwarz_vmult_surrogate.argtypes = [C.c_int, C.c_int, _ip, _dp, C.c_double, C.c_double,
+                                                 _dp, _dp]
+        L._ext_ready = True
+    return L
+
+
+def ksvd(M, big_shape, small_shape, rank):
+    """Best Kronecker rank-r approximation M ~ sum_r B_r (x) A_r (compute_ksvd)."""
+    M = _c64(M)
+    bm, bn = big_shape
+    sm, sn = small_shape
+    B = np.zeros((rank, bm, bn))
+    A = np.zeros((rank, sm, sn))
+    assert _lib_ext().or_ksvd(bm, bn, sm, sn, _d(M), rank, _d(B), _d(A)) == 0
+    return B, A
+
+
+def ksvd_diag(d, big, small, rank):
+    """Diagonal variant: diagonals of B_r (big) and A_r (small)."""
+    d = _c64(d)
+    B = np.zeros((rank, big))
+    A = np.zeros((rank, small))
+    assert _lib_ext().or_ksvd_diag(big, small, _d(d), rank, _d(B), _d(A)) == 0
+    return B, A
+
+
+def distorted_coords(dim, nc, seed, amplitude=0.25):
+    """Vertex coordinates of the unit cube with nc cells per direction, every interior vertex
+    displaced by U[-amplitude h, amplitude h] per coordinate (numpy Philox, seed)."""
+    nv = [n + 1 for n in nc]
+    grids = np.meshgrid(*[np.arange(n) / (n - 1) for n in reversed(nv)], indexing="ij")
+    X = np.stack([grids[dim - 1 - d] for d in range(dim)], axis=-1).reshape(-1, dim)
+    g = np.random.Generator(np.random.Philox(seed))
+    disp = g.uniform(-amplitude, amplitude, X.shape) / np.array(nc)[None, :]
+    idx = np.indices(list(reversed(nv))).reshape(dim, -1)[::-1].T  # (x, y[, z]) per vertex
+    interior = np.all((idx > 0) & (idx < np.array(nc)[None, :]), axis=1)
+    X[interior] += disp[interior]
+    return np.ascontiguousarray(X)
+
+
+def surrogate_h(dim, nc, coords, nq=5):
+    """Per vertex patch, direction and 1-D cell: surrogate width [P, dim, 2]."""
+    nc3 = _nc3(dim, nc)
+    lower, _, _ = patches(dim, nc, 1, 0)
+    out = np.zeros((len(lower), dim, 2))
+    assert _lib_ext().or_surrogate_h(dim, nc3.ctypes.data_as(_ip), _d(_c64(coords)), nq, _d(out)) == 0
+    return out
+
+
+def schwarz_vmult_surrogate(dim, k, nc, hp, src, omega=1.0, ip=1.0):
+    nc3 = _nc3(dim, nc)
+    src = _c64(src)
+    dst = np.zeros_like(src)
+    assert _lib_ext().or_schwarz_vmult_surrogate(dim, k, nc3.ctypes.data_as(_ip), _d(_c64(hp)), float(ip),
+                                                 float(omega), _d(src), _d(dst)) == 0
+    return dst

@@ -1345,3 +1345,290 @@ int or_mg_cg_solve(int dim, int k, int n_rep, int nc_fine, double ip, int patch_
   free(G.E);
   return converged ? it : -1;
 }
+
+/* ===================================================================================== */
+/*                       Kronecker SVD (low Kronecker-rank approximation)                */
+/* ===================================================================================== */
+
+/* One-sided Jacobi SVD (Hestenes) of the m x n row-major matrix A: on return A holds U*S
+ * (column j = sigma_j u_j), V (n x n) the right singular vectors, s the singular values,
+ * all sorted by descending sigma. */
+static void svd_onesided(int m, int n, double *A, double *V, double *s)
+{
+  for(int i = 0; i < n * n; ++i) V[i] = 0.0;
+  for(int i = 0; i < n; ++i) V[i * n + i] = 1.0;
+  for(int sweep = 0; sweep < 100; ++sweep)
+  {
+    int rotated = 0;
+    for(int p = 0; p < n - 1; ++p)
+      for(int q = p + 1; q < n; ++q)
+      {
+        double al = 0.0, be = 0.0, ga = 0.0;
+        for(int i = 0; i < m; ++i)
+        {
+          al += A[i * n + p] * A[i * n + p];
+          be += A[i * n + q] * A[i * n + q];
+          ga += A[i * n + p] * A[i * n + q];
+        }
+        if(fabs(ga) <= 1e-15 * sqrt(al * be) || ga == 0.0) continue;
+        rotated = 1;
+        const double zeta = (be - al) / (2.0 * ga);
+        const double t = (zeta >= 0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+        const double c = 1.0 / sqrt(1.0 + t * t), sn = c * t;
+        for(int i = 0; i < m; ++i)
+        {
+          const double ap = A[i * n + p], aq = A[i * n + q];
+          A[i * n + p] = c * ap - sn * aq;
+          A[i * n + q] = sn * ap + c * aq;
+        }
+        for(int i = 0; i < n; ++i)
+        {
+          const double vp = V[i * n + p], vq = V[i * n + q];
+          V[i * n + p] = c * vp - sn * vq;
+          V[i * n + q] = sn * vp + c * vq;
+        }
+      }
+    if(!rotated) break;
+  }
+  for(int j = 0; j < n; ++j)
+  {
+    double nn = 0.0;
+    for(int i = 0; i < m; ++i) nn += A[i * n + j] * A[i * n + j];
+    s[j] = sqrt(nn);
+  }
+  /* sort descending (selection on columns) */
+  for(int a = 0; a < n; ++a)
+  {
+    int b = a;
+    for(int j = a + 1; j < n; ++j)
+      if(s[j] > s[b]) b = j;
+    if(b == a) continue;
+    double t = s[a]; s[a] = s[b]; s[b] = t;
+    for(int i = 0; i < m; ++i) { t = A[i * n + a]; A[i * n + a] = A[i * n + b]; A[i * n + b] = t; }
+    for(int i = 0; i < n; ++i) { t = V[i * n + a]; V[i * n + a] = V[i * n + b]; V[i * n + b] = t; }
+  }
+}
+
+/* Best Kronecker rank-r approximation M ~ sum_r B_r (x) A_r (TPSS/kroneckersvd.h:207-296,
+ * compute_ksvd; "big" B_r is bm x bn, "small" A_r is sm x sn, M = (bm sm) x (bn sn)).  As in the
+ * reference, the rearranged matrix R[(k,l),(i,j)] = M[k sm + i][l sn + j] (Van Loan & Pitsianis)
+ * is decomposed by an SVD and sigma_r is split as sqrt(sigma_r) on both factors; here the SVD is
+ * a one-sided Jacobi SVD instead of the reference's Lanczos bidiagonalization.  Signs: the first
+ * nonzero entry of each A_r is made positive.  B: rank * bm*bn, A: rank * sm*sn. */
+int or_ksvd(int bm, int bn, int sm, int sn, const double *M, int rank, double *B, double *A)
+{
+  const int rows = bm * bn, cols = sm * sn;
+  if(rank < 1 || rank > (rows < cols ? rows : cols)) return -1;
+  double *R = (double *)malloc(sizeof(double) * rows * cols);
+  double *V = (double *)malloc(sizeof(double) * cols * cols);
+  double *s = (double *)malloc(sizeof(double) * cols);
+  const int ld = bn * sn;
+  for(int k = 0; k < bm; ++k)
+    for(int l = 0; l < bn; ++l)
+      for(int i = 0; i < sm; ++i)
+        for(int j = 0; j < sn; ++j)
+          R[(k * bn + l) * cols + i * sn + j] = M[(k * sm + i) * ld + l * sn + j];
+  svd_onesided(rows, cols, R, V, s);
+  for(int r = 0; r < rank; ++r)
+  {
+    const double rs = sqrt(s[r]);
+    double sign = 1.0;
+    for(int j = 0; j < cols; ++j)
+      if(fabs(V[j * cols + r]) > 1e-14) { sign = V[j * cols + r] > 0 ? 1.0 : -1.0; break; }
+    for(int j = 0; j < cols; ++j) A[r * cols + j] = sign * V[j * cols + r] * rs;
+    for(int i = 0; i < rows; ++i) B[r * rows + i] = s[r] > 0 ? sign * R[i * cols + r] / s[r] * rs : 0.0;
+  }
+  free(R);
+  free(V);
+  free(s);
+  return 0;
+}
+
+/* Diagonal variant (TPSS/kroneckersvd.h:412-490): M = diag(d), d of length bm*sm; the
+ * factors are diagonal, B_r = diag(u_r sqrt(sigma_r)), A_r = diag(v_r sqrt(sigma_r)).
+ * Outputs the diagonals: B: rank * bm, A: rank * sm. */
+int or_ksvd_diag(int bm, int sm, const double *d, int rank, double *B, double *A)
+{
+  if(rank < 1 || rank > (bm < sm ? bm : sm)) return -1;
+  double *R = (double *)malloc(sizeof(double) * bm * sm);
+  double *V = (double *)malloc(sizeof(double) * sm * sm);
+  double *s = (double *)malloc(sizeof(double) * sm);
+  memcpy(R, d, sizeof(double) * bm * sm);
+  svd_onesided(bm, sm, R, V, s);
+  for(int r = 0; r < rank; ++r)
+  {
+    const double rs = sqrt(s[r]);
+    double sign = 1.0;
+    for(int j = 0; j < sm; ++j)
+      if(fabs(V[j * sm + r]) > 1e-14) { sign = V[j * sm + r] > 0 ? 1.0 : -1.0; break; }
+    for(int j = 0; j < sm; ++j) A[r * sm + j] = sign * V[j * sm + r] * rs;
+    for(int i = 0; i < bm; ++i) B[r * bm + i] = s[r] > 0 ? sign * R[i * sm + r] / s[r] * rs : 0.0;
+  }
+  free(R);
+  free(V);
+  free(s);
+  return 0;
+}
+
+/* ===================================================================================== */
+/*                         surrogate patches on distorted meshes                         */
+/* ===================================================================================== */
+
+/* Trilinear (bilinear) map of a cell with vertex coordinates X[2^dim][dim] (lexicographic
+ * vertex order), evaluated at reference point xi. */
+static void cell_map(int dim, const double *X, const double *xi, double *x)
+{
+  for(int c = 0; c < dim; ++c) x[c] = 0.0;
+  for(int v = 0; v < (1 << dim); ++v)
+  {
+    double w = 1.0;
+    for(int d = 0; d < dim; ++d) w *= ((v >> d) & 1) ? xi[d] : 1.0 - xi[d];
+    for(int c = 0; c < dim; ++c) x[c] += w * X[v * dim + c];
+  }
+}
+
+/* Average arc lengths between opposite faces of one cell (MappingInfo::compute_average_scaling,
+ * TPSS/mapping_info.templates.h:42-240, use_arc_length = true): nq Gauss-Lobatto points per
+ * direction; h_d = sum over face points of weight * length of the polyline through the nq
+ * points of the fibre in direction d. */
+static void cell_arc_lengths(int dim, const double *X, int nq, double *h)
+{
+  double z[32], wq[32];
+  or_gauss_lobatto(nq, z);
+  /* Gauss-Lobatto weights on [0,1]: w_i = 1/(n(n-1) P_{n-1}(x_i)^2) on [-1,1], halved */
+  for(int i = 0; i < nq; ++i)
+  {
+    double p, dp;
+    legendre_p(nq - 1, 2.0 * z[i] - 1.0, &p, &dp);
+    if(i == 0 || i == nq - 1) p = (i == 0 && ((nq - 1) % 2)) ? -1.0 : 1.0;
+    wq[i] = 1.0 / (nq * (nq - 1.0) * p * p);
+  }
+  for(int d = 0; d < dim; ++d)
+  {
+    double acc = 0.0;
+    const int nf = dim == 2 ? nq : nq * nq;
+    for(int f = 0; f < nf; ++f)
+    {
+      int fi[2] = {f % nq, f / nq};
+      double wf = 1.0;
+      for(int t = 0; t < dim - 1; ++t) wf *= wq[fi[t]];
+      double len = 0.0, prev[3] = {0, 0, 0};
+      for(int i = 0; i < nq; ++i)
+      {
+        double xi[3] = {0, 0, 0}, x[3];
+        int t = 0;
+        for(int e = 0; e < dim; ++e) xi[e] = e == d ? z[i] : z[fi[t++]];
+        cell_map(dim, X, xi, x);
+        if(i > 0)
+        {
+          double dd = 0.0;
+          for(int c = 0; c < dim; ++c) dd += (x[c] - prev[c]) * (x[c] - prev[c]);
+          len += sqrt(dd);
+        }
+        for(int c = 0; c < dim; ++c) prev[c] = x[c];
+      }
+      acc += wf * len;
+    }
+    h[d] = acc;
+  }
+}
+
+/* Surrogate 1-D cell widths of every vertex patch of a structured mesh with distorted
+ * vertex coordinates coords[(nx+1)(ny+1)(nz+1)][dim] (lexicographic vertices): for patch p and
+ * direction d, out[(p*dim + d)*2 + c] = mean over the 2^(dim-1) patch cells with 1-D index c
+ * of their arc length in direction d.  Patches in the oracle's order (or_patches). */
+int or_surrogate_h(int dim, const int *nc_in, const double *coords, int nq, double *out)
+{
+  int nc[3] = {1, 1, 1};
+  for(int d = 0; d < dim; ++d) nc[d] = nc_in[d];
+  int ncol;
+  int64_t P = or_patches(dim, nc, 1, 0, NULL, NULL, &ncol);
+  int32_t *lower = (int32_t *)malloc(sizeof(int32_t) * 3 * (P ? P : 1));
+  int32_t *color = (int32_t *)malloc(sizeof(int32_t) * (P ? P : 1));
+  or_patches(dim, nc, 1, 0, lower, color, &ncol);
+  const int nv0 = nc[0] + 1, nv1 = nc[1] + 1;
+  for(int64_t p = 0; p < P; ++p)
+  {
+    double hsum[3][2] = {{0, 0}, {0, 0}, {0, 0}};
+    for(int cn = 0; cn < (1 << dim); ++cn)
+    {
+      int c[3] = {lower[3 * p], lower[3 * p + 1], lower[3 * p + 2]};
+      for(int d = 0; d < dim; ++d) c[d] += (cn >> d) & 1;
+      double X[8 * 3];
+      for(int v = 0; v < (1 << dim); ++v)
+      {
+        int vi[3] = {c[0], c[1], c[2]};
+        for(int d = 0; d < dim; ++d) vi[d] += (v >> d) & 1;
+        const int64_t vid = vi[0] + (int64_t)nv0 * (vi[1] + (int64_t)nv1 * vi[2]);
+        for(int d = 0; d < dim; ++d) X[v * dim + d] = coords[vid * dim + d];
+      }
+      double h[3];
+      cell_arc_lengths(dim, X, nq, h);
+      for(int d = 0; d < dim; ++d) hsum[d][(cn >> d) & 1] += h[d] / (1 << (dim - 1));
+    }
+    for(int d = 0; d < dim; ++d)
+      for(int c = 0; c < 2; ++c) out[(p * dim + d) * 2 + c] = hsum[d][c];
+  }
+  free(lower);
+  free(color);
+  return 0;
+}
+
+/* Additive vertex-patch Schwarz vmult with per-patch surrogate widths hp[(p*dim+d)*2+c]
+ * (one FD problem per patch and direction), lexicographic cells. */
+int or_schwarz_vmult_surrogate(int dim, int k, const int *nc_in, const double *hp, double ip,
+                               double omega, const double *src, double *dst)
+{
+  int nc[3] = {1, 1, 1};
+  for(int d = 0; d < dim; ++d) nc[d] = nc_in[d];
+  double *hx = (double *)malloc(sizeof(double) * nc[0]);
+  double *hy = (double *)malloc(sizeof(double) * nc[1]);
+  double *hz = (double *)malloc(sizeof(double) * nc[2]);
+  for(int c = 0; c < nc[0]; ++c) hx[c] = 1.0 / nc[0];
+  for(int c = 0; c < nc[1]; ++c) hy[c] = 1.0 / nc[1];
+  for(int c = 0; c < nc[2]; ++c) hz[c] = 1.0 / nc[2];
+  level_t L;
+  level_init(&L, dim, k, nc, hx, hy, hz, ip, NULL);
+  patches_t T;
+  patches_build(&T, &L, 1, 0);
+  /* replace the FD entries by per-patch surrogate problems */
+  free(T.cache.items);
+  memset(&T.cache, 0, sizeof(T.cache));
+  for(int64_t p = 0; p < T.P; ++p)
+  {
+    int32_t lo[3];
+    /* recover the patch's lower cell from its first cell start */
+    const int64_t cell0 = T.cell_first[p * T.npc] / L.ncell_dofs;
+    lo[0] = (int32_t)(cell0 % nc[0]);
+    lo[1] = (int32_t)((cell0 / nc[0]) % nc[1]);
+    lo[2] = (int32_t)(cell0 / ((int64_t)nc[0] * nc[1]));
+    for(int d = 0; d < dim; ++d)
+    {
+      /* always a new entry (no key sharing): index = p*dim + d */
+      if(T.cache.n == T.cache.cap)
+      {
+        T.cache.cap = T.cache.cap ? 2 * T.cache.cap : 64;
+        T.cache.items = (fd1d_t *)realloc(T.cache.items, sizeof(fd1d_t) * T.cache.cap);
+      }
+      fd1d_t *f = &T.cache.items[T.cache.n];
+      const double hh[2] = {hp[(p * dim + d) * 2], hp[(p * dim + d) * 2 + 1]};
+      const int blo = lo[d] == 0, bhi = lo[d] + 1 == nc[d] - 1;
+      double M[OR_MAXN * OR_MAXN], A[OR_MAXN * OR_MAXN];
+      or_patch_matrices_1d(k, 2, hh, blo, bhi, ip, M, A);
+      if(or_gen_eig(2 * (k + 1), A, M, f->S, f->lam) != 0) return -1;
+      f->ncp = 2;
+      f->h0 = hh[0];
+      f->h1 = hh[1];
+      f->lo = blo;
+      f->hi = bhi;
+      T.fd[p * dim + d] = T.cache.n++;
+    }
+  }
+  memset(dst, 0, sizeof(double) * L.n_dofs);
+  for(int c = 0; c < T.ncol; ++c) apply_color(&L, &T, c, 2, omega, NULL, src, dst);
+  patches_free(&T);
+  free(hx);
+  free(hy);
+  free(hz);
+  return 0;
+}

@@ -387,3 +387,25 @@ def test_streamed_kernel_rejects_unsupported(tpss, cuda):
     x = torch.zeros(sh.n_dofs(), dtype=torch.float64, device=cuda)
     with pytest.raises(tpss.TPSSInvalidArgument):
         p.vmult(x, x.clone())
+
+
+@pytest.mark.parametrize("dim,k,nc,precision", [(2, 3, (6, 5), 0), (3, 2, (4, 3, 5), 0), (3, 3, (5, 4, 4), 1),
+                                                 (2, 5, (4, 4), 1)])
+def test_surrogate_patches_on_distorted_mesh(tpss, oracle, cuda, dim, k, nc, precision):
+    """Vertex patches on a distorted mesh with surrogate Cartesian widths (average arc lengths)."""
+    import torch
+    X = oracle.distorted_coords(dim, nc, 42)
+    N = int(np.prod(nc)) * (k + 1) ** dim
+    src = philox(77, N)
+    ad = tpss.SubdomainHandler.AdditionalData(dim=dim, degree=k, n_cells=nc, patch_variant=1,
+                                              vertex_coords=X)
+    sh = tpss.SubdomainHandler(ad)
+    p = tpss.SchwarzPreconditioner()
+    p.initialize(sh, None, tpss.SchwarzPreconditioner.AdditionalData(relaxation=0.4, precision=precision))
+    s = torch.tensor(src, dtype=torch.float64, device=cuda)
+    d = torch.empty_like(s)
+    p.vmult(d, s)
+    ref = oracle.schwarz_vmult_surrogate(dim, k, nc, oracle.surrogate_h(dim, nc, X), src, omega=0.4)
+    assert rel_err(d.cpu().numpy(), ref) <= (1e-12 if precision == 0 else 2e-5)
+    with pytest.raises(tpss.TPSSNotImplemented):
+        tpss.LaplaceOperator(sh, 1.0)

@@ -113,6 +113,8 @@ class SubdomainHandler:
         cell_h: Optional[Sequence[Sequence[float]]] = None
         cell_dof_start: Optional[Sequence[int]] = None
         coloring: Optional[Sequence[int]] = None  # user coloring in default patch order
+        vertex_coords: Optional[Sequence[float]] = None  # distorted mesh: [(n+1)^dim, dim]
+        surrogate_n_q: int = 5
 
     def __init__(self, additional_data: Optional["SubdomainHandler.AdditionalData"] = None):
         self._h = None
@@ -143,6 +145,11 @@ class SubdomainHandler:
             col = np.ascontiguousarray(ad.coloring, dtype=np.int32)
             keep.append(col)
             d.patch_color = col.ctypes.data_as(C.POINTER(C.c_int32))
+        if ad.vertex_coords is not None:
+            vc = np.ascontiguousarray(ad.vertex_coords, dtype=np.float64)
+            keep.append(vc)
+            d.vertex_coords = vc.ctypes.data_as(C.POINTER(C.c_double))
+        d.surrogate_n_q = int(ad.surrogate_n_q)
         h = C.c_void_p()
         check(L.tpss_layout_create(C.byref(d), C.byref(h)))
         self._h = h

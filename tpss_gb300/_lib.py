@@ -57,7 +57,8 @@ class LayoutDesc(C.Structure):
     _fields_ = [("dim", C.c_int), ("degree", C.c_int), ("dof_layout", C.c_int),
                 ("patch_variant", C.c_int), ("smoother_variant", C.c_int),
                 ("n_cells", C.c_int * 3), ("cell_h", C.POINTER(C.c_double) * 3),
-                ("cell_dof_start", C.POINTER(C.c_int64)), ("patch_color", C.POINTER(C.c_int32))]
+                ("cell_dof_start", C.POINTER(C.c_int64)), ("patch_color", C.POINTER(C.c_int32)),
+                ("vertex_coords", C.POINTER(C.c_double)), ("surrogate_n_q", C.c_int)]
 
 
 class PrecondDesc(C.Structure):

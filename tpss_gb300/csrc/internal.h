@@ -186,6 +186,7 @@ struct tpss_layout
   tpss::DeviceBuffer<int32_t> d_patch_fd;     // P*dim
   tpss::DeviceBuffer<int64_t> d_cell_start;   // n_cells (empty when lexicographic)
   std::vector<int32_t> vertex_fd[3];           // vertex patches: FD entry of vertex v_d, per d
+  bool per_patch_fd = false;                   // FD keys differ per patch (surrogate widths)
   tpss::DeviceBuffer<int32_t> d_vertex_fd[3];
 };
 

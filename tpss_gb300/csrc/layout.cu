@@ -10,6 +10,7 @@
 // it is checked to be conflict-free (no cell twice within a color), the contract the reference
 // leaves to the user for additive TBB loops (patch_info.templates.h:461-470).
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -49,6 +50,90 @@ struct PatchRec
   bool boundary;
   int64_t lex;  // default lexicographic anchor order
 };
+
+// ---- surrogate widths of vertex patches on distorted meshes
+// Gauss-Lobatto points and weights on [0,1] (endpoints plus roots of P'_{n-1}).
+void lobatto_rule(int n, std::vector<double> &z, std::vector<double> &w)
+{
+  z.assign(n, 0.0);
+  w.assign(n, 0.0);
+  const int m = n - 1;
+  for(int i = 0; i < n; ++i)
+  {
+    double x = -std::cos(M_PI * i / m);
+    auto leg = [m](double t, double &p, double &dp) {
+      double p0 = 1.0, p1 = t;
+      for(int j = 2; j <= m; ++j)
+      {
+        const double p2 = ((2 * j - 1) * t * p1 - (j - 1) * p0) / j;
+        p0 = p1;
+        p1 = p2;
+      }
+      p = m == 0 ? 1.0 : p1;
+      dp = m * (t * p1 - p0) / (t * t - 1.0);
+    };
+    double p = 0, dp = 0;
+    if(i > 0 && i < m)
+      for(int it = 0; it < 200; ++it)
+      {
+        leg(x, p, dp);
+        const double ddp = (2.0 * x * dp - m * (m + 1.0) * p) / (1.0 - x * x);
+        const double step = dp / ddp;
+        x -= step;
+        if(std::fabs(step) < 1e-17) break;
+      }
+    if(i == 0 || i == m)
+      p = (i == 0 && (m % 2)) ? -1.0 : 1.0;
+    else
+      leg(x, p, dp);
+    z[i] = 0.5 * (x + 1.0);
+    w[i] = 1.0 / (n * (n - 1.0) * p * p);
+  }
+}
+
+// arc length in each direction of the trilinear cell with corner coordinates X[2^dim][dim]
+void cell_arc_lengths(int dim, const double *X, const std::vector<double> &z,
+                      const std::vector<double> &w, double *h)
+{
+  const int nq = (int)z.size();
+  auto map = [&](const double *xi, double *x) {
+    for(int c = 0; c < dim; ++c) x[c] = 0.0;
+    for(int v = 0; v < (1 << dim); ++v)
+    {
+      double wt = 1.0;
+      for(int e = 0; e < dim; ++e) wt *= ((v >> e) & 1) ? xi[e] : 1.0 - xi[e];
+      for(int c = 0; c < dim; ++c) x[c] += wt * X[v * dim + c];
+    }
+  };
+  for(int d = 0; d < dim; ++d)
+  {
+    double acc = 0.0;
+    const int nf = dim == 2 ? nq : nq * nq;
+    for(int f = 0; f < nf; ++f)
+    {
+      const int fi[2] = {f % nq, f / nq};
+      double wf = 1.0;
+      for(int t = 0; t < dim - 1; ++t) wf *= w[fi[t]];
+      double len = 0.0, prev[3] = {0, 0, 0};
+      for(int i = 0; i < nq; ++i)
+      {
+        double xi[3] = {0, 0, 0}, x[3];
+        int t = 0;
+        for(int e = 0; e < dim; ++e) xi[e] = e == d ? z[i] : z[fi[t++]];
+        map(xi, x);
+        if(i > 0)
+        {
+          double s2 = 0.0;
+          for(int c = 0; c < dim; ++c) s2 += (x[c] - prev[c]) * (x[c] - prev[c]);
+          len += std::sqrt(s2);
+        }
+        for(int c = 0; c < dim; ++c) prev[c] = x[c];
+      }
+      acc += wf * len;
+    }
+    h[d] = acc;
+  }
+}
 
 void build_layout(tpss_layout &L, const tpss_layout_desc &d)
 {
@@ -167,6 +252,15 @@ void build_layout(tpss_layout &L, const tpss_layout_desc &d)
   L.cell_multiplicity.assign(L.n_cells, 0);
   std::vector<int32_t> last_color(L.n_cells, -1);
   std::map<std::tuple<double, double, int, int>, int32_t> keymap;
+  if(d.vertex_coords)
+  {
+    TPSS_REQUIRE(vertex, "surrogate widths are defined for vertex patches");
+    TPSS_REQUIRE(d.surrogate_n_q == 0 || (d.surrogate_n_q >= 2 && d.surrogate_n_q <= 16),
+                 "surrogate_n_q must be in 2..16");
+    L.per_patch_fd = true;
+  }
+  std::vector<double> gl_z, gl_w;
+  if(d.vertex_coords) lobatto_rule(d.surrogate_n_q ? d.surrogate_n_q : 5, gl_z, gl_w);
   for(int64_t p = 0; p < L.P; ++p)
   {
     const auto &r = recs[p];
@@ -189,10 +283,35 @@ void build_layout(tpss_layout &L, const tpss_layout_desc &d)
              "coloring conflict: a cell belongs to two patches of color " + std::to_string(r.color));
       last_color[cell] = r.color;
     }
+    double hs[3][2] = {{0, 0}, {0, 0}, {0, 0}};
+    if(d.vertex_coords)
+    {
+      // surrogate widths: average over the 2^(dim-1) patch cells sharing a 1-D cell index
+      for(int cn = 0; cn < L.npc; ++cn)
+      {
+        int c[3] = {r.lo[0], r.lo[1], r.lo[2]};
+        for(int e = 0; e < dim; ++e) c[e] += (cn >> e) & 1;
+        double X[8 * 3], hc[3];
+        for(int v = 0; v < (1 << dim); ++v)
+        {
+          int vi[3] = {c[0], c[1], c[2]};
+          for(int e = 0; e < dim; ++e) vi[e] += (v >> e) & 1;
+          const int64_t vid = vi[0] + (int64_t)(L.nc[0] + 1) * (vi[1] + (int64_t)(L.nc[1] + 1) * vi[2]);
+          for(int e = 0; e < dim; ++e) X[v * dim + e] = d.vertex_coords[vid * dim + e];
+        }
+        cell_arc_lengths(dim, X, gl_z, gl_w, hc);
+        for(int e = 0; e < dim; ++e) hs[e][(cn >> e) & 1] += hc[e] / (1 << (dim - 1));
+      }
+    }
     for(int dd = 0; dd < dim; ++dd)
     {
       const int c0 = r.lo[dd], c1 = r.lo[dd] + L.ncp - 1;
-      const double h0 = L.h[dd][c0], h1 = L.ncp == 2 ? L.h[dd][c1] : 0.0;
+      double h0 = L.h[dd][c0], h1 = L.ncp == 2 ? L.h[dd][c1] : 0.0;
+      if(d.vertex_coords)
+      {
+        h0 = hs[dd][0];
+        h1 = hs[dd][1];
+      }
       const int lo = c0 == 0, hi = c1 == L.nc[dd] - 1;
       auto key = std::make_tuple(h0, h1, lo, hi);
       auto it = keymap.find(key);
@@ -211,7 +330,7 @@ void build_layout(tpss_layout &L, const tpss_layout_desc &d)
   L.patch_first = std::move(first);
   // vertex patches on the structured level: the FD key of direction d depends only on the
   // vertex index v_d, which the streaming kernel uses instead of per-patch indices
-  if(vertex)
+  if(vertex && !L.per_patch_fd)
     for(int dd = 0; dd < dim; ++dd)
     {
       L.vertex_fd[dd].assign(L.nc[dd] + 1, -1);

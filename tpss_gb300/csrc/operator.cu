@@ -459,6 +459,8 @@ extern "C" int tpss_operator_create(const tpss_layout *layout, double ip_factor,
     TPSS_REQUIRE(layout && out, "null argument");
     TPSS_REQUIRE(ip_factor > 0.0, "ip_factor must be positive");
     *out = nullptr;
+    if(layout->per_patch_fd)
+      fail(TPSS_ERR_NOT_IMPLEMENTED, "the SIPG operator is implemented for Cartesian (tensor-product) levels");
     layout_to_device(*layout);
     auto op = std::make_unique<tpss_operator>();
     op->layout = layout;

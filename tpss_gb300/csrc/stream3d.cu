@@ -58,7 +58,7 @@ bool launch_stream(const tpss_layout &L, const StreamLaunch &l, cudaStream_t s)
 
 bool stream_supported(const tpss_layout &L)
 {
-  return L.dim == 3 && L.patch_variant == TPSS_PATCH_VERTEX && L.k >= 1 && L.k <= 4 &&
+  return L.dim == 3 && L.patch_variant == TPSS_PATCH_VERTEX && !L.per_patch_fd && L.k >= 1 && L.k <= 4 &&
          L.nc[0] >= 2 && L.nc[1] >= 2 && L.nc[2] >= 2;
 }
 
