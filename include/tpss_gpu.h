@@ -150,6 +150,31 @@ int tpss_precond_vmult_add(tpss_precond *p, double *dst, const double *src, void
  * (TPSS_ERR_NOT_IMPLEMENTED). */
 int tpss_precond_Tvmult(tpss_precond *p, double *dst, const double *src, void *stream);
 
+/*
+ * Allocation-free vmult.  This entry point has no counterpart in the reference.
+ *
+ * Same result as tpss_precond_vmult for additive vertex patches in 3D with FP32 arithmetic,
+ * degree <= 4, on a Cartesian level (the column-streamed smoother), but the call allocates
+ * and frees no device memory.  It is meant for callers that may not allocate once their solve
+ * has started: a host application that owns all device memory through its own pool and
+ * forbids library-side cudaMalloc/cudaFree after setup, or one that cannot afford the device
+ * synchronization of cudaFree or an out-of-memory failure in the middle of an iteration.
+ * (tpss_precond_vmult grows its scratch buffer with cudaMalloc on first use.)
+ *
+ * The scratch for the partial sums of cells shared between work items is a fixed device array
+ * of 32 MiB (8 Mi floats), held by every GPU that loads the library until the process exits.
+ * A level whose scratch need exceeds it is rejected with TPSS_ERR_INVALID_ARGUMENT; 3D DGQ4
+ * fits up to 33^3 cells.  Everything else the call uses (index tables, FD data) was
+ * allocated when the preconditioner was created.
+ *
+ * The first call on a device looks up the array's device address (cudaGetSymbolAddress) with
+ * that device current; make that first call before any stream capture.  All calls share the
+ * array and it keeps the last call's contents; every entry a call reads is written by the same
+ * call first, so nothing needs clearing, but calls that overlap on the GPU (for example on two
+ * streams at once) race on it.
+ */
+int tpss_precond_vmult_static_scratch(tpss_precond *p, double *dst, const double *src, void *stream);
+
 /* TimeInfo (TPSS/time_info.h:23-64): the five preconditioner timers of
  * schwarz_preconditioner.templates.h:22-26, in seconds, measured with CUDA events. */
 typedef struct tpss_time_info

@@ -97,6 +97,7 @@ SIGNATURES = {
     "tpss_precond_vmult": (C.c_int, [_vp, _vp, _vp, _vp]),
     "tpss_precond_vmult_add": (C.c_int, [_vp, _vp, _vp, _vp]),
     "tpss_precond_Tvmult": (C.c_int, [_vp, _vp, _vp, _vp]),
+    "tpss_precond_vmult_static_scratch": (C.c_int, [_vp, _vp, _vp, _vp]),
     "tpss_precond_time_info": (C.c_int, [_vp, C.POINTER(TimeInfo), C.POINTER(C.c_int)]),
     "tpss_precond_destroy": (None, [_vp]),
     "tpss_smoother_create": (C.c_int, [_vp, _vp, C.c_int, C.c_double, C.POINTER(_vp)]),

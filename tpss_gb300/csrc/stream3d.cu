@@ -1,4 +1,7 @@
 // stream3d.cu -- launcher of the streamed 3D vertex-patch smoother (see stream3d.cuh).
+#include <mutex>
+#include <string>
+
 #include "internal.h"
 #include "stream3d.cuh"
 
@@ -74,3 +77,123 @@ bool launch_stream3d(const tpss_layout &L, const StreamLaunch &l, cudaStream_t s
   }
 }
 }  // namespace tpss
+
+// ------------------------------------------------------------------------------------------
+// Allocation-free variant of the streamed smoother (tpss_precond_vmult_static_scratch).
+//
+// The regular vmult keeps the halo partial sums in a buffer that it grows with cudaMalloc
+// on first use.  This variant uses a fixed scratch array in device global memory instead,
+// defined at file scope below, so the call itself allocates and frees nothing.
+// ------------------------------------------------------------------------------------------
+namespace tpss
+{
+namespace
+{
+// maximum halo size of the allocation-free entry point: 8 Mi floats = 32 MiB per device
+constexpr size_t kStaticHaloFloats = size_t(8) << 20;
+}  // namespace
+}  // namespace tpss
+
+// Every GPU that loads the library holds this array until the process exits.
+static __device__ __align__(256) float g_static_halo[tpss::kStaticHaloFloats];
+
+namespace tpss
+{
+namespace
+{
+// Host code cannot use g_static_halo directly (its name is a host-side stand-in); the
+// device address is looked up once per device with that device current.
+std::mutex g_static_halo_mu;
+float *g_static_halo_ptr[64] = {nullptr};
+
+float *static_halo_address()
+{
+  int dev = 0;
+  TPSS_CUDA(cudaGetDevice(&dev));
+  TPSS_REQUIRE(dev >= 0 && dev < 64, "device index out of range");
+  std::lock_guard<std::mutex> lock(g_static_halo_mu);
+  if(!g_static_halo_ptr[dev])
+  {
+    void *ptr = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&ptr, g_static_halo);
+    if(e != cudaSuccess || !ptr)
+      fail(TPSS_ERR_CUDA, std::string("cudaGetSymbolAddress(g_static_halo): ") + cudaGetErrorString(e));
+    g_static_halo_ptr[dev] = static_cast<float *>(ptr);
+  }
+  return g_static_halo_ptr[dev];
+}
+
+template<class C>
+void launch_stream_static(const tpss_layout &L, const tpss_precond &p, const double *src, double *dst,
+                          cudaStream_t s)
+{
+  stream::StreamArgs a;
+  a.src = src;
+  a.dst = dst;
+  a.cell_start = L.lexicographic ? nullptr : L.d_cell_start.ptr;
+  a.fd = p.tables->fd32.ptr;
+  a.fd_eo = p.tables->fd32_eo.ptr;
+  a.sym = p.tables->sym.ptr;
+  a.es_eo = 4 * (L.n / 2) * p.tables->hpad32 + p.tables->npad32;
+  for(int d = 0; d < 3; ++d)
+  {
+    a.vfd[d] = L.d_vertex_fd[d].ptr;
+    a.nc[d] = L.nc[d];
+  }
+  a.T[0] = (L.nc[0] - 1 + C::BX - 1) / C::BX;
+  a.T[1] = (L.nc[1] - 1 + C::BY - 1) / C::BY;
+  a.T[2] = (L.nc[2] - 1 + C::BZ - 1) / C::BZ;
+  a.omega = (float)p.desc.relaxation;
+  a.ras = p.desc.use_ras_weights != 0;
+  const int64_t n_items = (int64_t)a.T[0] * a.T[1] * a.T[2];
+  const size_t halo_floats = (size_t)n_items * (C::BZ + 1) * C::LCELLS * C::CD;
+  if(halo_floats > kStaticHaloFloats)
+    fail(TPSS_ERR_INVALID_ARGUMENT,
+         "level too large for the allocation-free smoother: its halo needs " +
+           std::to_string(halo_floats) + " floats, the static scratch holds " +
+           std::to_string(kStaticHaloFloats) + " (32 MiB)");
+  a.halo = static_halo_address();
+  static int per_sm = 0;
+  const size_t smem = C::smem_bytes();
+  if(per_sm == 0)
+  {
+    TPSS_CUDA(cudaFuncSetAttribute(stream::stream_kernel<C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)smem));
+    int occ = 0;
+    TPSS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, stream::stream_kernel<C>, C::THREADS, smem));
+    per_sm = occ < 1 ? 1 : occ;
+  }
+  const int64_t cap = (int64_t)num_sms() * per_sm;
+  const int grid = (int)(n_items < cap ? n_items : cap);
+  stream::stream_kernel<C><<<grid, C::THREADS, smem, s>>>(a);
+  TPSS_CUDA(cudaGetLastError());
+  const int64_t work = L.n_cells * C::CD;
+  const int64_t fb = (work + 255) / 256, fcap = (int64_t)num_sms() * 8;
+  stream::fixup_kernel<C><<<(int)(fb < fcap ? fb : fcap), 256, 0, s>>>(a);
+  TPSS_CUDA(cudaGetLastError());
+}
+}  // namespace
+}  // namespace tpss
+
+extern "C" int tpss_precond_vmult_static_scratch(tpss_precond *p, double *dst, const double *src,
+                                                 void *stream)
+{
+  return tpss::guarded([&] {
+    TPSS_REQUIRE(p && dst && src, "null argument");
+    TPSS_REQUIRE(dst != src, "dst and src must not alias");
+    const tpss_layout &L = *p->tables->layout;
+    if(!(L.smoother_variant == TPSS_ADDITIVE && p->desc.precision == TPSS_FP32 && tpss::stream_supported(L)))
+      tpss::fail(TPSS_ERR_INVALID_ARGUMENT,
+                 "the allocation-free smoother needs additive 3D vertex patches on a Cartesian level, "
+                 "FP32 arithmetic and degree <= 4");
+    cudaStream_t s = tpss::as_stream(stream);
+    switch(L.k)
+    {
+    case 1: tpss::launch_stream_static<tpss::Cfg3<2>>(L, *p, src, dst, s); break;
+    case 2: tpss::launch_stream_static<tpss::Cfg3<3>>(L, *p, src, dst, s); break;
+    case 3: tpss::launch_stream_static<tpss::Cfg3<4>>(L, *p, src, dst, s); break;
+    case 4: tpss::launch_stream_static<tpss::Cfg3<5>>(L, *p, src, dst, s); break;
+    default: tpss::fail(TPSS_ERR_INVALID_ARGUMENT, "degree must be <= 4");
+    }
+  });
+}
