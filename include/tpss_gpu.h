@@ -121,6 +121,8 @@ typedef struct tpss_precond_desc
   int kernel_variant;          /* additive smoother kernel: TPSS_KERNEL_AUTO, TPSS_KERNEL_COLOR
                                   (one fused launch per color) or TPSS_KERNEL_STREAM (3D vertex
                                   patches, FP32, k <= 4: column-streamed, one pass) */
+  int stream_variant;          /* initial work decomposition of the column-streamed kernel
+                                  (0..3, see tpss_precond_autotune); 0 by default */
 } tpss_precond_desc;
 
 #define TPSS_KERNEL_AUTO 0
@@ -174,6 +176,15 @@ int tpss_precond_Tvmult(tpss_precond *p, double *dst, const double *src, void *s
  * streams at once) race on it.
  */
 int tpss_precond_vmult_static_scratch(tpss_precond *p, double *dst, const double *src, void *stream);
+
+/* Autotuner (no counterpart in the reference): times every work decomposition of the smoother
+ * kernel for this level (for the column-streamed kernel: pencils per thread and vertex layers per
+ * work item) on the caller's vectors, `reps` applications each, and keeps the fastest for later
+ * vmult calls.  On return dst = P src, *chosen is the selected variant, ms_per_variant (optional,
+ * >= 4 entries) the measured milliseconds per application and *n_variants their count (1 when the
+ * level has a single kernel). */
+int tpss_precond_autotune(tpss_precond *p, double *dst, const double *src, int reps, int *chosen,
+                          double *ms_per_variant, int *n_variants, void *stream);
 
 /* TimeInfo (TPSS/time_info.h:23-64): the five preconditioner timers of
  * schwarz_preconditioner.templates.h:22-26, in seconds, measured with CUDA events. */

@@ -63,6 +63,8 @@ public:
     std::vector<std::vector<double>> cell_h;  // empty: uniform 1/n per direction
     std::vector<int64_t> cell_dof_start;      // empty: lexicographic cell blocks
     std::vector<int32_t> coloring;            // empty: default coloring
+    std::vector<double> vertex_coords;        // distorted mesh: (n+1)^dim x dim, empty: Cartesian
+    int surrogate_n_q = 5;
   };
 
   SubdomainHandler() = default;
@@ -85,6 +87,8 @@ public:
       d.cell_h[i] = ad.cell_h[i].empty() ? nullptr : ad.cell_h[i].data();
     d.cell_dof_start = ad.cell_dof_start.empty() ? nullptr : ad.cell_dof_start.data();
     d.patch_color = ad.coloring.empty() ? nullptr : ad.coloring.data();
+    d.vertex_coords = ad.vertex_coords.empty() ? nullptr : ad.vertex_coords.data();
+    d.surrogate_n_q = ad.surrogate_n_q;
     check(tpss_layout_create(&d, &handle_));
     additional_data_ = ad;
   }
@@ -167,6 +171,7 @@ public:
     double ip_factor = 1.;
     bool check_finite = false;
     int kernel_variant = TPSS_KERNEL_AUTO;
+    int stream_variant = 0;
   };
 
   SchwarzPreconditioner() = default;
@@ -213,6 +218,15 @@ public:
     check(tpss_precond_Tvmult(handle_, dst, src, stream));
   }
 
+  /* times the kernel variants on (src -> dst), keeps the fastest; returns its index */
+  int autotune(double *dst, const double *src, int reps = 5, void *stream = nullptr)
+  {
+    int chosen = 0, nv = 0;
+    double ms[8];
+    check(tpss_precond_autotune(handle_, dst, src, reps, &chosen, ms, &nv, stream));
+    return chosen;
+  }
+
   std::vector<TimeInfo> get_time_data() const
   {
     int n = 0;
@@ -243,6 +257,7 @@ private:
     d.ip_factor = ad.ip_factor;
     d.check_finite = ad.check_finite;
     d.kernel_variant = ad.kernel_variant;
+    d.stream_variant = ad.stream_variant;
     return d;
   }
 

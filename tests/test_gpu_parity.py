@@ -409,3 +409,30 @@ def test_surrogate_patches_on_distorted_mesh(tpss, oracle, cuda, dim, k, nc, pre
     assert rel_err(d.cpu().numpy(), ref) <= (1e-12 if precision == 0 else 2e-5)
     with pytest.raises(tpss.TPSSNotImplemented):
         tpss.LaplaceOperator(sh, 1.0)
+
+
+@pytest.mark.parametrize("k,nc", [(4, (9, 6, 19)), (3, (7, 5, 13)), (2, (6, 6, 17)), (1, (5, 9, 18))])
+def test_streamed_variants_and_autotune(tpss, oracle, cuda, k, nc):
+    """Every work decomposition of the streamed kernel gives the oracle's result; the autotuner
+    keeps one of them and leaves dst = P src."""
+    import torch
+    N = int(np.prod(nc)) * (k + 1) ** 3
+    src = philox(400 + k, N)
+    ref = oracle.schwarz_vmult(3, k, nc, src, patch_variant=1, omega=0.15)
+    ad = tpss.SubdomainHandler.AdditionalData(dim=3, degree=k, n_cells=nc, patch_variant=1)
+    sh = tpss.SubdomainHandler(ad)
+    s = torch.tensor(src, dtype=torch.float64, device=cuda)
+    for v in range(4):
+        p = tpss.SchwarzPreconditioner()
+        p.initialize(sh, None, tpss.SchwarzPreconditioner.AdditionalData(
+            relaxation=0.15, precision=1, kernel_variant=2, stream_variant=v))
+        d = torch.full_like(s, float("nan"))
+        p.vmult(d, s)
+        assert rel_err(d.cpu().numpy(), ref) <= 2e-5, v
+    d = torch.full_like(s, float("nan"))
+    chosen, ms = p.autotune(d, s, reps=2)
+    assert 0 <= chosen < 4 and len(ms) == 4 and all(t > 0 for t in ms)
+    assert rel_err(d.cpu().numpy(), ref) <= 2e-5
+    d2 = torch.empty_like(s)
+    p.vmult(d2, s)
+    assert rel_err(d2.cpu().numpy(), ref) <= 2e-5

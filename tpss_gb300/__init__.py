@@ -244,6 +244,7 @@ class SchwarzPreconditioner:
         ip_factor: float = 1.0
         check_finite: bool = False
         kernel_variant: int = 0  # 0 auto, 1 one launch per color, 2 column-streamed (3D, FP32)
+        stream_variant: int = 0  # work decomposition of the column-streamed kernel (0..3)
 
     def __init__(self):
         self._h = None
@@ -261,6 +262,7 @@ class SchwarzPreconditioner:
         d.precision, d.ip_factor = int(ad.precision), float(ad.ip_factor)
         d.check_finite = int(ad.check_finite)
         d.kernel_variant = int(ad.kernel_variant)
+        d.stream_variant = int(ad.stream_variant)
         return d
 
     def initialize(self, subdomain_handler, linear_operator=None, additional_data=None):
@@ -320,6 +322,17 @@ class SchwarzPreconditioner:
     def Tvmult(self, dst, src, stream=None):
         n = self.m()
         check(load().tpss_precond_Tvmult(self._h, _ptr(dst, n), _ptr(src, n), _stream(stream)))
+
+    def autotune(self, dst, src, reps=5, stream=None):
+        """Time the kernel variants for this level on (src -> dst) and keep the fastest.
+        Returns (chosen variant, milliseconds per variant)."""
+        n = self.m()
+        chosen, nv = C.c_int(0), C.c_int(0)
+        ms = np.zeros(8)
+        check(load().tpss_precond_autotune(self._h, _ptr(dst, n), _ptr(src, n), int(reps),
+                                           C.byref(chosen), ms.ctypes.data_as(C.POINTER(C.c_double)),
+                                           C.byref(nv), _stream(stream)))
+        return chosen.value, ms[: nv.value].tolist()
 
     def get_time_data(self):
         L = load()

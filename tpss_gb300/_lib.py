@@ -65,7 +65,7 @@ class PrecondDesc(C.Structure):
     _fields_ = [("relaxation", C.c_double), ("reverse", C.c_int), ("symmetrized", C.c_int),
                 ("use_ras_weights", C.c_int), ("use_ras_boolean_weights", C.c_int),
                 ("precision", C.c_int), ("ip_factor", C.c_double), ("check_finite", C.c_int),
-                ("kernel_variant", C.c_int)]
+                ("kernel_variant", C.c_int), ("stream_variant", C.c_int)]
 
 
 class TimeInfo(C.Structure):
@@ -98,6 +98,8 @@ SIGNATURES = {
     "tpss_precond_vmult_add": (C.c_int, [_vp, _vp, _vp, _vp]),
     "tpss_precond_Tvmult": (C.c_int, [_vp, _vp, _vp, _vp]),
     "tpss_precond_vmult_static_scratch": (C.c_int, [_vp, _vp, _vp, _vp]),
+    "tpss_precond_autotune": (C.c_int, [_vp, _vp, _vp, C.c_int, C.POINTER(C.c_int), _dp,
+                                        C.POINTER(C.c_int), _vp]),
     "tpss_precond_time_info": (C.c_int, [_vp, C.POINTER(TimeInfo), C.POINTER(C.c_int)]),
     "tpss_precond_destroy": (None, [_vp]),
     "tpss_smoother_create": (C.c_int, [_vp, _vp, C.c_int, C.c_double, C.POINTER(_vp)]),

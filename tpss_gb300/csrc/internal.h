@@ -243,6 +243,7 @@ struct tpss_precond
   tpss::DeviceBuffer<double> residual;  // multiplicative scratch
   tpss::DeviceBuffer<int> flag;         // finiteness check
   tpss::DeviceBuffer<float> halo;       // streamed kernel: partial sums of shared cells
+  int stream_variant = 0;               // streamed kernel variant (autotuner)
   std::vector<tpss::TimerSlot> timers;
   std::vector<tpss::PendingEvent> pending;
   std::vector<cudaEvent_t> event_pool;
@@ -291,8 +292,10 @@ struct StreamLaunch
   double omega;
   int ras;
   DeviceBuffer<float> *halo;  // scratch, grown on demand
+  int variant = 0;            // work decomposition chosen by the autotuner
 };
 bool stream_supported(const tpss_layout &L);
+int stream_variant_count(const tpss_layout &L);
 bool launch_stream3d(const tpss_layout &L, const StreamLaunch &l, cudaStream_t s);
 
 // upload the layout's index tables (layout.cu)

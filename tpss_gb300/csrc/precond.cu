@@ -166,6 +166,7 @@ void validate_desc(const tpss_precond_desc &d)
 {
   TPSS_REQUIRE(d.kernel_variant >= TPSS_KERNEL_AUTO && d.kernel_variant <= TPSS_KERNEL_STREAM,
                "invalid kernel variant");
+  TPSS_REQUIRE(d.stream_variant >= 0 && d.stream_variant <= 3, "stream_variant must be in 0..3");
   TPSS_REQUIRE(d.relaxation > 0.0, "Invalid relaxation factor.");
   TPSS_REQUIRE(d.precision == TPSS_FP64 || d.precision == TPSS_FP32, "invalid precision");
   if(d.use_ras_weights && d.use_ras_boolean_weights)
@@ -351,6 +352,7 @@ void precond_vmult(tpss_precond *p, double *dst, const double *src, cudaStream_t
       l.omega = p->desc.relaxation;
       l.ras = p->desc.use_ras_weights != 0;
       l.halo = &p->halo;
+      l.variant = p->stream_variant;
       if(!launch_stream3d(L, l, s)) fail(TPSS_ERR_CUDA, "streamed smoother launch failed");
     }
     else
@@ -421,6 +423,7 @@ extern "C" int tpss_precond_create(const tpss_layout *layout, tpss_operator *op,
     auto p = std::make_unique<tpss_precond>();
     p->desc = *desc;
     p->op = op;
+    p->stream_variant = desc->stream_variant;
     p->tables = build_tables(*layout, desc->ip_factor, desc->use_ras_weights != 0);
     p->timers.resize(5);
     for(int i = 0; i < 5; ++i) p->timers[i].name = kTimerNames[i];
@@ -574,3 +577,58 @@ extern "C" int tpss_smoother_vmult(tpss_smoother *sm, double *x, const double *b
 }
 
 extern "C" void tpss_smoother_destroy(tpss_smoother *s) { delete s; }
+
+extern "C" int tpss_precond_autotune(tpss_precond *p, double *dst, const double *src, int reps,
+                                     int *chosen, double *ms_per_variant, int *n_variants,
+                                     void *stream)
+{
+  return guarded([&] {
+    TPSS_REQUIRE(p && dst && src && reps >= 1, "invalid argument");
+    cudaStream_t s = as_stream(stream);
+    const tpss_layout &L = *p->tables->layout;
+    const int nv = use_stream(p) ? stream_variant_count(L) : 1;
+    if(n_variants) *n_variants = nv;
+    if(nv <= 1)
+    {
+      if(chosen) *chosen = 0;
+      if(ms_per_variant) ms_per_variant[0] = 0.;  // a single variant is not timed
+      precond_vmult(p, dst, src, s);
+      return;
+    }
+    struct Events
+    {
+      cudaEvent_t e[2] = {nullptr, nullptr};
+      ~Events()
+      {
+        for(cudaEvent_t x : e)
+          if(x) cudaEventDestroy(x);
+      }
+    } ev;
+    TPSS_CUDA(cudaEventCreate(&ev.e[0]));
+    TPSS_CUDA(cudaEventCreate(&ev.e[1]));
+    cudaEvent_t e0 = ev.e[0], e1 = ev.e[1];
+    int best = 0;
+    float best_ms = 0.f;
+    for(int v = 0; v < nv; ++v)
+    {
+      p->stream_variant = v;
+      precond_vmult(p, dst, src, s);  // warm-up (scratch sizing, attributes)
+      TPSS_CUDA(cudaEventRecord(e0, s));
+      for(int r = 0; r < reps; ++r) precond_vmult(p, dst, src, s);
+      TPSS_CUDA(cudaEventRecord(e1, s));
+      TPSS_CUDA(cudaEventSynchronize(e1));
+      float ms = 0.f;
+      TPSS_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      ms /= reps;
+      if(ms_per_variant) ms_per_variant[v] = ms;
+      if(v == 0 || ms < best_ms)
+      {
+        best = v;
+        best_ms = ms;
+      }
+    }
+    p->stream_variant = best;
+    if(chosen) *chosen = best;
+    precond_vmult(p, dst, src, s);  // dst holds the chosen variant's result
+  });
+}

@@ -65,14 +65,58 @@ bool stream_supported(const tpss_layout &L)
          L.nc[0] >= 2 && L.nc[1] >= 2 && L.nc[2] >= 2;
 }
 
+// Variants the autotuner chooses from (same mathematics, different work decomposition):
+//   0: 4x4 vertex columns, 8 vertex layers per item, 4 pencils per thread
+//   1: 4x4 columns, 8 layers, 5 (k = 4) or 2 (k <= 3) pencils per thread
+//   2: 4x4 columns, 4 layers per item (more items, more z-shared layers)
+//   3: 4x4 columns, 16 layers per item (fewer items, fewer z-shared layers)
+int stream_variant_count(const tpss_layout &L) { return stream_supported(L) ? 4 : 0; }
+
+template<int K1, int V>
+struct VariantCfg;
+template<int K1>
+struct VariantCfg<K1, 0>
+{
+  using type = stream::SCfg<K1, 4, 4, 8, 4>;
+};
+template<int K1>
+struct VariantCfg<K1, 1>
+{
+  using type = stream::SCfg<K1, 4, 4, 8, K1 == 5 ? 5 : 2>;
+};
+template<int K1>
+struct VariantCfg<K1, 2>
+{
+  using type = stream::SCfg<K1, 4, 4, 4, 4>;
+};
+template<int K1>
+struct VariantCfg<K1, 3>
+{
+  using type = stream::SCfg<K1, 4, 4, 16, 4>;
+};
+
+template<int K1>
+bool launch_variant(const tpss_layout &L, const StreamLaunch &l, cudaStream_t s, int v)
+{
+  switch(v)
+  {
+  case 0: return launch_stream<typename VariantCfg<K1, 0>::type>(L, l, s);
+  case 1: return launch_stream<typename VariantCfg<K1, 1>::type>(L, l, s);
+  case 2: return launch_stream<typename VariantCfg<K1, 2>::type>(L, l, s);
+  case 3: return launch_stream<typename VariantCfg<K1, 3>::type>(L, l, s);
+  default: return false;
+  }
+}
+
 bool launch_stream3d(const tpss_layout &L, const StreamLaunch &l, cudaStream_t s)
 {
+  const int v = l.variant;
   switch(L.k)
   {
-  case 1: return launch_stream<Cfg3<2>>(L, l, s);
-  case 2: return launch_stream<Cfg3<3>>(L, l, s);
-  case 3: return launch_stream<Cfg3<4>>(L, l, s);
-  case 4: return launch_stream<Cfg3<5>>(L, l, s);
+  case 1: return launch_variant<2>(L, l, s, v);
+  case 2: return launch_variant<3>(L, l, s, v);
+  case 3: return launch_variant<4>(L, l, s, v);
+  case 4: return launch_variant<5>(L, l, s, v);
   default: return false;
   }
 }
