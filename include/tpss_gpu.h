@@ -46,6 +46,19 @@ extern "C" {
 #define TPSS_ADDITIVE 0
 #define TPSS_MULTIPLICATIVE 1
 /* arithmetic of the smoother (gather, local solve, scatter); vectors stay FP64 */
+/* local solvers (tpss_precond_desc.local_solver) */
+#define TPSS_LOCAL_FD 0      /* fast diagonalization of the layout's 1-D patch problems
+                                (Cartesian, or surrogate patches on a distorted level) */
+#define TPSS_LOCAL_EXACT 1   /* dense inverse of the exact patch matrix (TensorProductMatrix
+                                basic state + InverseTable); needs the mapped level operator,
+                                at most 160 DoFs per patch */
+#define TPSS_LOCAL_KSUM 2    /* fast diagonalization of the Kronecker sum closest to the
+                                exact patch matrix with the surrogate masses fixed (low
+                                Kronecker-rank approximation, kroneckersvd.h:207-402); needs
+                                the mapped level operator */
+#define TPSS_LOCAL_LEARNED 3 /* surrogate 1-D problems corrected by a trained network
+                                (tpss_mlp) from the patch's vertex geometry */
+
 #define TPSS_FP64 0
 #define TPSS_FP32 1
 
@@ -54,6 +67,7 @@ typedef struct tpss_operator tpss_operator;
 typedef struct tpss_precond tpss_precond;
 typedef struct tpss_smoother tpss_smoother;
 typedef struct tpss_mg tpss_mg;
+typedef struct tpss_mlp tpss_mlp;
 
 /*
  * Patch layout of one level: replaces SubdomainHandler::reinit
@@ -123,6 +137,8 @@ typedef struct tpss_precond_desc
                                   patches, FP32, k <= 4: column-streamed, one pass) */
   int stream_variant;          /* initial work decomposition of the column-streamed kernel
                                   (0..3, see tpss_precond_autotune); 0 by default */
+  int local_solver;            /* TPSS_LOCAL_*: how the patch inverses are formed */
+  const tpss_mlp *model;       /* trained network for TPSS_LOCAL_LEARNED, else NULL */
 } tpss_precond_desc;
 
 #define TPSS_KERNEL_AUTO 0
@@ -230,6 +246,15 @@ typedef struct tpss_mg_desc
                          apps/multigrid.h:176-182), which lets the whole V-cycle be one graph */
   int use_graph;      /* capture the V-cycle in CUDA graphs (one graph with the dense coarse
                          solver; down- and up-sweep graphs around the CG coarse solve) */
+  const double *vertex_coords; /* NULL: Cartesian unit cube. Else the finest level's vertices,
+                                  lexicographic (x fastest), dim coordinates each: every level
+                                  is a distorted (multilinear) mesh whose vertices are every
+                                  2^(L-l)-th finest vertex, with the mapped SIPG operator and
+                                  surrogate-patch local solvers (create_distorted_cube,
+                                  apps/mesh.h:160-200; mapping_info.templates.h:42-240) */
+  int surrogate_n_q;           /* Gauss-Lobatto points of the surrogate arc lengths (0: 5) */
+  int local_solver;            /* TPSS_LOCAL_* of the level smoothers (distorted levels) */
+  const tpss_mlp *model;       /* trained network for TPSS_LOCAL_LEARNED */
 } tpss_mg_desc;
 
 int tpss_mg_create(const tpss_mg_desc *desc, tpss_mg **out);
@@ -260,6 +285,50 @@ int tpss_transfer_restrict_add(int dim, int degree, const int *n_cells_coarse, d
  * current GPU in FLOP/s for TPSS_FP32 or TPSS_FP64 (8 independent FMA chains per thread on
  * every SM, `iters` FMAs per chain, timed with CUDA events).  The roofline denominator of the
  * CUDA-core-bound fast-diagonalization kernels. */
+/* ---------------------------------------------------------------------------------------
+ * Learned local solver (no counterpart in the reference: its distorted-mesh local solver is
+ * the surrogate patch of mapping_info.templates.h:42-240). A small fully connected network
+ * (tanh hidden layers, linear output, FP32) maps a vertex patch's geometry to corrections of
+ * the surrogate 1-D problems; it is trained on the GPU against the Kronecker-sum fit of the
+ * exact patch matrices and used through tpss_precond_desc.local_solver = TPSS_LOCAL_LEARNED.
+ * All x / y / target arrays are device pointers, row-major [rows][width], FP32.
+ * ------------------------------------------------------------------------------------- */
+typedef struct tpss_mlp_desc
+{
+  int n_in, n_hidden, n_hidden_layers, n_out;
+  uint64_t seed;               /* Glorot-uniform initialisation */
+} tpss_mlp_desc;
+
+int tpss_mlp_create(const tpss_mlp_desc *desc, tpss_mlp **out);
+int tpss_mlp_sizes(const tpss_mlp *m, int *n_in, int *n_out);
+/* parameters: per layer W [out][in] row-major then b [out] (host arrays of n_params floats) */
+int tpss_mlp_n_params(const tpss_mlp *m, int64_t *n_params);
+int tpss_mlp_get_params(const tpss_mlp *m, float *host);
+int tpss_mlp_set_params(tpss_mlp *m, const float *host);
+int tpss_mlp_forward(tpss_mlp *m, const float *x, int64_t rows, float *y, void *stream);
+/* mean squared error over rows x n_out outputs and its gradient (host, n_params floats) */
+int tpss_mlp_loss_grad(tpss_mlp *m, const float *x, const float *target, int64_t rows, double *loss,
+                       float *grad_host);
+int tpss_mlp_eval_loss(tpss_mlp *m, const float *x, const float *target, int64_t rows, double *loss);
+/* Adam on mini-batches of a seeded permutation; loss_per_epoch (host, may be NULL) receives the
+ * full-set loss after every epoch */
+int tpss_mlp_train(tpss_mlp *m, const float *x, const float *target, int64_t rows, int epochs,
+                   int batch, double lr, uint64_t seed, double *loss_per_epoch, void *stream);
+void tpss_mlp_destroy(tpss_mlp *m);
+
+/* network sizes for a layout's vertex patches: n_in = 3^d d + 2d, n_out = d n (n+1) / 2 */
+int tpss_learned_sizes(const tpss_layout *layout, int *n_in, int *n_out);
+/* features of every patch of a distorted layout (P x n_in, device) */
+int tpss_learned_features(const tpss_layout *layout, float *x);
+/* training targets of every patch (P x n_out, device): the surrogate-basis correction that the
+ * Kronecker-sum fit of the exact patch matrix gives; needs the mapped level operator */
+int tpss_learned_targets(const tpss_layout *layout, const tpss_operator *op, double ip_factor,
+                         float *y);
+/* exact patch matrices of patches [first, first + count) (count x n_loc x n_loc, row-major,
+ * patch-local lexicographic DoFs, device FP64) from the mapped level operator */
+int tpss_local_matrices(const tpss_layout *layout, const tpss_operator *op, int64_t first,
+                        int64_t count, double *out);
+
 int tpss_diag_fma_peak(int precision, int iters, double *flops_per_second, void *stream);
 
 const char *tpss_last_error(void);

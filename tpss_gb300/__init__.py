@@ -179,6 +179,11 @@ class SubdomainHandler:
     def n_subdomains(self) -> int:
         return self._n_patches
 
+    def n_dofs_per_patch(self) -> int:
+        ad = self.additional_data
+        ncp = 2 if ad.patch_variant == PatchVariant.vertex else 1
+        return (ncp * (ad.degree + 1)) ** ad.dim
+
     def n_colors(self) -> int:
         return self._n_colors
 
@@ -245,6 +250,8 @@ class SchwarzPreconditioner:
         check_finite: bool = False
         kernel_variant: int = 0  # 0 auto, 1 one launch per color, 2 column-streamed (3D, FP32)
         stream_variant: int = 0  # work decomposition of the column-streamed kernel (0..3)
+        local_solver: int = 0    # LocalSolver.fd / exact / ksum / learned
+        model: "MLP" = None      # trained network for LocalSolver.learned
 
     def __init__(self):
         self._h = None
@@ -263,6 +270,8 @@ class SchwarzPreconditioner:
         d.check_finite = int(ad.check_finite)
         d.kernel_variant = int(ad.kernel_variant)
         d.stream_variant = int(ad.stream_variant)
+        d.local_solver = int(ad.local_solver)
+        d.model = ad.model.handle if ad.model is not None else None
         return d
 
     def initialize(self, subdomain_handler, linear_operator=None, additional_data=None):
@@ -391,15 +400,133 @@ class SchwarzSmoother:
             pass
 
 
+class LocalSolver:
+    """How the patch inverses are formed (tpss_precond_desc.local_solver)."""
+    fd = 0       # fast diagonalization of the layout's (Cartesian or surrogate) 1-D problems
+    exact = 1    # dense inverse of the exact patch matrix (basic state + InverseTable)
+    ksum = 2     # FD of the Kronecker sum fitted to the exact patch matrix
+    learned = 3  # surrogate 1-D problems corrected by a trained MLP
+
+
+class MLP:
+    """Fully connected tanh network trained on the GPU by the library's own kernels."""
+
+    def __init__(self, n_in, n_out, n_hidden=64, n_hidden_layers=3, seed=0):
+        d = _lib.MlpDesc()
+        d.n_in, d.n_out, d.n_hidden, d.n_hidden_layers, d.seed = n_in, n_out, n_hidden, n_hidden_layers, seed
+        h = C.c_void_p()
+        check(load().tpss_mlp_create(C.byref(d), C.byref(h)))
+        self._h = h
+        self.n_in, self.n_out = n_in, n_out
+        n = C.c_int64()
+        check(load().tpss_mlp_n_params(h, C.byref(n)))
+        self.n_params = n.value
+
+    @property
+    def handle(self):
+        return self._h
+
+    def get_params(self):
+        p = np.zeros(self.n_params, dtype=np.float32)
+        check(load().tpss_mlp_get_params(self._h, p.ctypes.data_as(C.POINTER(C.c_float))))
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        assert p.size == self.n_params
+        check(load().tpss_mlp_set_params(self._h, p.ctypes.data_as(C.POINTER(C.c_float))))
+
+    def forward(self, x, stream=None):
+        import torch
+        assert x.dtype == torch.float32 and x.is_cuda and x.shape[1] == self.n_in
+        y = torch.empty((x.shape[0], self.n_out), dtype=torch.float32, device=x.device)
+        check(load().tpss_mlp_forward(self._h, C.c_void_p(x.data_ptr()), x.shape[0],
+                                      C.c_void_p(y.data_ptr()), _stream(stream)))
+        return y
+
+    def loss_grad(self, x, target):
+        loss = C.c_double()
+        g = np.zeros(self.n_params, dtype=np.float32)
+        check(load().tpss_mlp_loss_grad(self._h, C.c_void_p(x.data_ptr()), C.c_void_p(target.data_ptr()),
+                                        x.shape[0], C.byref(loss), g.ctypes.data_as(C.POINTER(C.c_float))))
+        return loss.value, g
+
+    def loss(self, x, target):
+        loss = C.c_double()
+        check(load().tpss_mlp_eval_loss(self._h, C.c_void_p(x.data_ptr()), C.c_void_p(target.data_ptr()),
+                                        x.shape[0], C.byref(loss)))
+        return loss.value
+
+    def train(self, x, target, epochs, batch=256, lr=1e-3, seed=0, stream=None):
+        """Adam on shuffled mini-batches; returns the full-set loss after every epoch."""
+        hist = np.zeros(max(epochs, 1))
+        check(load().tpss_mlp_train(self._h, C.c_void_p(x.data_ptr()), C.c_void_p(target.data_ptr()),
+                                    x.shape[0], int(epochs), int(batch), float(lr), int(seed),
+                                    hist.ctypes.data_as(C.POINTER(C.c_double)), _stream(stream)))
+        return hist[:epochs]
+
+    def __del__(self):
+        try:
+            if self._h:
+                load().tpss_mlp_destroy(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+
+def learned_sizes(subdomain_handler):
+    a, b = C.c_int(), C.c_int()
+    check(load().tpss_learned_sizes(subdomain_handler.handle, C.byref(a), C.byref(b)))
+    return a.value, b.value
+
+
+def learned_features(subdomain_handler, device="cuda"):
+    """Network inputs of every patch of a distorted layout, [P, n_in] float32 on the device."""
+    import torch
+    n_in, _ = learned_sizes(subdomain_handler)
+    x = torch.empty((subdomain_handler.n_subdomains(), n_in), dtype=torch.float32, device=device)
+    check(load().tpss_learned_features(subdomain_handler.handle, C.c_void_p(x.data_ptr())))
+    return x
+
+
+def learned_targets(subdomain_handler, operator, ip_factor=1.0, device="cuda"):
+    """Training targets of every patch, [P, n_out] float32 on the device."""
+    import torch
+    _, n_out = learned_sizes(subdomain_handler)
+    y = torch.empty((subdomain_handler.n_subdomains(), n_out), dtype=torch.float32, device=device)
+    check(load().tpss_learned_targets(subdomain_handler.handle, operator.handle, float(ip_factor),
+                                      C.c_void_p(y.data_ptr())))
+    return y
+
+
+def local_matrices(subdomain_handler, operator, first, count, device="cuda"):
+    """Exact patch matrices [count, n_loc, n_loc] (FP64) of patches first..first+count-1."""
+    import torch
+    n_loc = subdomain_handler.n_dofs_per_patch()
+    out = torch.empty((count, n_loc, n_loc), dtype=torch.float64, device=device)
+    check(load().tpss_local_matrices(subdomain_handler.handle, operator.handle, int(first), int(count),
+                                     C.c_void_p(out.data_ptr())))
+    return out
+
+
 class MultigridSolver:
     """CG preconditioned by one GMG V-cycle with Schwarz smoothers on the unit cube."""
 
     def __init__(self, dim, degree, n_rep, n_cells_fine, patch_variant=PatchVariant.vertex,
                  smoother_variant=SmootherVariant.additive, relaxation=None, ip_factor=1.0,
-                 precision=Precision.fp64, coarse_tol=1e-12, coarse_solver=0, use_graph=True):
+                 precision=Precision.fp64, coarse_tol=1e-12, coarse_solver=0, use_graph=True,
+                 vertex_coords=None, surrogate_n_q=5, local_solver=0, model=None):
         if relaxation is None:
             relaxation = lookup_damping_factor(patch_variant, smoother_variant, dim)
         d = _lib.MgDesc()
+        if vertex_coords is not None:
+            self._coords = np.ascontiguousarray(vertex_coords, dtype=np.float64)
+            assert self._coords.shape == ((n_cells_fine + 1) ** dim, dim), "vertex_coords shape"
+            d.vertex_coords = self._coords.ctypes.data_as(C.POINTER(C.c_double))
+            d.surrogate_n_q = int(surrogate_n_q)
+        d.local_solver = int(local_solver)
+        d.model = model.handle if model is not None else None
+        self._model = model
         d.dim, d.degree, d.n_rep, d.n_cells_fine = dim, degree, n_rep, n_cells_fine
         d.ip_factor, d.patch_variant, d.smoother_variant = float(ip_factor), patch_variant, smoother_variant
         d.relaxation, d.precision, d.coarse_tol = float(relaxation), precision, float(coarse_tol)

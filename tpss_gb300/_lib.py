@@ -58,14 +58,21 @@ class LayoutDesc(C.Structure):
                 ("patch_variant", C.c_int), ("smoother_variant", C.c_int),
                 ("n_cells", C.c_int * 3), ("cell_h", C.POINTER(C.c_double) * 3),
                 ("cell_dof_start", C.POINTER(C.c_int64)), ("patch_color", C.POINTER(C.c_int32)),
-                ("vertex_coords", C.POINTER(C.c_double)), ("surrogate_n_q", C.c_int)]
+                ("vertex_coords", C.POINTER(C.c_double)), ("surrogate_n_q", C.c_int),
+                ("local_solver", C.c_int), ("model", C.c_void_p)]
 
 
 class PrecondDesc(C.Structure):
     _fields_ = [("relaxation", C.c_double), ("reverse", C.c_int), ("symmetrized", C.c_int),
                 ("use_ras_weights", C.c_int), ("use_ras_boolean_weights", C.c_int),
                 ("precision", C.c_int), ("ip_factor", C.c_double), ("check_finite", C.c_int),
-                ("kernel_variant", C.c_int), ("stream_variant", C.c_int)]
+                ("kernel_variant", C.c_int), ("stream_variant", C.c_int),
+                ("local_solver", C.c_int), ("model", C.c_void_p)]
+
+
+class MlpDesc(C.Structure):
+    _fields_ = [("n_in", C.c_int), ("n_hidden", C.c_int), ("n_hidden_layers", C.c_int),
+                ("n_out", C.c_int), ("seed", C.c_uint64)]
 
 
 class TimeInfo(C.Structure):
@@ -77,11 +84,14 @@ class MgDesc(C.Structure):
                 ("n_cells_fine", C.c_int), ("ip_factor", C.c_double),
                 ("patch_variant", C.c_int), ("smoother_variant", C.c_int),
                 ("relaxation", C.c_double), ("precision", C.c_int), ("coarse_tol", C.c_double),
-                ("coarse_solver", C.c_int), ("use_graph", C.c_int)]
+                ("coarse_solver", C.c_int), ("use_graph", C.c_int),
+                ("vertex_coords", C.POINTER(C.c_double)), ("surrogate_n_q", C.c_int),
+                ("local_solver", C.c_int), ("model", C.c_void_p)]
 
 
 _vp = C.c_void_p
 _dp = C.POINTER(C.c_double)
+_fp = C.POINTER(C.c_float)
 
 # symbol -> (restype, argtypes); every symbol declared in include/tpss_gpu.h
 SIGNATURES = {
@@ -117,6 +127,21 @@ SIGNATURES = {
     "tpss_transfer_prolongate_add": (C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_int), _vp, _vp, _vp]),
     "tpss_transfer_restrict_add": (C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_int), _vp, _vp, _vp]),
     "tpss_diag_fma_peak": (C.c_int, [C.c_int, C.c_int, _dp, _vp]),
+    "tpss_mlp_create": (C.c_int, [C.POINTER(MlpDesc), C.POINTER(_vp)]),
+    "tpss_mlp_sizes": (C.c_int, [_vp, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "tpss_mlp_n_params": (C.c_int, [_vp, C.POINTER(C.c_int64)]),
+    "tpss_mlp_get_params": (C.c_int, [_vp, _fp]),
+    "tpss_mlp_set_params": (C.c_int, [_vp, _fp]),
+    "tpss_mlp_forward": (C.c_int, [_vp, _vp, C.c_int64, _vp, _vp]),
+    "tpss_mlp_loss_grad": (C.c_int, [_vp, _vp, _vp, C.c_int64, _dp, _fp]),
+    "tpss_mlp_eval_loss": (C.c_int, [_vp, _vp, _vp, C.c_int64, _dp]),
+    "tpss_mlp_train": (C.c_int, [_vp, _vp, _vp, C.c_int64, C.c_int, C.c_int, C.c_double, C.c_uint64,
+                                 _dp, _vp]),
+    "tpss_mlp_destroy": (None, [_vp]),
+    "tpss_learned_sizes": (C.c_int, [_vp, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "tpss_learned_features": (C.c_int, [_vp, _vp]),
+    "tpss_learned_targets": (C.c_int, [_vp, _vp, C.c_double, _vp]),
+    "tpss_local_matrices": (C.c_int, [_vp, _vp, C.c_int64, C.c_int64, _vp]),
     "tpss_last_error": (C.c_char_p, []),
     "tpss_version": (C.c_char_p, []),
 }

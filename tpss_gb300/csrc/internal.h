@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <functional>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -187,8 +188,22 @@ struct tpss_layout
   tpss::DeviceBuffer<int64_t> d_cell_start;   // n_cells (empty when lexicographic)
   std::vector<int32_t> vertex_fd[3];           // vertex patches: FD entry of vertex v_d, per d
   bool per_patch_fd = false;                   // FD keys differ per patch (surrogate widths)
+  std::vector<double> coords;                  // vertex coordinates of a distorted level (host)
   tpss::DeviceBuffer<int32_t> d_vertex_fd[3];
 };
+
+namespace tpss
+{
+// block-sparse SIPG matrix of a multilinear (distorted) level (mapped.cu)
+struct MappedOperator
+{
+  int nd = 0, nb = 0;     // cell DoFs, blocks per block row (2 dim + 1)
+  int64_t n_cells = 0;
+  DeviceBuffer<double> coords;  // vertex coordinates
+  DeviceBuffer<double> vals;    // n_cells * nb blocks of nd x nd, entry (i, j) at j * nd + i
+  DeviceBuffer<int32_t> col;    // n_cells * nb column cell (lexicographic), -1 = none
+};
+}  // namespace tpss
 
 struct tpss_operator
 {
@@ -197,6 +212,7 @@ struct tpss_operator
   tpss::DeviceBuffer<double> d_mass[3], d_blk[3];
   tpss::DeviceBuffer<double> d_fac[3];  // operator_factors_1d per direction
   int nblk_cells[3] = {0, 0, 0};
+  std::unique_ptr<tpss::MappedOperator> mapped;  // set on distorted levels
 };
 
 namespace tpss
@@ -218,6 +234,13 @@ struct FdTables
   int hpad32 = 0;
   DeviceBuffer<float> fd32_eo;
   DeviceBuffer<int32_t> sym;
+  // per-patch entries (entry p * dim + d) instead of the layout's shared keys
+  DeviceBuffer<int32_t> own_fd;
+  // exact local inverses (local solver TPSS_LOCAL_EXACT): P x nloc x nloc, transposed
+  DeviceBuffer<double> dense64;
+  DeviceBuffer<float> dense32;
+  bool dense = false;
+  int64_t learned_fallbacks = 0;  // learned solver: patch directions kept at the surrogate
 };
 
 struct TimerSlot
@@ -266,6 +289,37 @@ struct FdLaunch
 };
 bool launch_fd_f32(int dim, int k, int ncp, const FdLaunch &a, cudaStream_t s);
 bool launch_fd_f64(int dim, int k, int ncp, const FdLaunch &a, cudaStream_t s);
+
+// mapped (distorted) levels (mapped.cu)
+size_t mapped_smem_bytes(int dim, int np);
+void mapped_build(tpss_operator &op, const tpss_layout &L, double ip);
+void mapped_apply(const tpss_operator &op, double *dst, const double *src, cudaStream_t s);
+std::vector<double> mapped_dense(const tpss_operator &op);
+// FD setup helpers (precond.cu, eigen.cu)
+void gen_eig_batched(int n, int n_problems, const std::vector<double> &Ms,
+                     const std::vector<double> &As, std::vector<double> &S,
+                     std::vector<double> &lam);
+void key_matrices(const tpss_layout &L, double ip, std::vector<double> &Ms, std::vector<double> &As);
+std::vector<double> per_patch(const tpss_layout &L, const std::vector<double> &keyed);
+
+// learned local solver (learned.cu, mlp.cu)
+using TableMaker = std::function<std::shared_ptr<FdTables>(const std::vector<double> *,
+                                                           const std::vector<double> *)>;
+std::shared_ptr<FdTables> build_learned_tables(const tpss_layout &L, const tpss_precond_desc &d,
+                                               const TableMaker &make);
+void mlp_infer(const tpss_mlp &m, const float *x_dev, int64_t rows, float *y_dev, cudaStream_t s);
+int mlp_n_in(const tpss_mlp &m);
+int mlp_n_out(const tpss_mlp &m);
+
+// local solvers from exact patch matrices (local.cu)
+void check_exact_local(const tpss_layout &L, const tpss_operator *op);
+void build_dense_inverses(const tpss_layout &L, const tpss_operator &op, bool fp32,
+                          DeviceBuffer<double> &inv64, DeviceBuffer<float> &inv32);
+void dense_apply_color(const tpss_layout &L, const void *inv, bool fp32, int color, double omega,
+                       double *dst, const double *src, cudaStream_t s);
+std::vector<double> ksum_fit(const tpss_layout &L, const tpss_operator &op, const std::vector<double> &Ms);
+void extract_local_matrices(const tpss_layout &L, const tpss_operator &op, int64_t p0, int64_t count,
+                            double *out_dev);
 
 // operator and transfer (operator.cu)
 void operator_apply(tpss_operator *op, double *dst, const double *src, cudaStream_t s);

@@ -258,6 +258,9 @@ void build_layout(tpss_layout &L, const tpss_layout_desc &d)
     TPSS_REQUIRE(d.surrogate_n_q == 0 || (d.surrogate_n_q >= 2 && d.surrogate_n_q <= 16),
                  "surrogate_n_q must be in 2..16");
     L.per_patch_fd = true;
+    const size_t nv = (size_t)(L.nc[0] + 1) * (dim > 1 ? L.nc[1] + 1 : 1) * (dim > 2 ? L.nc[2] + 1 : 1);
+    L.coords.assign(d.vertex_coords, d.vertex_coords + nv * dim);
+    for(double x : L.coords) TPSS_REQUIRE(std::isfinite(x), "vertex_coords must be finite");
   }
   std::vector<double> gl_z, gl_w;
   if(d.vertex_coords) lobatto_rule(d.surrogate_n_q ? d.surrogate_n_q : 5, gl_z, gl_w);

@@ -63,9 +63,9 @@ int grid_for(int64_t n)
   return (int)(b < cap ? (b > 0 ? b : 1) : cap);
 }
 
-// Dense SIPG matrix of a small structured level (Kronecker sum of the global 1-D operators)
-// and its inverse by Cholesky, both FP64 on the host.
-std::vector<double> dense_inverse(const tpss_layout &L, double ip)
+// Dense SIPG matrix of a small Cartesian level (Kronecker sum of the global 1-D operators),
+// FP64 on the host.
+std::vector<double> dense_matrix(const tpss_layout &L, double ip)
 {
   const Shape1D s = make_shape_1d(L.k);
   const int np = L.np, dim = L.dim;
@@ -133,7 +133,12 @@ std::vector<double> dense_inverse(const tpss_layout &L, double ip)
               if(v != 0.0) A[(size_t)row * N + gidx(pc)] = v;
             }
       }
-  // Cholesky A = G G^T (lower), then A^-1 = G^-T G^-1
+  return A;
+}
+
+// inverse of an SPD matrix by Cholesky A = G G^T (lower), A^-1 = G^-T G^-1, FP64 on the host
+std::vector<double> cholesky_inverse(const std::vector<double> &A, int64_t N)
+{
   std::vector<double> G(A);
   for(int64_t j = 0; j < N; ++j)
   {
@@ -381,10 +386,29 @@ extern "C" int tpss_mg_create(const tpss_mg_desc *d, tpss_mg **out)
     auto mg = std::make_unique<tpss_mg>();
     mg->desc = *d;
     mg->lv.resize(nl);
+    std::vector<double> coords;
     for(int l = 0; l < nl; ++l)
     {
       MgLevel &lv = mg->lv[l];
       tpss_layout_desc ld{};
+      if(d->vertex_coords)
+      {
+        // distorted hierarchy: a coarse level keeps every 2^(L-l)-th vertex of the finest
+        const int nf = d->n_cells_fine, nv = nf + 1, stride = 1 << (nl - 1 - l);
+        const int ncl = d->n_rep << l, nvl = ncl + 1;
+        const int nz = d->dim > 2 ? nvl : 1;
+        coords.assign((size_t)nvl * nvl * nz * d->dim, 0.0);
+        for(int z = 0; z < nz; ++z)
+          for(int y = 0; y < nvl; ++y)
+            for(int x = 0; x < nvl; ++x)
+            {
+              const int64_t src = x * stride + (int64_t)nv * (y * stride + (int64_t)nv * z * stride);
+              const int64_t dst = x + (int64_t)nvl * (y + (int64_t)nvl * z);
+              for(int e = 0; e < d->dim; ++e) coords[dst * d->dim + e] = d->vertex_coords[src * d->dim + e];
+            }
+        ld.vertex_coords = coords.data();
+        ld.surrogate_n_q = d->surrogate_n_q;
+      }
       ld.dim = d->dim;
       ld.degree = d->degree;
       ld.dof_layout = TPSS_DOF_DGQ;
@@ -401,6 +425,8 @@ extern "C" int tpss_mg_create(const tpss_mg_desc *d, tpss_mg **out)
         pd.relaxation = d->relaxation;
         pd.precision = d->precision;
         pd.ip_factor = d->ip_factor;
+        pd.local_solver = d->local_solver;
+        pd.model = d->model;
         rc = tpss_precond_create(lv.L, lv.op, &pd, &lv.P);
         if(rc) fail(rc, tpss_last_error());
       }
@@ -414,7 +440,9 @@ extern "C" int tpss_mg_create(const tpss_mg_desc *d, tpss_mg **out)
     if(d->coarse_solver == 1)
     {
       TPSS_REQUIRE(n0 <= 4096, "dense coarse solver limited to 4096 coarse DoFs");
-      std::vector<double> inv = dense_inverse(*mg->lv[0].L, d->ip_factor);
+      const tpss_operator &cop = *mg->lv[0].op;
+      std::vector<double> inv = cholesky_inverse(
+        cop.mapped ? mapped_dense(cop) : dense_matrix(*mg->lv[0].L, d->ip_factor), n0);
       mg->coarse_inv.upload(inv.data(), inv.size());
     }
     mg->cp.resize(n0);

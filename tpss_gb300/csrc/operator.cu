@@ -398,6 +398,11 @@ void operator_apply(tpss_operator *op, double *dst, const double *src, cudaStrea
 {
   const tpss_layout &L = *op->layout;
   TPSS_REQUIRE(dst && src && dst != src, "operator: invalid vectors");
+  if(op->mapped)
+  {
+    mapped_apply(*op, dst, src, s);
+    return;
+  }
   OpArgs a;
   a.src = src;
   a.dst = dst;
@@ -459,12 +464,17 @@ extern "C" int tpss_operator_create(const tpss_layout *layout, double ip_factor,
     TPSS_REQUIRE(layout && out, "null argument");
     TPSS_REQUIRE(ip_factor > 0.0, "ip_factor must be positive");
     *out = nullptr;
-    if(layout->per_patch_fd)
-      fail(TPSS_ERR_NOT_IMPLEMENTED, "the SIPG operator is implemented for Cartesian (tensor-product) levels");
     layout_to_device(*layout);
     auto op = std::make_unique<tpss_operator>();
     op->layout = layout;
     op->ip = ip_factor;
+    if(!layout->coords.empty())
+    {
+      // distorted level: block-sparse matrix assembled by quadrature on the mapped cells
+      mapped_build(*op, *layout, ip_factor);
+      *out = op.release();
+      return;
+    }
     const Shape1D s = make_shape_1d(layout->k);
     for(int d = 0; d < layout->dim; ++d)
     {

@@ -34,11 +34,11 @@ int pad_to(int n, int w) { return (n + w - 1) / w * w; }
 // which lets the kernels contract with two h x h matrices (h = n/2) instead of one n x n.
 // The resulting inverse is the same operator; only the rounding differs.
 void build_even_odd(const tpss_layout &L, FdTables &T, const std::vector<double> &Ms,
-                    const std::vector<double> &As)
+                    const std::vector<double> &As, bool keyed)
 {
   const int n = L.n, nn = n * n;
   std::vector<int32_t> sym(T.n_entries, 0);
-  if(L.ncp == 2 && n % 2 == 0)
+  if(keyed && L.ncp == 2 && n % 2 == 0)
     for(int e = 0; e < T.n_entries; ++e)
     {
       const auto &k = L.fd_keys[e];
@@ -99,24 +99,66 @@ void build_even_odd(const tpss_layout &L, FdTables &T, const std::vector<double>
   T.sym.upload(sym.data(), sym.size());
 }
 
-std::shared_ptr<FdTables> build_tables(const tpss_layout &L, double ip, bool ras)
+}  // namespace
+
+// 1-D patch matrices (mass, SIPG Laplace) of every FD key of the layout
+void key_matrices(const tpss_layout &L, double ip, std::vector<double> &Ms, std::vector<double> &As)
 {
-  auto t0 = std::chrono::steady_clock::now();
-  auto T = std::make_shared<FdTables>();
-  T->layout = &L;
-  T->n = L.n;
-  T->n_entries = (int)L.fd_keys.size();
-  T->npad32 = pad_to(L.n, 4);
-  T->npad64 = pad_to(L.n, 2);
-  const int n = L.n, nn = n * n;
+  const int n = L.n, nn = n * n, ne = (int)L.fd_keys.size();
   const Shape1D shape = make_shape_1d(L.k);
-  std::vector<double> Ms((size_t)T->n_entries * nn), As((size_t)T->n_entries * nn);
-  for(int e = 0; e < T->n_entries; ++e)
+  Ms.assign((size_t)ne * nn, 0.0);
+  As.assign((size_t)ne * nn, 0.0);
+  for(int e = 0; e < ne; ++e)
   {
     const auto &key = L.fd_keys[e];
     const double h[2] = {key.h0, key.h1};
     patch_matrices_1d(shape, L.ncp, h, key.lo != 0, key.hi != 0, ip, &Ms[(size_t)e * nn],
                       &As[(size_t)e * nn]);
+  }
+}
+
+// per patch and direction (entry p * dim + d): the 1-D matrices of the patch's FD key
+std::vector<double> per_patch(const tpss_layout &L, const std::vector<double> &keyed)
+{
+  const size_t nn = (size_t)L.n * L.n;
+  std::vector<double> out((size_t)L.P * L.dim * nn);
+  for(int64_t i = 0; i < L.P * L.dim; ++i)
+    std::copy_n(&keyed[(size_t)L.patch_fd_key[i] * nn], nn, &out[(size_t)i * nn]);
+  return out;
+}
+
+namespace
+{
+
+// FD tables of the layout's keys, or (patchM, patchA given) of one 1-D problem per patch and
+// direction
+std::shared_ptr<FdTables> build_tables(const tpss_layout &L, double ip, bool ras,
+                                       const std::vector<double> *patchM = nullptr,
+                                       const std::vector<double> *patchA = nullptr)
+{
+  auto t0 = std::chrono::steady_clock::now();
+  auto T = std::make_shared<FdTables>();
+  T->layout = &L;
+  T->n = L.n;
+  T->npad32 = pad_to(L.n, 4);
+  T->npad64 = pad_to(L.n, 2);
+  const int n = L.n, nn = n * n;
+  std::vector<double> Ms, As;
+  const bool keyed = patchM == nullptr;
+  if(keyed)
+  {
+    key_matrices(L, ip, Ms, As);
+    T->n_entries = (int)L.fd_keys.size();
+  }
+  else
+  {
+    TPSS_REQUIRE(L.P * L.dim < (int64_t)INT32_MAX, "too many patches");
+    Ms = *patchM;
+    As = *patchA;
+    T->n_entries = (int)(L.P * L.dim);
+    std::vector<int32_t> map((size_t)L.P * L.dim);
+    for(size_t i = 0; i < map.size(); ++i) map[i] = (int32_t)i;
+    T->own_fd.upload(map.data(), map.size());
   }
   gen_eig_batched(n, T->n_entries, Ms, As, T->S_host, T->lam_host);
   // kernel tables: [S^T n x npad][S n x npad][lambda npad]
@@ -143,7 +185,7 @@ std::shared_ptr<FdTables> build_tables(const tpss_layout &L, double ip, bool ras
   fill((float *)nullptr, T->npad32, t32);
   T->fd64.upload(t64.data(), t64.size());
   T->fd32.upload(t32.data(), t32.size());
-  build_even_odd(L, *T, Ms, As);
+  build_even_odd(L, *T, Ms, As, keyed);
   if(ras)
   {
     // RAS weights: 1 / (number of patches sharing the cell), the gathered "appearances" of
@@ -162,6 +204,46 @@ std::shared_ptr<FdTables> build_tables(const tpss_layout &L, double ip, bool ras
   return T;
 }
 
+// local solvers of a preconditioner according to desc.local_solver
+std::shared_ptr<FdTables> build_local_solvers(const tpss_layout &L, const tpss_operator *op,
+                                              const tpss_precond_desc &d)
+{
+  const bool ras = d.use_ras_weights != 0;
+  switch(d.local_solver)
+  {
+  case TPSS_LOCAL_EXACT:
+  {
+    check_exact_local(L, op);
+    auto t0 = std::chrono::steady_clock::now();
+    auto T = std::make_shared<FdTables>();
+    T->layout = &L;
+    T->n = L.n;
+    T->dense = true;
+    build_dense_inverses(L, *op, d.precision == TPSS_FP32, T->dense64, T->dense32);
+    T->setup_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    return T;
+  }
+  case TPSS_LOCAL_KSUM:
+  {
+    check_exact_local(L, op);
+    auto t0 = std::chrono::steady_clock::now();
+    std::vector<double> Mk, Ak;
+    key_matrices(L, d.ip_factor, Mk, Ak);
+    const std::vector<double> Mp = per_patch(L, Mk);
+    const std::vector<double> Ap = ksum_fit(L, *op, Mp);
+    auto T = build_tables(L, d.ip_factor, ras, &Mp, &Ap);
+    T->setup_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    return T;
+  }
+  case TPSS_LOCAL_LEARNED:
+    return build_learned_tables(L, d, [&](const std::vector<double> *Mp, const std::vector<double> *Ap) {
+      return build_tables(L, d.ip_factor, ras, Mp, Ap);
+    });
+  default:
+    return build_tables(L, d.ip_factor, ras);
+  }
+}
+
 void validate_desc(const tpss_precond_desc &d)
 {
   TPSS_REQUIRE(d.kernel_variant >= TPSS_KERNEL_AUTO && d.kernel_variant <= TPSS_KERNEL_STREAM,
@@ -169,6 +251,12 @@ void validate_desc(const tpss_precond_desc &d)
   TPSS_REQUIRE(d.stream_variant >= 0 && d.stream_variant <= 3, "stream_variant must be in 0..3");
   TPSS_REQUIRE(d.relaxation > 0.0, "Invalid relaxation factor.");
   TPSS_REQUIRE(d.precision == TPSS_FP64 || d.precision == TPSS_FP32, "invalid precision");
+  TPSS_REQUIRE(d.local_solver >= TPSS_LOCAL_FD && d.local_solver <= TPSS_LOCAL_LEARNED,
+               "invalid local solver");
+  if(d.local_solver == TPSS_LOCAL_EXACT && d.use_ras_weights)
+    fail(TPSS_ERR_NOT_IMPLEMENTED, "RAS weights are implemented for the FD local solvers");
+  if(d.local_solver == TPSS_LOCAL_LEARNED)
+    TPSS_REQUIRE(d.model != nullptr, "the learned local solver needs a trained model");
   if(d.use_ras_weights && d.use_ras_boolean_weights)
     fail(TPSS_ERR_INVALID_ARGUMENT, "It isn't possible to use more than one RAS option.");
   if(d.use_ras_boolean_weights)
@@ -272,11 +360,18 @@ void apply_color(tpss_precond *p, int color, double *dst, const double *src, cud
   const tpss_layout &L = *p->tables->layout;
   const int64_t b = L.color_start[color], e = L.color_start[color + 1];
   if(e <= b) return;
+  if(p->tables->dense)
+  {
+    const bool f32 = p->desc.precision == TPSS_FP32;
+    dense_apply_color(L, f32 ? (const void *)p->tables->dense32.ptr : (const void *)p->tables->dense64.ptr,
+                      f32, color, p->desc.relaxation, dst, src, s);
+    return;
+  }
   FdLaunch a;
   a.src = src;
   a.dst = dst;
   a.patch_first = L.d_patch_first.ptr + b * L.npc;
-  a.patch_fd = L.d_patch_fd.ptr + b * L.dim;
+  a.patch_fd = (p->tables->own_fd.n ? p->tables->own_fd.ptr : L.d_patch_fd.ptr) + b * L.dim;
   const bool ras = p->desc.use_ras_weights && L.smoother_variant == TPSS_ADDITIVE;
   a.ras_w = ras ? p->tables->ras_w.ptr + b * L.npc : nullptr;
   a.n_patches = e - b;
@@ -322,7 +417,7 @@ bool use_stream(const tpss_precond *p)
   const tpss_layout &L = *p->tables->layout;
   if(p->desc.kernel_variant == TPSS_KERNEL_COLOR) return false;
   const bool ok = L.smoother_variant == TPSS_ADDITIVE && p->desc.precision == TPSS_FP32 &&
-                  stream_supported(L);
+                  stream_supported(L) && !p->tables->dense && p->tables->own_fd.n == 0;
   if(p->desc.kernel_variant == TPSS_KERNEL_STREAM && !ok)
     fail(TPSS_ERR_INVALID_ARGUMENT, "the streamed kernel needs additive 3D vertex patches, FP32, k <= 4");
   return ok;
@@ -424,7 +519,7 @@ extern "C" int tpss_precond_create(const tpss_layout *layout, tpss_operator *op,
     p->desc = *desc;
     p->op = op;
     p->stream_variant = desc->stream_variant;
-    p->tables = build_tables(*layout, desc->ip_factor, desc->use_ras_weights != 0);
+    p->tables = build_local_solvers(*layout, op, *desc);
     p->timers.resize(5);
     for(int i = 0; i < 5; ++i) p->timers[i].name = kTimerNames[i];
     p->timers[2].time = p->tables->setup_seconds;
@@ -442,6 +537,11 @@ extern "C" int tpss_precond_create_shallow(const tpss_precond *other, const tpss
     validate_desc(*desc);
     TPSS_REQUIRE(desc->ip_factor == other->desc.ip_factor,
                  "shallow copies share the local solvers: ip_factor must match");
+    TPSS_REQUIRE(desc->local_solver == other->desc.local_solver && desc->model == other->desc.model,
+                 "shallow copies share the local solvers: local_solver must match");
+    if(other->tables->dense)
+      TPSS_REQUIRE(desc->precision == other->desc.precision,
+                   "shallow copies of dense local inverses keep the precision");
     auto p = std::make_unique<tpss_precond>();
     p->desc = *desc;
     p->op = other->op;
