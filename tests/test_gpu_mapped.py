@@ -64,17 +64,25 @@ def test_mapped_operator_on_cartesian_coords_equals_tensor_operator(tpss, mapped
     assert rel_err(a.cpu().numpy(), b.cpu().numpy()) <= 1e-12
 
 
-@pytest.mark.parametrize("dim,k,n_rep,ncf,seed", [(2, 2, 2, 16, 5), (2, 3, 2, 8, 6), (3, 1, 2, 8, 7)])
-def test_mg_cg_on_distorted_mesh(tpss, oracle, mapped, cuda, dim, k, n_rep, ncf, seed):
-    """CG + V-cycle on a distorted hierarchy: mapped operators on every level, surrogate-patch
-    FD smoothers, dense coarse solve; identical iterations to the numpy oracle."""
+# amplitude 0.15 for the surrogate smoother: at 0.25 its damped additive sweep is no longer a
+# contraction on some patches and CG iteration counts become sensitive to rounding
+@pytest.mark.parametrize("dim,k,n_rep,ncf,seed,amp,local", [
+    (2, 2, 2, 16, 5, 0.15, "surrogate"), (2, 3, 2, 8, 6, 0.15, "surrogate"),
+    (3, 1, 2, 8, 7, 0.15, "surrogate"), (2, 2, 2, 16, 5, 0.25, "ksum"),
+    (2, 2, 2, 16, 5, 0.25, "exact"), (3, 1, 2, 8, 7, 0.2, "ksum"), (3, 1, 2, 8, 7, 0.2, "exact")])
+def test_mg_cg_on_distorted_mesh(tpss, oracle, mapped, cuda, dim, k, n_rep, ncf, seed, amp, local):
+    """CG + V-cycle on a distorted hierarchy: mapped operators on every level, Schwarz
+    smoothers with surrogate / Kronecker-sum / exact local solvers, dense coarse solve;
+    identical iterations to the numpy oracle."""
     import torch
-    X = oracle.distorted_coords(dim, [ncf] * dim, seed, 0.25)
+    X = oracle.distorted_coords(dim, [ncf] * dim, seed, amp)
     N = ncf ** dim * (k + 1) ** dim
     f = philox(seed, N)
     om = oracle.lookup_damping_factor(1, 0, dim)
-    it_ref, hist_ref, u_ref = mapped.mg_cg_solve_mapped(dim, k, n_rep, ncf, X, f, om)
-    mg = tpss.MultigridSolver(dim, k, n_rep, ncf, relaxation=om, coarse_solver=1, vertex_coords=X)
+    it_ref, hist_ref, u_ref = mapped.mg_cg_solve_mapped(dim, k, n_rep, ncf, X, f, om, local=local)
+    ls = {"surrogate": tpss.LocalSolver.fd, "ksum": tpss.LocalSolver.ksum, "exact": tpss.LocalSolver.exact}[local]
+    mg = tpss.MultigridSolver(dim, k, n_rep, ncf, relaxation=om, coarse_solver=1, vertex_coords=X,
+                              local_solver=ls)
     u = torch.zeros(N, dtype=torch.float64, device=cuda)
     ft = torch.tensor(f, dtype=torch.float64, device=cuda)
     it, hist = mg.solve(u, ft)

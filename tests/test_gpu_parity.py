@@ -407,8 +407,6 @@ def test_surrogate_patches_on_distorted_mesh(tpss, oracle, cuda, dim, k, nc, pre
     p.vmult(d, s)
     ref = oracle.schwarz_vmult_surrogate(dim, k, nc, oracle.surrogate_h(dim, nc, X), src, omega=0.4)
     assert rel_err(d.cpu().numpy(), ref) <= (1e-12 if precision == 0 else 2e-5)
-    with pytest.raises(tpss.TPSSNotImplemented):
-        tpss.LaplaceOperator(sh, 1.0)
 
 
 @pytest.mark.parametrize("k,nc", [(4, (9, 6, 19)), (3, (7, 5, 13)), (2, (6, 6, 17)), (1, (5, 9, 18))])
