@@ -47,6 +47,8 @@ def parse():
     ap.add_argument("--precision", choices=["fp32", "fp64"], default="fp32")
     ap.add_argument("--omega", type=float, default=0.15)
     ap.add_argument("--no-solve", action="store_true")
+    ap.add_argument("--no-distorted", action="store_true")
+    ap.add_argument("--distortion", type=float, default=0.15)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--seed", type=int, default=0)
@@ -343,6 +345,8 @@ def run_ours(args):
     if not args.no_solve:
         out["operator"] = operator_time(tpss, sh, src, W)
         out["solve"] = solve_times(tpss, args)
+    if not args.no_distorted:
+        out["distorted"] = distorted_section(tpss, args)
     if rank == 0 and not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline(args, W)
     if rank == 0:
@@ -446,6 +450,68 @@ def solve_times(tpss, args):
     res["workload"] = (f"CG + V-cycle (1 pre/1 post additive vertex-patch Schwarz step, omega "
                        f"{args.omega}), 3D SIPG DGQ{k} {n}^3, f ~ U[-1,1], to 1e-8 rel. residual")
     return res
+
+
+def distorted_section(tpss, args):
+    """Distorted 3D DGQ3 32^3 level (interior vertices moved by `distortion` x the shortest
+    edge in random directions, as the reference's distort_random): train the learned local
+    solver's network on the patches of four other meshes, then solve CG + V-cycle to 1e-8 with
+    surrogate (FP64, FP32), Kronecker-sum-fitted (FP32) and learned (FP32) local solvers."""
+    import torch
+    from tpss_gb300.mesh import distorted_cube
+    dim, k, n, fac = 3, 3, 32, args.distortion
+    out = {"workload": f"3D SIPG DGQ{k} {n}^3 distorted mesh (vertices moved {fac} x shortest edge), "
+                       f"CG + V-cycle to 1e-8, additive vertex patches omega 0.15, dense coarse solve"}
+    t0 = time.perf_counter()
+    xs, ys = [], []
+    for seed in range(100, 104):
+        X = distorted_cube(dim, [n] * dim, seed, fac)
+        sh = tpss.SubdomainHandler(tpss.SubdomainHandler.AdditionalData(
+            dim=dim, degree=k, n_cells=(n,) * dim, patch_variant=tpss.PatchVariant.vertex, vertex_coords=X))
+        op = tpss.LaplaceOperator(sh)
+        xs.append(tpss.learned_features(sh))
+        ys.append(tpss.learned_targets(sh, op))
+        del op, sh
+    torch.cuda.synchronize()
+    x, y = torch.cat(xs), torch.cat(ys)
+    t1 = time.perf_counter()
+    m = tpss.MLP(x.shape[1], y.shape[1], n_hidden=64, n_hidden_layers=3, seed=1)
+    l0 = m.loss(x, y)
+    hist = m.train(x, y, epochs=40, batch=256, lr=1e-3, seed=2)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    out["training"] = {"patches": int(x.shape[0]), "inputs": int(x.shape[1]), "outputs": int(y.shape[1]),
+                       "network": "3 x 64 tanh, Adam lr 1e-3, batch 256, 40 epochs",
+                       "data_seconds": t1 - t0, "train_seconds": t2 - t1,
+                       "loss_initial": l0, "loss_final": float(hist[-1])}
+    X = distorted_cube(dim, [n] * dim, 7, fac)
+    N = n ** dim * (k + 1) ** dim
+    f = torch.tensor(philox_src(N, args.seed), dtype=torch.float64, device="cuda")
+    runs = (("surrogate_fp64", tpss.LocalSolver.fd, tpss.Precision.fp64, None),
+            ("surrogate_fp32", tpss.LocalSolver.fd, tpss.Precision.fp32, None),
+            ("ksum_fp32", tpss.LocalSolver.ksum, tpss.Precision.fp32, None),
+            ("learned_fp32", tpss.LocalSolver.learned, tpss.Precision.fp32, m))
+    for name, ls, prec, model in runs:
+        ts = time.perf_counter()
+        mg = tpss.MultigridSolver(dim, k, 2, n, relaxation=0.15, precision=prec, coarse_solver=1,
+                                  use_graph=True, vertex_coords=X, local_solver=ls, model=model)
+        torch.cuda.synchronize()
+        setup = time.perf_counter() - ts
+        u = torch.zeros_like(f)
+        mg.vmult(u, f)  # warm-up: graph capture
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        try:
+            it, h = mg.solve(u, f, rel_tol=1e-8, max_iter=300)
+            torch.cuda.synchronize()
+            out[name] = {"setup_seconds": setup, "seconds": time.perf_counter() - t0, "iterations": it}
+        except tpss.TPSSNotConverged:
+            out[name] = {"setup_seconds": setup, "iterations": "not converged in 300"}
+        del mg
+    a, b = out["learned_fp32"], out["surrogate_fp64"]
+    if "seconds" in a and "seconds" in b:
+        out["learned_fp32_over_surrogate_fp64_time"] = a["seconds"] / b["seconds"]
+    return out
 
 
 def main():

@@ -258,7 +258,8 @@ def mg_cg_solve_mapped(dim, k, n_rep, nc_fine, X, f, omega, rel_tol=1e-8, abs_to
                     inv[l].append((idx, np.linalg.inv(K)))
                 else:
                     Ms = [m for m, _ in MA]
-                    inv[l].append((idx, fd_inverse(Ms, ksum_fit_closed(K, Ms))))
+                    Af = keep_definite(Ms, ksum_fit_closed(K, Ms), [a for _, a in MA])
+                    inv[l].append((idx, fd_inverse(Ms, Af)))
 
     def smooth(l, r):
         if local == "surrogate":
@@ -441,3 +442,12 @@ def ksum_fit_closed(K, Ms):
         Ad = R / cd - (dim - 1) / dim * full / P * Ms[d]
         A.append((Ad + Ad.T) / 2)
     return A
+
+
+def keep_definite(Ms, A_new, A_sur):
+    """The fitted 1-D problems if the smallest eigenvalue of their Kronecker sum is at least
+    half of the surrogate's, else the surrogate problems (the product's fallback rule)."""
+    import scipy.linalg as sl
+    snew = sum(sl.eigh(A_new[d], Ms[d], eigvals_only=True).min() for d in range(len(Ms)))
+    ssur = sum(sl.eigh(A_sur[d], Ms[d], eigvals_only=True).min() for d in range(len(Ms)))
+    return A_new if (np.isfinite(snew) and snew >= 0.5 * ssur) else A_sur

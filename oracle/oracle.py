@@ -314,9 +314,27 @@ def ksvd_diag(d, big, small, rank):
     return B, A
 
 
-def distorted_coords(dim, nc, seed, amplitude=0.25):
+def distorted_coords(dim, nc, seed, amplitude=0.25, mode="cube"):
     """Vertex coordinates of the unit cube with nc cells per direction, every interior vertex
-    displaced by U[-amplitude h, amplitude h] per coordinate (numpy Philox, seed)."""
+    displaced (numpy Philox, seed).
+    mode "cube": by U[-amplitude h_d, amplitude h_d] in every coordinate d;
+    mode "edge": as the reference's mesh generator does it (GridTools::distort_random called
+    from apps/mesh.h:160-190): in a uniformly random direction, by amplitude times the
+    shortest edge at the vertex. Per-coordinate shifts of 0.25 h can invert cells (a 32^3
+    mesh with seed 7 has 8 cells with a negative corner Jacobian); shifts of at most 0.25 of
+    the shortest edge cannot."""
+    if mode == "edge":
+        nv = [n + 1 for n in nc]
+        grids = np.meshgrid(*[np.arange(n) / (n - 1) for n in reversed(nv)], indexing="ij")
+        X = np.stack([grids[dim - 1 - d] for d in range(dim)], axis=-1).reshape(-1, dim)
+        g = np.random.Generator(np.random.Philox(seed))
+        v = g.normal(size=X.shape)
+        v /= np.linalg.norm(v, axis=1, keepdims=True)
+        hmin = 1.0 / max(nc[:dim])
+        idx = np.indices(list(reversed(nv))).reshape(dim, -1)[::-1].T
+        interior = np.all((idx > 0) & (idx < np.array(nc)[None, :]), axis=1)
+        X[interior] += amplitude * hmin * v[interior]
+        return np.ascontiguousarray(X)
     nv = [n + 1 for n in nc]
     grids = np.meshgrid(*[np.arange(n) / (n - 1) for n in reversed(nv)], indexing="ij")
     X = np.stack([grids[dim - 1 - d] for d in range(dim)], axis=-1).reshape(-1, dim)

@@ -87,7 +87,7 @@ def test_ksum_local_solver_vs_numpy_fit(tpss, oracle, nd, xcheck, cuda, dim, k, 
     for lo, MA, _, _ in nd.patch_problems(dim, k, list(nc), X):
         idx = xcheck.patch_dofs(dim, k, list(nc), lo, 2)
         Ms = [m for m, _ in MA]
-        Af = nd.ksum_fit_closed(A[np.ix_(idx, idx)], Ms)
+        Af = nd.keep_definite(Ms, nd.ksum_fit_closed(A[np.ix_(idx, idx)], Ms), [a for _, a in MA])
         ref[idx] += 0.3 * (nd.fd_inverse(Ms, Af) @ src[idx])
     assert rel_err(got, ref) <= 1e-10
 

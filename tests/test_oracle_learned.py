@@ -94,3 +94,15 @@ def test_numpy_mlp_gradient_matches_finite_differences(mlp):
         e[i] = eps
         fd[i] = (mlp.loss_grad(p + e, widths, x, t)[0] - mlp.loss_grad(p - e, widths, x, t)[0]) / (2 * eps)
     assert np.abs(g - fd).max() <= 1e-7 * max(1.0, np.abs(fd).max())
+
+
+def test_product_mesh_generator_matches_oracle_and_keeps_cells_valid(nd, oracle):
+    from tpss_gb300.mesh import distorted_cube
+    X = distorted_cube(3, [6, 5, 7], 3, 0.25)
+    assert np.array_equal(X, oracle.distorted_coords(3, [6, 5, 7], 3, 0.25, mode="edge"))
+    nc = [6, 5, 7]
+    for c in [(i, j, l) for i in range(6) for j in range(5) for l in range(7)]:
+        V = nd.cell_vertices(X, 3, nc, list(c))
+        for corner in range(8):
+            xi = [(corner >> d) & 1 for d in range(3)]
+            assert np.linalg.det(nd.jacobian(V, xi)) > 0

@@ -240,7 +240,7 @@ struct FdTables
   DeviceBuffer<double> dense64;
   DeviceBuffer<float> dense32;
   bool dense = false;
-  int64_t learned_fallbacks = 0;  // learned solver: patch directions kept at the surrogate
+  int64_t learned_fallbacks = 0;  // fitted / learned solvers: patches kept at the surrogate
 };
 
 struct TimerSlot
@@ -301,6 +301,8 @@ void gen_eig_batched(int n, int n_problems, const std::vector<double> &Ms,
                      std::vector<double> &lam);
 void key_matrices(const tpss_layout &L, double ip, std::vector<double> &Ms, std::vector<double> &As);
 std::vector<double> per_patch(const tpss_layout &L, const std::vector<double> &keyed);
+int64_t keep_definite(const tpss_layout &L, const std::vector<double> &Mp, std::vector<double> &Ap,
+                      const std::vector<double> &Asur);
 
 // learned local solver (learned.cu, mlp.cu)
 using TableMaker = std::function<std::shared_ptr<FdTables>(const std::vector<double> *,

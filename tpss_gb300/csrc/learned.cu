@@ -8,8 +8,9 @@
 // whose targets come from the Kronecker sum fitted to the EXACT patch matrix with the same
 // masses (local.cu): A_d' = A_d^fit. At inference A_d' = A_d + D^1/2 T_d D^1/2 is
 // diagonalized with M_d like any FD entry, so the smoother kernels are unchanged. A patch
-// direction whose corrected A_d' is not positive definite keeps the surrogate problem (the
-// fallback).
+// direction whose corrected A_d' is not positive definite, or a patch whose corrected
+// Kronecker sum loses more than half of the surrogate's smallest eigenvalue, keeps the
+// surrogate problems (the fallback).
 //
 // Network input per vertex patch (3^d vertices): the displacement of every patch vertex from
 // the regular lattice around the patch's centre vertex, coordinate d in units of the patch's
@@ -105,6 +106,7 @@ std::shared_ptr<FdTables> build_learned_tables(const tpss_layout &L, const tpss_
   }
   std::vector<double> Mp, Ap;
   surrogate_problems(L, d.ip_factor, Mp, Ap);
+  const std::vector<double> Asur = Ap;
   std::vector<double> H(nn), W(nn);
   int64_t fallbacks = 0;
   for(int64_t p = 0; p < L.P; ++p)
@@ -148,6 +150,7 @@ std::shared_ptr<FdTables> build_learned_tables(const tpss_layout &L, const tpss_
       else
         ++fallbacks;
     }
+  fallbacks += keep_definite(L, Mp, Ap, Asur);
   auto T = make(&Mp, &Ap);
   T->learned_fallbacks = fallbacks;
   T->setup_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();

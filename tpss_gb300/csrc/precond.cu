@@ -127,9 +127,46 @@ std::vector<double> per_patch(const tpss_layout &L, const std::vector<double> &k
   return out;
 }
 
+// Replace, patch by patch, approximate 1-D problems whose Kronecker sum is not safely positive
+// definite: the smallest eigenvalue of the sum, sum_d min_i lambda_(d,i), must stay at least half
+// of the surrogate's, else the patch keeps the surrogate problems. Returns the patch count.
+int64_t keep_definite(const tpss_layout &L, const std::vector<double> &Mp, std::vector<double> &Ap,
+                      const std::vector<double> &Asur)
+{
+  const int n = L.n, nn = n * n, dim = L.dim;
+  const int ne = (int)(L.P * dim);
+  std::vector<double> S, lam, Ss, lams;
+  gen_eig_batched(n, ne, Mp, Ap, S, lam);
+  gen_eig_batched(n, ne, Mp, Asur, Ss, lams);
+  int64_t count = 0;
+  for(int64_t p = 0; p < L.P; ++p)
+  {
+    double snew = 0.0, ssur = 0.0;
+    bool finite = true;
+    for(int d = 0; d < dim; ++d)
+    {
+      const double *a = &lam[((size_t)p * dim + d) * n], *b = &lams[((size_t)p * dim + d) * n];
+      double ma = a[0], mb = b[0];
+      for(int i = 0; i < n; ++i)
+      {
+        finite = finite && std::isfinite(a[i]);
+        ma = std::min(ma, a[i]);
+        mb = std::min(mb, b[i]);
+      }
+      snew += ma;
+      ssur += mb;
+    }
+    if(!(finite && snew >= 0.5 * ssur))
+    {
+      ++count;
+      std::copy_n(&Asur[(size_t)p * dim * nn], (size_t)dim * nn, &Ap[(size_t)p * dim * nn]);
+    }
+  }
+  return count;
+}
+
 namespace
 {
-
 // FD tables of the layout's keys, or (patchM, patchA given) of one 1-D problem per patch and
 // direction
 std::shared_ptr<FdTables> build_tables(const tpss_layout &L, double ip, bool ras,
@@ -230,8 +267,10 @@ std::shared_ptr<FdTables> build_local_solvers(const tpss_layout &L, const tpss_o
     std::vector<double> Mk, Ak;
     key_matrices(L, d.ip_factor, Mk, Ak);
     const std::vector<double> Mp = per_patch(L, Mk);
-    const std::vector<double> Ap = ksum_fit(L, *op, Mp);
+    std::vector<double> Ap = ksum_fit(L, *op, Mp);
+    const int64_t kept = keep_definite(L, Mp, Ap, per_patch(L, Ak));
     auto T = build_tables(L, d.ip_factor, ras, &Mp, &Ap);
+    T->learned_fallbacks = kept;
     T->setup_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     return T;
   }
