@@ -461,7 +461,8 @@ def distorted_section(tpss, args):
     from tpss_gb300.mesh import distorted_cube
     dim, k, n, fac = 3, 3, 32, args.distortion
     out = {"workload": f"3D SIPG DGQ{k} {n}^3 distorted mesh (vertices moved {fac} x shortest edge), "
-                       f"CG + V-cycle to 1e-8, additive vertex patches omega 0.15, dense coarse solve"}
+                       f"CG + V-cycle to 1e-8, additive vertex patches, damping 0.15 scaled per level by "
+                       f"8 / (1.05 lambda_max(P A)), dense coarse solve"}
     t0 = time.perf_counter()
     xs, ys = [], []
     for seed in range(100, 104):
@@ -494,7 +495,8 @@ def distorted_section(tpss, args):
     for name, ls, prec, model in runs:
         ts = time.perf_counter()
         mg = tpss.MultigridSolver(dim, k, 2, n, relaxation=0.15, precision=prec, coarse_solver=1,
-                                  use_graph=True, vertex_coords=X, local_solver=ls, model=model)
+                                  use_graph=True, vertex_coords=X, local_solver=ls, model=model,
+                                  auto_relaxation=True)
         torch.cuda.synchronize()
         setup = time.perf_counter() - ts
         u = torch.zeros_like(f)
@@ -504,7 +506,8 @@ def distorted_section(tpss, args):
         try:
             it, h = mg.solve(u, f, rel_tol=1e-8, max_iter=300)
             torch.cuda.synchronize()
-            out[name] = {"setup_seconds": setup, "seconds": time.perf_counter() - t0, "iterations": it}
+            out[name] = {"setup_seconds": setup, "seconds": time.perf_counter() - t0, "iterations": it,
+                         "damping_per_level": [round(mg.relaxation(l)[0], 5) for l in range(1, mg.n_levels)]}
         except tpss.TPSSNotConverged:
             out[name] = {"setup_seconds": setup, "iterations": "not converged in 300"}
         del mg

@@ -255,6 +255,11 @@ typedef struct tpss_mg_desc
   int surrogate_n_q;           /* Gauss-Lobatto points of the surrogate arc lengths (0: 5) */
   int local_solver;            /* TPSS_LOCAL_* of the level smoothers (distorted levels) */
   const tpss_mlp *model;       /* trained network for TPSS_LOCAL_LEARNED */
+  int auto_relaxation;         /* 0: every level uses `relaxation` (the reference). 1: a level
+                                  whose smoother spectrum lambda_max(P A) exceeds the Cartesian
+                                  2^dim is damped by relaxation * 2^dim / (1.05 lambda_max),
+                                  lambda_max from 30 power steps at setup (no counterpart in
+                                  the reference) */
 } tpss_mg_desc;
 
 int tpss_mg_create(const tpss_mg_desc *desc, tpss_mg **out);
@@ -268,6 +273,9 @@ int tpss_mg_vmult(tpss_mg *mg, double *dst, const double *src, void *stream);
  * max_iter+1, may be NULL) the residual norms. */
 int tpss_mg_cg_solve(tpss_mg *mg, double *u, const double *f, double rel_tol, double abs_tol,
                      int max_iter, int *iterations, double *res_history, void *stream);
+/* Damping used by the smoother of level 1..L and, with auto_relaxation, the estimate of
+ * lambda_max(P A) it was scaled by (0 otherwise). No counterpart in the reference. */
+int tpss_mg_relaxation(const tpss_mg *mg, int level, double *relaxation, double *lambda_max);
 /* Level objects for direct use (level 0 = coarsest). */
 int tpss_mg_level(tpss_mg *mg, int level, tpss_layout **layout, tpss_operator **op,
                   tpss_precond **precond);

@@ -224,8 +224,37 @@ def level_coords(dim, nc_fine, X, levels_down):
     return X
 
 
+def lcg_start(n):
+    """The power iteration's start vector: 64-bit LCG (Knuth MMIX constants), seed 0x5eed,
+    top 53 bits as a uniform in [0,1), minus 0.5."""
+    out = np.zeros(n)
+    st = 0x5EED
+    M = (1 << 64) - 1
+    for i in range(n):
+        st = (st * 6364136223846793005 + 1442695040888963407) & M
+        out[i] = (st >> 11) * (1.0 / 9007199254740992.0) - 0.5
+    return out
+
+
+def scaled_relaxation(A, smooth1, omega, dim, steps=30):
+    """omega * 2^dim / (1.05 lambda) if smaller than omega, lambda = Rayleigh-quotient power
+    estimate of lambda_max(P A) (P = undamped smoother)."""
+    x = lcg_start(A.shape[0])
+    lam = 0.0
+    for _ in range(steps):
+        t = A @ x
+        r = smooth1(t)
+        xt, tr, rr = x @ t, t @ r, r @ r
+        if not (xt > 0 and rr > 0):
+            break
+        lam = tr / xt
+        x = r / np.sqrt(rr)
+    w = min(omega, omega * 2 ** dim / (1.05 * lam)) if lam > 0 else omega
+    return w, lam
+
+
 def mg_cg_solve_mapped(dim, k, n_rep, nc_fine, X, f, omega, rel_tol=1e-8, abs_tol=1e-14,
-                       max_iter=100, ip=1.0, local="surrogate"):
+                       max_iter=100, ip=1.0, local="surrogate", auto_relaxation=False):
     """CG preconditioned by one V-cycle on a distorted hierarchy: dense mapped SIPG level
     matrices, DG embedding transfer, additive vertex-patch Schwarz smoother with surrogate-patch
     FD local solvers (one pre-, one post-step), dense exact coarse solve. Same V-cycle and
@@ -261,13 +290,21 @@ def mg_cg_solve_mapped(dim, k, n_rep, nc_fine, X, f, omega, rel_tol=1e-8, abs_to
                     Af = keep_definite(Ms, ksum_fit_closed(K, Ms), [a for _, a in MA])
                     inv[l].append((idx, fd_inverse(Ms, Af)))
 
-    def smooth(l, r):
+    omegas = [omega] * nl
+
+    def smooth(l, r, w=None):
+        w = omegas[l] if w is None else w
         if local == "surrogate":
-            return o.schwarz_vmult_surrogate(dim, k, [ncs[l]] * dim, hp[l], r, omega=omega, ip=ip)
+            return o.schwarz_vmult_surrogate(dim, k, [ncs[l]] * dim, hp[l], r, omega=w, ip=ip)
         out = np.zeros_like(r)
         for idx, Pinv in inv[l]:
-            out[idx] += omega * (Pinv @ r[idx])
+            out[idx] += w * (Pinv @ r[idx])
         return out
+
+    if auto_relaxation:
+        for l in range(1, nl):
+            omegas[l], _ = scaled_relaxation(A[l], lambda v, l=l: smooth(l, v, 1.0), omega, dim)
+    mg_cg_solve_mapped.last_omegas = list(omegas)
 
     def vcycle(l, b):
         if l == 0:

@@ -89,3 +89,29 @@ def test_mg_cg_on_distorted_mesh(tpss, oracle, mapped, cuda, dim, k, n_rep, ncf,
     assert it == it_ref
     assert rel_err(u.cpu().numpy(), u_ref) <= 1e-8
     assert rel_err(hist, hist_ref) <= 1e-8
+
+
+@pytest.mark.parametrize("dim,k,ncf,amp,local", [(3, 2, 8, 0.15, "surrogate"), (2, 3, 8, 0.25, "ksum")])
+def test_mg_scaled_relaxation_on_distorted_mesh(tpss, oracle, mapped, cuda, dim, k, ncf, amp, local):
+    """Spectrum-scaled damping: the per-level lambda_max(P A) estimates and the CG iterations
+    match the oracle's; with it the 3D surrogate smoother converges where the reference's fixed
+    damping makes the V-cycle indefinite."""
+    import torch
+    from tpss_gb300.mesh import distorted_cube
+    X = distorted_cube(dim, [ncf] * dim, 7, amp)
+    N = ncf ** dim * (k + 1) ** dim
+    f = philox(7, N)
+    om = oracle.lookup_damping_factor(1, 0, dim)
+    it_ref, hist_ref, u_ref = mapped.mg_cg_solve_mapped(dim, k, 2, ncf, X, f, om, local=local,
+                                                        auto_relaxation=True, max_iter=300)
+    w_ref = mapped.mg_cg_solve_mapped.last_omegas
+    ls = {"surrogate": tpss.LocalSolver.fd, "ksum": tpss.LocalSolver.ksum}[local]
+    mg = tpss.MultigridSolver(dim, k, 2, ncf, relaxation=om, coarse_solver=1, vertex_coords=X,
+                              local_solver=ls, auto_relaxation=True)
+    for l in range(1, mg.n_levels):
+        w, lam = mg.relaxation(l)
+        assert abs(w - w_ref[l]) <= 1e-8 * w_ref[l]
+    u = torch.zeros(N, dtype=torch.float64, device=cuda)
+    it, hist = mg.solve(u, torch.tensor(f, dtype=torch.float64, device=cuda), max_iter=300)
+    assert it == it_ref > 0
+    assert rel_err(u.cpu().numpy(), u_ref) <= 1e-8

@@ -515,7 +515,8 @@ class MultigridSolver:
     def __init__(self, dim, degree, n_rep, n_cells_fine, patch_variant=PatchVariant.vertex,
                  smoother_variant=SmootherVariant.additive, relaxation=None, ip_factor=1.0,
                  precision=Precision.fp64, coarse_tol=1e-12, coarse_solver=0, use_graph=True,
-                 vertex_coords=None, surrogate_n_q=5, local_solver=0, model=None):
+                 vertex_coords=None, surrogate_n_q=5, local_solver=0, model=None,
+                 auto_relaxation=False):
         if relaxation is None:
             relaxation = lookup_damping_factor(patch_variant, smoother_variant, dim)
         d = _lib.MgDesc()
@@ -526,6 +527,7 @@ class MultigridSolver:
             d.surrogate_n_q = int(surrogate_n_q)
         d.local_solver = int(local_solver)
         d.model = model.handle if model is not None else None
+        d.auto_relaxation = int(auto_relaxation)
         self._model = model
         d.dim, d.degree, d.n_rep, d.n_cells_fine = dim, degree, n_rep, n_cells_fine
         d.ip_factor, d.patch_variant, d.smoother_variant = float(ip_factor), patch_variant, smoother_variant
@@ -543,6 +545,12 @@ class MultigridSolver:
 
     def n_dofs(self):
         return self._n
+
+    def relaxation(self, level):
+        """(damping, lambda_max estimate) of the smoother on level 1..L."""
+        w, lam = C.c_double(), C.c_double()
+        check(load().tpss_mg_relaxation(self._h, int(level), C.byref(w), C.byref(lam)))
+        return w.value, lam.value
 
     def vmult(self, dst, src, stream=None):
         check(load().tpss_mg_vmult(self._h, _ptr(dst, self._n), _ptr(src, self._n), _stream(stream)))

@@ -59,7 +59,7 @@ class LayoutDesc(C.Structure):
                 ("n_cells", C.c_int * 3), ("cell_h", C.POINTER(C.c_double) * 3),
                 ("cell_dof_start", C.POINTER(C.c_int64)), ("patch_color", C.POINTER(C.c_int32)),
                 ("vertex_coords", C.POINTER(C.c_double)), ("surrogate_n_q", C.c_int),
-                ("local_solver", C.c_int), ("model", C.c_void_p)]
+                ("local_solver", C.c_int), ("model", C.c_void_p), ("auto_relaxation", C.c_int)]
 
 
 class PrecondDesc(C.Structure):
@@ -86,7 +86,7 @@ class MgDesc(C.Structure):
                 ("relaxation", C.c_double), ("precision", C.c_int), ("coarse_tol", C.c_double),
                 ("coarse_solver", C.c_int), ("use_graph", C.c_int),
                 ("vertex_coords", C.POINTER(C.c_double)), ("surrogate_n_q", C.c_int),
-                ("local_solver", C.c_int), ("model", C.c_void_p)]
+                ("local_solver", C.c_int), ("model", C.c_void_p), ("auto_relaxation", C.c_int)]
 
 
 _vp = C.c_void_p
@@ -127,6 +127,7 @@ SIGNATURES = {
     "tpss_transfer_prolongate_add": (C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_int), _vp, _vp, _vp]),
     "tpss_transfer_restrict_add": (C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_int), _vp, _vp, _vp]),
     "tpss_diag_fma_peak": (C.c_int, [C.c_int, C.c_int, _dp, _vp]),
+    "tpss_mg_relaxation": (C.c_int, [_vp, C.c_int, _dp, _dp]),
     "tpss_mlp_create": (C.c_int, [C.POINTER(MlpDesc), C.POINTER(_vp)]),
     "tpss_mlp_sizes": (C.c_int, [_vp, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "tpss_mlp_n_params": (C.c_int, [_vp, C.POINTER(C.c_int64)]),

@@ -185,6 +185,7 @@ struct MgLevel
   tpss_layout *L = nullptr;
   tpss_operator *op = nullptr;
   tpss_precond *P = nullptr;
+  double lambda_max = 0.0;  // estimate of lambda_max(P A) when the damping is scaled
   DeviceBuffer<double> x, b, t, r;
 };
 
@@ -372,6 +373,56 @@ void vcycle(tpss_mg *mg, cudaStream_t s)
 }
 }  // namespace
 
+namespace
+{
+// Damping from the spectrum of the additive smoother: the largest eigenvalue of P A (P the
+// undamped Schwarz preconditioner) is 2^dim for exact vertex-patch solvers on a Cartesian level
+// (every cell lies in 2^dim patches), where the reference's damping factor is tuned. On a
+// distorted level it grows (overlap of non-orthogonal patches, inexact local solvers), and with
+// the Cartesian damping the smoothing sweep stops being a contraction, which makes the V-cycle
+// indefinite. Power iteration with the Rayleigh quotient in the A inner product,
+// lambda = (A x, P A x) / (x, A x), 30 steps, 5% safety margin; the level's damping becomes
+// omega * 2^dim / (1.05 lambda) when that is smaller than omega.
+void scale_relaxation(tpss_mg &mg, MgLevel &lv)
+{
+  const tpss_layout &L = *lv.L;
+  const int64_t n = L.n_dofs;
+  std::vector<double> x0(n);
+  uint64_t st = 0x5eedull;
+  for(int64_t i = 0; i < n; ++i)
+  {
+    st = st * 6364136223846793005ull + 1442695040888963407ull;  // LCG (Knuth MMIX constants)
+    x0[i] = double(st >> 11) * (1.0 / 9007199254740992.0) - 0.5;
+  }
+  TPSS_CUDA(cudaMemcpy(lv.x.ptr, x0.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
+  const double omega = lv.P->desc.relaxation;
+  lv.P->desc.relaxation = 1.0;
+  cudaStream_t s = nullptr;
+  auto dot = [&](const double *a, const double *b) {
+    vec_dot(n, a, b, mg.partial.ptr, mg.scal.ptr, s);
+    double h = 0.0;
+    TPSS_CUDA(cudaMemcpy(&h, mg.scal.ptr, sizeof(double), cudaMemcpyDeviceToHost));
+    return h;
+  };
+  double lambda = 0.0;
+  for(int it = 0; it < 30; ++it)
+  {
+    operator_apply(lv.op, lv.t.ptr, lv.x.ptr, s);  // t = A x
+    precond_vmult(lv.P, lv.r.ptr, lv.t.ptr, s);    // r = P A x
+    const double xt = dot(lv.x.ptr, lv.t.ptr), tr = dot(lv.t.ptr, lv.r.ptr), rr = dot(lv.r.ptr, lv.r.ptr);
+    if(!(xt > 0.0) || !(rr > 0.0)) break;
+    lambda = tr / xt;
+    vec_axpby(n, 1.0 / std::sqrt(rr), lv.r.ptr, 0.0, lv.x.ptr, s);  // x = r / |r|
+  }
+  TPSS_CUDA(cudaDeviceSynchronize());
+  const double cart = L.patch_variant == TPSS_PATCH_VERTEX ? double(1 << L.dim) : 1.0;
+  double w = omega;
+  if(lambda > 0.0) w = std::min(omega, omega * cart / (1.05 * lambda));
+  lv.P->desc.relaxation = w;
+  lv.lambda_max = lambda;
+}
+}  // namespace
+
 extern "C" int tpss_mg_create(const tpss_mg_desc *d, tpss_mg **out)
 {
   return guarded([&] {
@@ -458,6 +509,8 @@ extern "C" int tpss_mg_create(const tpss_mg_desc *d, tpss_mg **out)
     TPSS_CUDA(cudaEventCreateWithFlags(&mg->ev_in, cudaEventDisableTiming));
     TPSS_CUDA(cudaEventCreateWithFlags(&mg->ev_out, cudaEventDisableTiming));
     mg->E = embedding_table(d->degree);
+    if(d->auto_relaxation)
+      for(int l = 1; l < nl; ++l) scale_relaxation(*mg, mg->lv[l]);
     *out = mg.release();
   });
 }
@@ -560,3 +613,12 @@ extern "C" int tpss_mg_cg_solve(tpss_mg *mg, double *u, const double *f, double 
 }
 
 extern "C" void tpss_mg_destroy(tpss_mg *mg) { delete mg; }
+
+extern "C" int tpss_mg_relaxation(const tpss_mg *mg, int level, double *relaxation, double *lambda_max)
+{
+  return guarded([&] {
+    TPSS_REQUIRE(mg && level >= 1 && level < (int)mg->lv.size(), "invalid level (smoothers on 1..L)");
+    if(relaxation) *relaxation = mg->lv[level].P->desc.relaxation;
+    if(lambda_max) *lambda_max = mg->lv[level].lambda_max;
+  });
+}
