@@ -266,6 +266,8 @@ struct tpss_precond
   tpss::DeviceBuffer<double> residual;  // multiplicative scratch
   tpss::DeviceBuffer<int> flag;         // finiteness check
   tpss::DeviceBuffer<float> halo;       // streamed kernel: partial sums of shared cells
+  tpss::DeviceBuffer<int64_t> fix_rec[4];  // streamed kernel: shared-cell list per variant
+  int64_t fix_n[4] = {-1, -1, -1, -1};
   int stream_variant = 0;               // streamed kernel variant (autotuner)
   std::vector<tpss::TimerSlot> timers;
   std::vector<tpss::PendingEvent> pending;
@@ -349,6 +351,10 @@ struct StreamLaunch
   int ras;
   DeviceBuffer<float> *halo;  // scratch, grown on demand
   int variant = 0;            // work decomposition chosen by the autotuner
+  // shared-cell list of the fix-up pass for this variant (built on first use), or null for
+  // the list-free fix-up kernel
+  DeviceBuffer<int64_t> *fix_rec = nullptr;
+  int64_t *fix_n = nullptr;
 };
 bool stream_supported(const tpss_layout &L);
 int stream_variant_count(const tpss_layout &L);

@@ -487,6 +487,8 @@ void precond_vmult(tpss_precond *p, double *dst, const double *src, cudaStream_t
       l.ras = p->desc.use_ras_weights != 0;
       l.halo = &p->halo;
       l.variant = p->stream_variant;
+      l.fix_rec = &p->fix_rec[p->stream_variant];
+      l.fix_n = &p->fix_n[p->stream_variant];
       if(!launch_stream3d(L, l, s)) fail(TPSS_ERR_CUDA, "streamed smoother launch failed");
     }
     else

@@ -1,4 +1,5 @@
 // stream3d.cu -- launcher of the streamed 3D vertex-patch smoother (see stream3d.cuh).
+#include <cstring>
 #include <mutex>
 #include <string>
 
@@ -11,6 +12,48 @@ namespace
 {
 template<int K1>
 using Cfg3 = stream::SCfg<K1, 4, 4, 8, 4>;
+
+// records of the cells shared between items (stream::fixup_list_kernel), same order of the
+// partials as stream::fixup_kernel
+template<class C>
+void build_fixup_list(const tpss_layout &L, const stream::StreamArgs &a, DeviceBuffer<int64_t> &out,
+                      int64_t &n_out)
+{
+  std::vector<int64_t> rec;
+  for(int cz = 0; cz < L.nc[2]; ++cz)
+    for(int cy = 0; cy < L.nc[1]; ++cy)
+      for(int cx = 0; cx < L.nc[0]; ++cx)
+      {
+        int tx[2], lx[2], ty[2], ly[2], tz[2], lz[2];
+        const int nx = stream::tiles_of(cx, C::BX, a.T[0], tx, lx);
+        const int ny = stream::tiles_of(cy, C::BY, a.T[1], ty, ly);
+        const int nz = stream::tiles_of(cz, C::BZ, a.T[2], tz, lz);
+        if(nx * ny * nz == 1) continue;
+        const int64_t cell = cx + (int64_t)L.nc[0] * (cy + (int64_t)L.nc[1] * cz);
+        float scale = 1.f;
+        if(a.ras)
+          scale = 1.f / (stream::multiplicity(cx, L.nc[0]) * stream::multiplicity(cy, L.nc[1]) *
+                         stream::multiplicity(cz, L.nc[2]));
+        uint32_t bits;
+        std::memcpy(&bits, &scale, sizeof(bits));
+        const size_t r0 = rec.size();
+        rec.resize(r0 + stream::kFixRec, 0);
+        rec[r0] = L.cell_start[cell];
+        rec[r0 + 1] = int64_t(uint64_t(nx * ny * nz) | (uint64_t(bits) << 32));
+        int k = 0;
+        for(int kz = 0; kz < nz; ++kz)
+          for(int ky = 0; ky < ny; ++ky)
+            for(int kx = 0; kx < nx; ++kx)
+            {
+              const int64_t item = tx[kx] + (int64_t)a.T[0] * (ty[ky] + (int64_t)a.T[1] * tz[kz]);
+              const int lcell = lx[kx] + C::CX * ly[ky];
+              rec[r0 + 2 + k++] =
+                ((item * (C::BZ + 1) + lz[kz]) * C::LCELLS + lcell) * (int64_t)C::CD;
+            }
+      }
+  n_out = (int64_t)(rec.size() / stream::kFixRec);
+  out.upload(rec.data(), rec.size());
+}
 
 template<class C>
 bool launch_stream(const tpss_layout &L, const StreamLaunch &l, cudaStream_t s)
@@ -51,9 +94,23 @@ bool launch_stream(const tpss_layout &L, const StreamLaunch &l, cudaStream_t s)
   const int grid = (int)(n_items < cap ? n_items : cap);
   stream::stream_kernel<C><<<grid, C::THREADS, smem, s>>>(a);
   TPSS_CUDA(cudaGetLastError());
-  const int64_t work = L.n_cells * C::CD;
-  const int64_t fb = (work + 255) / 256, fcap = (int64_t)num_sms() * 8;
-  stream::fixup_kernel<C><<<(int)(fb < fcap ? fb : fcap), 256, 0, s>>>(a);
+  if(l.fix_rec)
+  {
+    if(*l.fix_n < 0) build_fixup_list<C>(L, a, *l.fix_rec, *l.fix_n);
+    const int64_t n = *l.fix_n;
+    if(n > 0)
+    {
+      constexpr int per = 128 / C::CD;
+      const int64_t fb = (n + per - 1) / per, fcap = (int64_t)num_sms() * 16;
+      stream::fixup_list_kernel<C><<<(int)(fb < fcap ? fb : fcap), 128, 0, s>>>(l.fix_rec->ptr, n, a.halo, a.dst);
+    }
+  }
+  else
+  {
+    const int64_t work = L.n_cells * C::CD;
+    const int64_t fb = (work + 255) / 256, fcap = (int64_t)num_sms() * 8;
+    stream::fixup_kernel<C><<<(int)(fb < fcap ? fb : fcap), 256, 0, s>>>(a);
+  }
   TPSS_CUDA(cudaGetLastError());
   return true;
 }

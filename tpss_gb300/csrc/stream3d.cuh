@@ -91,7 +91,7 @@ struct StreamArgs
 };
 
 // tiles (t, local index l) of direction d that contain cell c; returns the count (1 or 2)
-__device__ __forceinline__ int tiles_of(int c, int W, int T, int *t, int *l)
+__host__ __device__ __forceinline__ int tiles_of(int c, int W, int T, int *t, int *l)
 {
   int n = 0;
   const int tt = c / W;
@@ -110,7 +110,7 @@ __device__ __forceinline__ int tiles_of(int c, int W, int T, int *t, int *l)
   return n;
 }
 
-__device__ __forceinline__ float multiplicity(int c, int n)
+__host__ __device__ __forceinline__ float multiplicity(int c, int n)
 {
   return float((c >= 1 ? 1 : 0) + (c + 1 <= n - 1 ? 1 : 0));
 }
@@ -610,6 +610,33 @@ __global__ void fixup_kernel(StreamArgs a)
     if(a.ras)
       s /= multiplicity(cx, a.nc[0]) * multiplicity(cy, a.nc[1]) * multiplicity(cz, a.nc[2]);
     a.dst[(a.cell_start ? a.cell_start[cell] : cell * CD) + e] = double(s);
+  }
+}
+
+// The same sums from a precomputed list of the shared cells: per record (10 int64) the first
+// dst DoF of the cell, the partial count (low 32 bits) and the RAS scale bits (high 32 bits),
+// then up to 8 halo offsets in the fixup_kernel order. Blocks of 128 threads take
+// 128 / CD cells at a time, one thread per cell DoF; no index arithmetic per DoF.
+constexpr int kFixRec = 10;
+
+template<class C>
+__global__ void __launch_bounds__(128) fixup_list_kernel(const int64_t *__restrict__ rec, int64_t n,
+                                                         const float *__restrict__ halo,
+                                                         double *__restrict__ dst)
+{
+  constexpr int CD = C::CD;
+  constexpr int PER = 128 / CD;
+  const int lc = threadIdx.x / CD, e = threadIdx.x % CD;
+  if(lc >= PER) return;
+  for(int64_t r = (int64_t)blockIdx.x * PER + lc; r < n; r += (int64_t)gridDim.x * PER)
+  {
+    const int64_t *f = rec + r * kFixRec;
+    const int64_t meta = f[1];
+    const int count = int(meta & 0xffffffff);
+    const float scale = __int_as_float(int(uint64_t(meta) >> 32));
+    float s = 0.f;
+    for(int k = 0; k < count; ++k) s += halo[f[2 + k] + e];
+    dst[f[0] + e] = double(s * scale);
   }
 }
 
