@@ -294,6 +294,37 @@ int tpss_transfer_restrict_add(int dim, int degree, const int *n_cells_coarse, d
  * every SM, `iters` FMAs per chain, timed with CUDA events).  The roofline denominator of the
  * CUDA-core-bound fast-diagonalization kernels. */
 /* ---------------------------------------------------------------------------------------
+ * C0 interior-penalty biharmonic problem (apps/biharmonic_integrator.h, biharmonic_problem.h):
+ * clamped, FE_Q(k) on Gauss-Lobatto nodes, 2D unit square with n_rep * 2^L cells per direction.
+ * Vectors hold the interior nodes (n k - 1)^2, x fastest, FP64 on the device. Level -1 is the
+ * finest. The additive vertex-patch smoother (2k-1)^2 nodes per patch, 4 colors) uses
+ * TPSS_LOCAL_EXACT (dense inverse of the patch matrix, LocalSolverVariant::Exact) or
+ * TPSS_LOCAL_FD (fast diagonalization of the patch matrix without the mixed-derivative
+ * term, LocalSolverVariant::Bilaplacian).
+ * ------------------------------------------------------------------------------------- */
+typedef struct tpss_c0ip tpss_c0ip;
+typedef struct tpss_c0ip_desc
+{
+  int degree;          /* 2..7 */
+  int n_rep;           /* coarse cells per direction (>= 2) */
+  int n_cells_fine;    /* n_rep * 2^L */
+  double ip_factor;    /* EquationData::ip_factor */
+  int local_solver;    /* TPSS_LOCAL_EXACT or TPSS_LOCAL_FD */
+  int precision;       /* smoother arithmetic, TPSS_FP64 / TPSS_FP32 */
+  double relaxation;   /* Schwarz damping (vertex patches, 2D: 0.25 in TPSS.h:121-163) */
+} tpss_c0ip_desc;
+
+int tpss_c0ip_create(const tpss_c0ip_desc *desc, tpss_c0ip **out);
+int tpss_c0ip_info(const tpss_c0ip *c, int level, int64_t *n_dofs, int *n_levels);
+int tpss_c0ip_operator_vmult(tpss_c0ip *c, int level, double *dst, const double *src, void *stream);
+/* dst = relaxation * sum_j R_j^T A_j^-1 R_j src on level 1..L (SchwarzPreconditioner::vmult) */
+int tpss_c0ip_smoother_vmult(tpss_c0ip *c, int level, double *dst, const double *src, void *stream);
+/* CG + one V-cycle per iteration (dense coarse solve), ReductionControl semantics */
+int tpss_c0ip_cg_solve(tpss_c0ip *c, double *u, const double *f, double rel_tol, double abs_tol,
+                       int max_iter, int *iterations, double *res_history, void *stream);
+void tpss_c0ip_destroy(tpss_c0ip *c);
+
+/* ---------------------------------------------------------------------------------------
  * Learned local solver (no counterpart in the reference: its distorted-mesh local solver is
  * the surrogate patch of mapping_info.templates.h:42-240). A small fully connected network
  * (tanh hidden layers, linear output, FP32) maps a vertex patch's geometry to corrections of

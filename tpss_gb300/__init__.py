@@ -400,6 +400,54 @@ class SchwarzSmoother:
             pass
 
 
+class C0IPBiharmonic:
+    """Clamped C0IP biharmonic problem on the unit square (FE_Q(k), Gauss-Lobatto nodes):
+    level operators, the additive vertex-patch smoother and CG + V-cycle. Vectors: interior
+    nodes, x fastest, float64 CUDA tensors."""
+
+    def __init__(self, degree, n_rep, n_cells_fine, ip_factor=1.0, local_solver=1, precision=0,
+                 relaxation=0.25):
+        d = _lib.C0ipDesc()
+        d.degree, d.n_rep, d.n_cells_fine = degree, n_rep, n_cells_fine
+        d.ip_factor, d.local_solver, d.precision, d.relaxation = float(ip_factor), int(local_solver), int(precision), float(relaxation)
+        h = C.c_void_p()
+        check(load().tpss_c0ip_create(C.byref(d), C.byref(h)))
+        self._h = h
+        nl = C.c_int()
+        check(load().tpss_c0ip_info(h, -1, None, C.byref(nl)))
+        self.n_levels = nl.value
+
+    def n_dofs(self, level=-1):
+        n = C.c_int64()
+        check(load().tpss_c0ip_info(self._h, int(level), C.byref(n), None))
+        return n.value
+
+    def vmult(self, dst, src, level=-1, stream=None):
+        n = self.n_dofs(level)
+        check(load().tpss_c0ip_operator_vmult(self._h, int(level), _ptr(dst, n), _ptr(src, n), _stream(stream)))
+
+    def smooth(self, dst, src, level=-1, stream=None):
+        n = self.n_dofs(level)
+        check(load().tpss_c0ip_smoother_vmult(self._h, int(level), _ptr(dst, n), _ptr(src, n), _stream(stream)))
+
+    def solve(self, u, f, rel_tol=1e-8, abs_tol=1e-14, max_iter=200, stream=None):
+        n = self.n_dofs()
+        hist = np.zeros(max_iter + 1)
+        it = C.c_int(0)
+        check(load().tpss_c0ip_cg_solve(self._h, _ptr(u, n), _ptr(f, n), float(rel_tol), float(abs_tol),
+                                        int(max_iter), C.byref(it), hist.ctypes.data_as(C.POINTER(C.c_double)),
+                                        _stream(stream)))
+        return it.value, hist[: it.value + 1]
+
+    def __del__(self):
+        try:
+            if self._h:
+                load().tpss_c0ip_destroy(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+
 class LocalSolver:
     """How the patch inverses are formed (tpss_precond_desc.local_solver)."""
     fd = 0       # fast diagonalization of the layout's (Cartesian or surrogate) 1-D problems

@@ -70,6 +70,12 @@ class PrecondDesc(C.Structure):
                 ("local_solver", C.c_int), ("model", C.c_void_p)]
 
 
+class C0ipDesc(C.Structure):
+    _fields_ = [("degree", C.c_int), ("n_rep", C.c_int), ("n_cells_fine", C.c_int),
+                ("ip_factor", C.c_double), ("local_solver", C.c_int), ("precision", C.c_int),
+                ("relaxation", C.c_double)]
+
+
 class MlpDesc(C.Structure):
     _fields_ = [("n_in", C.c_int), ("n_hidden", C.c_int), ("n_hidden_layers", C.c_int),
                 ("n_out", C.c_int), ("seed", C.c_uint64)]
@@ -128,6 +134,13 @@ SIGNATURES = {
     "tpss_transfer_restrict_add": (C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_int), _vp, _vp, _vp]),
     "tpss_diag_fma_peak": (C.c_int, [C.c_int, C.c_int, _dp, _vp]),
     "tpss_mg_relaxation": (C.c_int, [_vp, C.c_int, _dp, _dp]),
+    "tpss_c0ip_create": (C.c_int, [C.POINTER(C0ipDesc), C.POINTER(_vp)]),
+    "tpss_c0ip_info": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_int)]),
+    "tpss_c0ip_operator_vmult": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp]),
+    "tpss_c0ip_smoother_vmult": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp]),
+    "tpss_c0ip_cg_solve": (C.c_int, [_vp, _vp, _vp, C.c_double, C.c_double, C.c_int,
+                                     C.POINTER(C.c_int), _dp, _vp]),
+    "tpss_c0ip_destroy": (None, [_vp]),
     "tpss_mlp_create": (C.c_int, [C.POINTER(MlpDesc), C.POINTER(_vp)]),
     "tpss_mlp_sizes": (C.c_int, [_vp, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "tpss_mlp_n_params": (C.c_int, [_vp, C.POINTER(C.c_int64)]),
