@@ -48,6 +48,7 @@ def parse():
     ap.add_argument("--omega", type=float, default=0.15)
     ap.add_argument("--no-solve", action="store_true")
     ap.add_argument("--no-distorted", action="store_true")
+    ap.add_argument("--no-c0ip", action="store_true")
     ap.add_argument("--distortion", type=float, default=0.15)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -347,6 +348,8 @@ def run_ours(args):
         out["solve"] = solve_times(tpss, args)
     if not args.no_distorted:
         out["distorted"] = distorted_section(tpss, args)
+    if not args.no_c0ip:
+        out["c0ip"] = c0ip_section(tpss, args)
     if rank == 0 and not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline(args, W)
     if rank == 0:
@@ -514,6 +517,43 @@ def distorted_section(tpss, args):
     a, b = out["learned_fp32"], out["surrogate_fp64"]
     if "seconds" in a and "seconds" in b:
         out["learned_fp32_over_surrogate_fp64_time"] = a["seconds"] / b["seconds"]
+    return out
+
+
+def c0ip_section(tpss, args):
+    """2D clamped C0IP biharmonic, FE_Q(3), 256^2 cells (588,289 interior nodes): smoother
+    throughput and CG + V-cycle to 1e-8 with the FP32 fast-diagonalization local solver (patch
+    matrix without the mixed term, a rank-2 Kronecker sum) against FP64 exact local inverses."""
+    import torch
+    k, n = 3, 256
+    N = (n * k - 1) ** 2
+    f = torch.tensor(philox_src(N, args.seed), dtype=torch.float64, device="cuda")
+    out = {"workload": f"2D C0IP biharmonic FE_Q({k}) {n}^2 cells, {N} DoFs, additive vertex patches "
+                       f"of {(2 * k - 1) ** 2} nodes, damping 0.25, CG + V-cycle to 1e-8, dense coarse solve"}
+    for name, ls, prec in (("fd_fp32", tpss.LocalSolver.fd, tpss.Precision.fp32),
+                           ("fd_fp64", tpss.LocalSolver.fd, tpss.Precision.fp64),
+                           ("exact_fp64", tpss.LocalSolver.exact, tpss.Precision.fp64)):
+        P = tpss.C0IPBiharmonic(k, 2, n, local_solver=ls, precision=prec, relaxation=0.25)
+        d = torch.empty_like(f)
+        for _ in range(3):
+            P.smooth(d, f)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(20):
+            P.smooth(d, f)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / 20
+        u = torch.zeros_like(f)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        it, hist = P.solve(u, f, rel_tol=1e-8, max_iter=200)
+        torch.cuda.synchronize()
+        out[name] = {"smoother_ms": ms, "smoother_dof_per_s": N / (ms * 1e-3),
+                     "solve_seconds": time.perf_counter() - t0, "iterations": it}
+        del P
+    out["fd_fp32_over_exact_fp64_time"] = out["fd_fp32"]["solve_seconds"] / out["exact_fp64"]["solve_seconds"]
     return out
 
 
