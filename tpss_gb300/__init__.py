@@ -332,6 +332,20 @@ class SchwarzPreconditioner:
         n = self.m()
         check(load().tpss_precond_Tvmult(self._h, _ptr(dst, n), _ptr(src, n), _stream(stream)))
 
+    def vmult_host(self, dst, src, stream=None):
+        """vmult with dst and src in host memory (pinned CPU float64 tensors or numpy arrays);
+        the copies overlap the streamed kernel. Stream-ordered."""
+        n = self.m()
+
+        def hptr(a):
+            if isinstance(a, np.ndarray):
+                assert a.dtype == np.float64 and a.size == n and a.flags.c_contiguous
+                return C.c_void_p(a.ctypes.data)
+            assert (not a.is_cuda) and a.dtype.is_floating_point and a.element_size() == 8 and a.numel() == n
+            return C.c_void_p(a.data_ptr())
+
+        check(load().tpss_precond_vmult_host(self._h, hptr(dst), hptr(src), _stream(stream)))
+
     def autotune(self, dst, src, reps=5, stream=None):
         """Time the kernel variants for this level on (src -> dst) and keep the fastest.
         Returns (chosen variant, milliseconds per variant)."""

@@ -114,6 +114,7 @@ SIGNATURES = {
     "tpss_precond_vmult_add": (C.c_int, [_vp, _vp, _vp, _vp]),
     "tpss_precond_Tvmult": (C.c_int, [_vp, _vp, _vp, _vp]),
     "tpss_precond_vmult_static_scratch": (C.c_int, [_vp, _vp, _vp, _vp]),
+    "tpss_precond_vmult_host": (C.c_int, [_vp, _vp, _vp, _vp]),
     "tpss_precond_autotune": (C.c_int, [_vp, _vp, _vp, C.c_int, C.POINTER(C.c_int), _dp,
                                         C.POINTER(C.c_int), _vp]),
     "tpss_precond_time_info": (C.c_int, [_vp, C.POINTER(TimeInfo), C.POINTER(C.c_int)]),

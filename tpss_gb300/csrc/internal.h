@@ -256,6 +256,38 @@ struct PendingEvent
   int slot;
 };
 
+// copy / compute / copy pipeline of the host-buffer smoother entry point
+struct HostPipe
+{
+  cudaStream_t up = nullptr, comp = nullptr, down = nullptr;
+  std::vector<cudaEvent_t> ev;
+  DeviceBuffer<double> src, dst;
+  cudaEvent_t event(size_t i)
+  {
+    while(ev.size() <= i)
+    {
+      cudaEvent_t e;
+      TPSS_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+      ev.push_back(e);
+    }
+    return ev[i];
+  }
+  void streams()
+  {
+    if(up) return;
+    TPSS_CUDA(cudaStreamCreateWithFlags(&up, cudaStreamNonBlocking));
+    TPSS_CUDA(cudaStreamCreateWithFlags(&comp, cudaStreamNonBlocking));
+    TPSS_CUDA(cudaStreamCreateWithFlags(&down, cudaStreamNonBlocking));
+  }
+  HostPipe() = default;
+  HostPipe(const HostPipe &) = delete;
+  ~HostPipe()
+  {
+    for(cudaEvent_t e : ev) cudaEventDestroy(e);
+    for(cudaStream_t s : {up, comp, down})
+      if(s) cudaStreamDestroy(s);
+  }
+};
 }  // namespace tpss
 
 struct tpss_precond
@@ -268,6 +300,8 @@ struct tpss_precond
   tpss::DeviceBuffer<float> halo;       // streamed kernel: partial sums of shared cells
   tpss::DeviceBuffer<int64_t> fix_rec[4];  // streamed kernel: shared-cell list per variant
   int64_t fix_n[4] = {-1, -1, -1, -1};
+  std::vector<int64_t> fix_layer[4];
+  tpss::HostPipe pipe;                  // host-buffer entry point
   int stream_variant = 0;               // streamed kernel variant (autotuner)
   std::vector<tpss::TimerSlot> timers;
   std::vector<tpss::PendingEvent> pending;
@@ -355,7 +389,12 @@ struct StreamLaunch
   // the list-free fix-up kernel
   DeviceBuffer<int64_t> *fix_rec = nullptr;
   int64_t *fix_n = nullptr;
+  std::vector<int64_t> *fix_layer = nullptr;  // first record of every cell layer (nc_z + 1)
 };
+
+// pipelined streamed smoother between host buffers: returns false when not applicable
+bool launch_stream3d_host(const tpss_layout &L, const StreamLaunch &l, HostPipe &pipe, double *h_dst,
+                          const double *h_src, cudaStream_t caller);
 bool stream_supported(const tpss_layout &L);
 int stream_variant_count(const tpss_layout &L);
 bool launch_stream3d(const tpss_layout &L, const StreamLaunch &l, cudaStream_t s);

@@ -462,6 +462,26 @@ bool use_stream(const tpss_precond *p)
   return ok;
 }
 
+StreamLaunch stream_launch(tpss_precond *p, double *dst, const double *src)
+{
+  const tpss_layout &L = *p->tables->layout;
+  StreamLaunch l;
+  l.src = src;
+  l.dst = dst;
+  l.fd32 = p->tables->fd32.ptr;
+  l.fd32_eo = p->tables->fd32_eo.ptr;
+  l.sym = p->tables->sym.ptr;
+  l.es_eo = 4 * (L.n / 2) * p->tables->hpad32 + p->tables->npad32;
+  l.omega = p->desc.relaxation;
+  l.ras = p->desc.use_ras_weights != 0;
+  l.halo = &p->halo;
+  l.variant = p->stream_variant;
+  l.fix_rec = &p->fix_rec[p->stream_variant];
+  l.fix_n = &p->fix_n[p->stream_variant];
+  l.fix_layer = &p->fix_layer[p->stream_variant];
+  return l;
+}
+
 void precond_vmult(tpss_precond *p, double *dst, const double *src, cudaStream_t s)
 {
   const tpss_layout &L = *p->tables->layout;
@@ -476,19 +496,7 @@ void precond_vmult(tpss_precond *p, double *dst, const double *src, cudaStream_t
     if(use_stream(p))
     {
       // one pass over all patches; every cell of dst is written, no zeroing needed
-      StreamLaunch l;
-      l.src = src;
-      l.dst = dst;
-      l.fd32 = p->tables->fd32.ptr;
-      l.fd32_eo = p->tables->fd32_eo.ptr;
-      l.sym = p->tables->sym.ptr;
-      l.es_eo = 4 * (L.n / 2) * p->tables->hpad32 + p->tables->npad32;
-      l.omega = p->desc.relaxation;
-      l.ras = p->desc.use_ras_weights != 0;
-      l.halo = &p->halo;
-      l.variant = p->stream_variant;
-      l.fix_rec = &p->fix_rec[p->stream_variant];
-      l.fix_n = &p->fix_n[p->stream_variant];
+      const StreamLaunch l = stream_launch(p, dst, src);
       if(!launch_stream3d(L, l, s)) fail(TPSS_ERR_CUDA, "streamed smoother launch failed");
     }
     else
@@ -771,5 +779,27 @@ extern "C" int tpss_precond_autotune(tpss_precond *p, double *dst, const double 
     p->stream_variant = best;
     if(chosen) *chosen = best;
     precond_vmult(p, dst, src, s);  // dst holds the chosen variant's result
+  });
+}
+
+extern "C" int tpss_precond_vmult_host(tpss_precond *p, double *dst, const double *src, void *stream)
+{
+  return guarded([&] {
+    TPSS_REQUIRE(p && dst && src, "null argument");
+    TPSS_REQUIRE(dst != src, "dst and src must not alias");
+    cudaStream_t s = as_stream(stream);
+    const tpss_layout &L = *p->tables->layout;
+    const size_t N = (size_t)L.n_dofs;
+    if(p->pipe.src.n < N) p->pipe.src.resize(N);
+    if(p->pipe.dst.n < N) p->pipe.dst.resize(N);
+    ScopedTimer step(p, 4, s);
+    if(L.smoother_variant == TPSS_ADDITIVE && use_stream(p) && !p->desc.check_finite)
+    {
+      const StreamLaunch l = stream_launch(p, p->pipe.dst.ptr, p->pipe.src.ptr);
+      if(launch_stream3d_host(L, l, p->pipe, dst, src, s)) return;
+    }
+    TPSS_CUDA(cudaMemcpyAsync(p->pipe.src.ptr, src, sizeof(double) * N, cudaMemcpyHostToDevice, s));
+    precond_vmult(p, p->pipe.dst.ptr, p->pipe.src.ptr, s);
+    TPSS_CUDA(cudaMemcpyAsync(dst, p->pipe.dst.ptr, sizeof(double) * N, cudaMemcpyDeviceToHost, s));
   });
 }

@@ -17,10 +17,13 @@ using Cfg3 = stream::SCfg<K1, 4, 4, 8, 4>;
 // partials as stream::fixup_kernel
 template<class C>
 void build_fixup_list(const tpss_layout &L, const stream::StreamArgs &a, DeviceBuffer<int64_t> &out,
-                      int64_t &n_out)
+                      int64_t &n_out, std::vector<int64_t> *layer_start)
 {
   std::vector<int64_t> rec;
+  if(layer_start) layer_start->assign(L.nc[2] + 1, 0);
   for(int cz = 0; cz < L.nc[2]; ++cz)
+  {
+    if(layer_start) (*layer_start)[cz] = (int64_t)(rec.size() / stream::kFixRec);
     for(int cy = 0; cy < L.nc[1]; ++cy)
       for(int cx = 0; cx < L.nc[0]; ++cx)
       {
@@ -51,12 +54,14 @@ void build_fixup_list(const tpss_layout &L, const stream::StreamArgs &a, DeviceB
                 ((item * (C::BZ + 1) + lz[kz]) * C::LCELLS + lcell) * (int64_t)C::CD;
             }
       }
+  }
   n_out = (int64_t)(rec.size() / stream::kFixRec);
+  if(layer_start) (*layer_start)[L.nc[2]] = n_out;
   out.upload(rec.data(), rec.size());
 }
 
 template<class C>
-bool launch_stream(const tpss_layout &L, const StreamLaunch &l, cudaStream_t s)
+stream::StreamArgs make_args(const tpss_layout &L, const StreamLaunch &l)
 {
   stream::StreamArgs a;
   a.src = l.src;
@@ -77,33 +82,113 @@ bool launch_stream(const tpss_layout &L, const StreamLaunch &l, cudaStream_t s)
   a.omega = (float)l.omega;
   a.ras = l.ras;
   const int64_t n_items = (int64_t)a.T[0] * a.T[1] * a.T[2];
+  a.item_begin = 0;
+  a.item_end = (int)n_items;
   const size_t halo_floats = (size_t)n_items * (C::BZ + 1) * C::LCELLS * C::CD;
   if(l.halo->n < halo_floats) l.halo->resize(halo_floats);
   a.halo = l.halo->ptr;
+  return a;
+}
+
+// resident CTAs of the streamed kernel (sets its shared-memory attribute once)
+template<class C>
+int64_t stream_cap()
+{
   static int per_sm = 0;
-  const size_t smem = C::smem_bytes();
   if(per_sm == 0)
   {
     TPSS_CUDA(cudaFuncSetAttribute(stream::stream_kernel<C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)smem));
+                                   (int)C::smem_bytes()));
     int occ = 0;
-    TPSS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, stream::stream_kernel<C>, C::THREADS, smem));
+    TPSS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, stream::stream_kernel<C>, C::THREADS,
+                                                            C::smem_bytes()));
     per_sm = occ < 1 ? 1 : occ;
   }
-  const int64_t cap = (int64_t)num_sms() * per_sm;
+  return (int64_t)num_sms() * per_sm;
+}
+
+template<class C>
+void launch_fixup_range(const stream::StreamArgs &a, const int64_t *rec, int64_t n, cudaStream_t s)
+{
+  if(n <= 0) return;
+  constexpr int per = 128 / C::CD;
+  const int64_t fb = (n + per - 1) / per, fcap = (int64_t)num_sms() * 16;
+  stream::fixup_list_kernel<C><<<(int)(fb < fcap ? fb : fcap), 128, 0, s>>>(rec, n, a.halo, a.dst);
+}
+
+// src and dst in host memory: the level is cut into chunks of z-items; per chunk the cell layers
+// it reads are copied in (stream up), its items are solved and the shared cells of the layers it
+// completes are summed (stream comp), and those finished layers are copied out (stream down)
+template<class C>
+bool launch_stream_host(const tpss_layout &L, const StreamLaunch &l0, HostPipe &pp, double *h_dst,
+                        const double *h_src, cudaStream_t caller)
+{
+  if(!L.lexicographic || !l0.fix_rec) return false;
+  StreamLaunch l = l0;
+  l.src = pp.src.ptr;
+  l.dst = pp.dst.ptr;
+  stream::StreamArgs a = make_args<C>(L, l);
+  if(*l.fix_n < 0) build_fixup_list<C>(L, a, *l.fix_rec, *l.fix_n, l.fix_layer);
+  const std::vector<int64_t> &ls = *l.fix_layer;
+  const int64_t layer = (int64_t)L.nc[0] * L.nc[1] * C::CD;  // DoFs of one cell layer
+  const int nz = L.nc[2], T2 = a.T[2];
+  const int64_t items_per_z = (int64_t)a.T[0] * a.T[1];
+  const int per = 1;  // one z-item per chunk: the shortest pipeline fill and drain
+  const int64_t cap = stream_cap<C>();
+  pp.streams();
+  size_t e = 0;
+  cudaEvent_t start = pp.event(e++);
+  TPSS_CUDA(cudaEventRecord(start, caller));
+  for(cudaStream_t st : {pp.up, pp.comp, pp.down}) TPSS_CUDA(cudaStreamWaitEvent(st, start, 0));
+  int copied = 0, fixed = 0;
+  for(int z0 = 0; z0 < T2; z0 += per)
+  {
+    const int z1 = std::min(T2, z0 + per);
+    const bool last = z1 == T2;
+    const int need = last ? nz : std::min(z1 * C::BZ + 1, nz);  // cell layers read so far
+    if(need > copied)
+      TPSS_CUDA(cudaMemcpyAsync(pp.src.ptr + copied * layer, h_src + copied * layer,
+                                sizeof(double) * (size_t)(need - copied) * layer, cudaMemcpyHostToDevice, pp.up));
+    copied = need;
+    cudaEvent_t up_done = pp.event(e++);
+    TPSS_CUDA(cudaEventRecord(up_done, pp.up));
+    TPSS_CUDA(cudaStreamWaitEvent(pp.comp, up_done, 0));
+    a.item_begin = (int)(z0 * items_per_z);
+    a.item_end = (int)(z1 * items_per_z);
+    const int64_t n_items = a.item_end - a.item_begin;
+    stream::stream_kernel<C><<<(int)std::min(n_items, cap), C::THREADS, C::smem_bytes(), pp.comp>>>(a);
+    TPSS_CUDA(cudaGetLastError());
+    const int bound = last ? nz : z1 * C::BZ;  // cell layers final after this chunk
+    launch_fixup_range<C>(a, l.fix_rec->ptr + ls[fixed] * stream::kFixRec, ls[bound] - ls[fixed], pp.comp);
+    TPSS_CUDA(cudaGetLastError());
+    cudaEvent_t comp_done = pp.event(e++);
+    TPSS_CUDA(cudaEventRecord(comp_done, pp.comp));
+    TPSS_CUDA(cudaStreamWaitEvent(pp.down, comp_done, 0));
+    if(bound > fixed)
+      TPSS_CUDA(cudaMemcpyAsync(h_dst + fixed * layer, pp.dst.ptr + fixed * layer,
+                                sizeof(double) * (size_t)(bound - fixed) * layer, cudaMemcpyDeviceToHost, pp.down));
+    fixed = bound;
+  }
+  cudaEvent_t done = pp.event(e++);
+  TPSS_CUDA(cudaEventRecord(done, pp.down));
+  TPSS_CUDA(cudaStreamWaitEvent(caller, done, 0));
+  return true;
+}
+
+template<class C>
+bool launch_stream(const tpss_layout &L, const StreamLaunch &l, cudaStream_t s)
+{
+  stream::StreamArgs a = make_args<C>(L, l);
+  const int64_t n_items = (int64_t)a.item_end;
+  const int64_t cap = stream_cap<C>();
   const int grid = (int)(n_items < cap ? n_items : cap);
+  const size_t smem = C::smem_bytes();
   stream::stream_kernel<C><<<grid, C::THREADS, smem, s>>>(a);
   TPSS_CUDA(cudaGetLastError());
   if(l.fix_rec)
   {
-    if(*l.fix_n < 0) build_fixup_list<C>(L, a, *l.fix_rec, *l.fix_n);
-    const int64_t n = *l.fix_n;
-    if(n > 0)
-    {
-      constexpr int per = 128 / C::CD;
-      const int64_t fb = (n + per - 1) / per, fcap = (int64_t)num_sms() * 16;
-      stream::fixup_list_kernel<C><<<(int)(fb < fcap ? fb : fcap), 128, 0, s>>>(l.fix_rec->ptr, n, a.halo, a.dst);
-    }
+    if(*l.fix_n < 0) build_fixup_list<C>(L, a, *l.fix_rec, *l.fix_n, l.fix_layer);
+    launch_fixup_range<C>(a, l.fix_rec->ptr, *l.fix_n, s);
   }
   else
   {
@@ -161,6 +246,34 @@ bool launch_variant(const tpss_layout &L, const StreamLaunch &l, cudaStream_t s,
   case 1: return launch_stream<typename VariantCfg<K1, 1>::type>(L, l, s);
   case 2: return launch_stream<typename VariantCfg<K1, 2>::type>(L, l, s);
   case 3: return launch_stream<typename VariantCfg<K1, 3>::type>(L, l, s);
+  default: return false;
+  }
+}
+
+template<int K1>
+bool launch_variant_host(const tpss_layout &L, const StreamLaunch &l, HostPipe &pp, double *h_dst,
+                         const double *h_src, cudaStream_t s, int v)
+{
+  switch(v)
+  {
+  case 0: return launch_stream_host<typename VariantCfg<K1, 0>::type>(L, l, pp, h_dst, h_src, s);
+  case 1: return launch_stream_host<typename VariantCfg<K1, 1>::type>(L, l, pp, h_dst, h_src, s);
+  case 2: return launch_stream_host<typename VariantCfg<K1, 2>::type>(L, l, pp, h_dst, h_src, s);
+  case 3: return launch_stream_host<typename VariantCfg<K1, 3>::type>(L, l, pp, h_dst, h_src, s);
+  default: return false;
+  }
+}
+
+bool launch_stream3d_host(const tpss_layout &L, const StreamLaunch &l, HostPipe &pp, double *h_dst,
+                          const double *h_src, cudaStream_t s)
+{
+  const int v = l.variant;
+  switch(L.k)
+  {
+  case 1: return launch_variant_host<2>(L, l, pp, h_dst, h_src, s, v);
+  case 2: return launch_variant_host<3>(L, l, pp, h_dst, h_src, s, v);
+  case 3: return launch_variant_host<4>(L, l, pp, h_dst, h_src, s, v);
+  case 4: return launch_variant_host<5>(L, l, pp, h_dst, h_src, s, v);
   default: return false;
   }
 }
@@ -247,6 +360,8 @@ void launch_stream_static(const tpss_layout &L, const tpss_precond &p, const dou
   a.omega = (float)p.desc.relaxation;
   a.ras = p.desc.use_ras_weights != 0;
   const int64_t n_items = (int64_t)a.T[0] * a.T[1] * a.T[2];
+  a.item_begin = 0;
+  a.item_end = (int)n_items;
   const size_t halo_floats = (size_t)n_items * (C::BZ + 1) * C::LCELLS * C::CD;
   if(halo_floats > kStaticHaloFloats)
     fail(TPSS_ERR_INVALID_ARGUMENT,

@@ -88,6 +88,7 @@ struct StreamArgs
   int T[3];                                // items per direction
   float omega;
   int ras;                                 // scale by 1/multiplicity
+  int item_begin, item_end;                // items of this launch (z-major item order)
 };
 
 // tiles (t, local index l) of direction d that contain cell c; returns the count (1 or 2)
@@ -466,7 +467,7 @@ __global__ void __launch_bounds__(C::THREADS, 1) stream_kernel(StreamArgs a)
   const int e_patch = (e % K1) + SX * ((e / K1) % K1) + SXY * (e / (K1 * K1));
   const int n_items = a.T[0] * a.T[1] * a.T[2];
 
-  for(int item = blockIdx.x; item < n_items; item += gridDim.x)
+  for(int item = a.item_begin + blockIdx.x; item < a.item_end && item < n_items; item += gridDim.x)
   {
     const int tx = item % a.T[0], ty = (item / a.T[0]) % a.T[1], tz = item / (a.T[0] * a.T[1]);
     // vertices of the item: v_d in [1 + W t, min(W (t+1), n_d - 1)]
