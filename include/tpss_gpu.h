@@ -279,6 +279,19 @@ int tpss_mg_vmult(tpss_mg *mg, double *dst, const double *src, void *stream);
  * max_iter+1, may be NULL) the residual norms. */
 int tpss_mg_cg_solve(tpss_mg *mg, double *u, const double *f, double rel_tol, double abs_tol,
                      int max_iter, int *iterations, double *res_history, void *stream);
+/* Batched solves (no counterpart in the reference, which runs one problem per process): many
+ * independent hierarchies (each described by a tpss_mg_desc; dense coarse solve and graphs
+ * recommended) solved by CG in lockstep -- every round enqueues one iteration per active
+ * problem on n_streams streams (V-cycles replay their CUDA graphs), then one host
+ * synchronization reads all residual norms. iterations: n_problems entries (-1 if a problem
+ * did not converge within max_iter, which also returns TPSS_ERR_NOT_CONVERGED). */
+typedef struct tpss_batch tpss_batch;
+int tpss_batch_create(const tpss_mg_desc *descs, int n_problems, int n_streams, tpss_batch **out);
+int tpss_batch_problem(tpss_batch *b, int i, tpss_mg **mg);
+int tpss_batch_solve(tpss_batch *b, double *const *u, const double *const *f, double rel_tol,
+                     double abs_tol, int max_iter, int *iterations, void *stream);
+void tpss_batch_destroy(tpss_batch *b);
+
 /* Damping used by the smoother of level 1..L and, with auto_relaxation, the estimate of
  * lambda_max(P A) it was scaled by (0 otherwise). No counterpart in the reference. */
 int tpss_mg_relaxation(const tpss_mg *mg, int level, double *relaxation, double *lambda_max);

@@ -462,6 +462,52 @@ class C0IPBiharmonic:
             pass
 
 
+class BatchSolver:
+    """Many independent CG + GMG problems (unit-cube SIPG levels) solved in lockstep: one CG
+    iteration per active problem per round, one host synchronization per round."""
+
+    def __init__(self, problems, n_streams=8):
+        """problems: list of dicts with MultigridSolver keyword arguments (dim, degree, n_rep,
+        n_cells_fine, relaxation, precision, coarse_solver, use_graph, ...)."""
+        arr = (_lib.MgDesc * len(problems))()
+        for d, pr in zip(arr, problems):
+            dim = pr["dim"]
+            pv = pr.get("patch_variant", PatchVariant.vertex)
+            sv = pr.get("smoother_variant", SmootherVariant.additive)
+            d.dim, d.degree, d.n_rep, d.n_cells_fine = dim, pr["degree"], pr["n_rep"], pr["n_cells_fine"]
+            d.ip_factor, d.patch_variant, d.smoother_variant = float(pr.get("ip_factor", 1.0)), pv, sv
+            rel = pr.get("relaxation")
+            d.relaxation = float(rel if rel is not None else lookup_damping_factor(pv, sv, dim))
+            d.precision = int(pr.get("precision", Precision.fp32))
+            d.coarse_tol = float(pr.get("coarse_tol", 1e-12))
+            d.coarse_solver = int(pr.get("coarse_solver", 1))
+            d.use_graph = int(pr.get("use_graph", 1))
+        h = C.c_void_p()
+        check(load().tpss_batch_create(arr, len(problems), int(n_streams), C.byref(h)))
+        self._h = h
+        self.problems = list(problems)
+        self.n_dofs = [pr["n_cells_fine"] ** pr["dim"] * (pr["degree"] + 1) ** pr["dim"] for pr in problems]
+
+    def solve(self, us, fs, rel_tol=1e-8, abs_tol=1e-14, max_iter=200, stream=None):
+        """us, fs: lists of float64 CUDA tensors; returns the CG iteration counts."""
+        n = len(self.problems)
+        assert len(us) == n and len(fs) == n
+        U = (C.c_void_p * n)(*[_ptr(u, m).value for u, m in zip(us, self.n_dofs)])
+        F = (C.c_void_p * n)(*[_ptr(f, m).value for f, m in zip(fs, self.n_dofs)])
+        its = (C.c_int * n)()
+        check(load().tpss_batch_solve(self._h, U, F, float(rel_tol), float(abs_tol), int(max_iter), its,
+                                      _stream(stream)))
+        return list(its)
+
+    def __del__(self):
+        try:
+            if self._h:
+                load().tpss_batch_destroy(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+
 class LocalSolver:
     """How the patch inverses are formed (tpss_precond_desc.local_solver)."""
     fd = 0       # fast diagonalization of the layout's (Cartesian or surrogate) 1-D problems

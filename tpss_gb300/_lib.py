@@ -142,6 +142,11 @@ SIGNATURES = {
     "tpss_c0ip_cg_solve": (C.c_int, [_vp, _vp, _vp, C.c_double, C.c_double, C.c_int,
                                      C.POINTER(C.c_int), _dp, _vp]),
     "tpss_c0ip_destroy": (None, [_vp]),
+    "tpss_batch_create": (C.c_int, [C.POINTER(MgDesc), C.c_int, C.c_int, C.POINTER(_vp)]),
+    "tpss_batch_problem": (C.c_int, [_vp, C.c_int, C.POINTER(_vp)]),
+    "tpss_batch_solve": (C.c_int, [_vp, C.POINTER(_vp), C.POINTER(_vp), C.c_double, C.c_double, C.c_int,
+                                   C.POINTER(C.c_int), _vp]),
+    "tpss_batch_destroy": (None, [_vp]),
     "tpss_mlp_create": (C.c_int, [C.POINTER(MlpDesc), C.POINTER(_vp)]),
     "tpss_mlp_sizes": (C.c_int, [_vp, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "tpss_mlp_n_params": (C.c_int, [_vp, C.POINTER(C.c_int64)]),

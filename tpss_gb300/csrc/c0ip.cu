@@ -189,16 +189,21 @@ __global__ void __launch_bounds__(256) c0ip_x_kernel(const double *__restrict__ 
   {
     const int x = int(t % n);
     const int64_t row = t - x;
+    // M and L couple nodes of one cell (|offset| <= k = bw / 2), B across a node (<= 2k)
     double sm = 0, sl = 0, sb = 0;
+    const int bh = bw / 2;
     for(int o = -bw; o <= bw; ++o)
     {
       const int j = x + o;
       if(j < 0 || j >= n) continue;
       const double v = u[row + j];
       const int at = x * w + o + bw;
-      sm += M[at] * v;
-      sl += L[at] * v;
       sb += B[at] * v;
+      if(o >= -bh && o <= bh)
+      {
+        sm += M[at] * v;
+        sl += L[at] * v;
+      }
     }
     tm[t] = sm;
     tl[t] = sl;
@@ -218,13 +223,15 @@ __global__ void __launch_bounds__(256) c0ip_y_kernel(const double *__restrict__ 
   {
     const int x = int(t % n), y = int(t / n);
     double s = 0;
+    const int bh = bw / 2;
     for(int o = -bw; o <= bw; ++o)
     {
       const int j = y + o;
       if(j < 0 || j >= n) continue;
       const int64_t src = (int64_t)j * n + x;
       const int at = y * w + o + bw;
-      s += M[at] * tb[src] + 2.0 * L[at] * tl[src] + B[at] * tm[src];
+      s += B[at] * tm[src];
+      if(o >= -bh && o <= bh) s += M[at] * tb[src] + 2.0 * L[at] * tl[src];
     }
     dst[t] = s;
   }
@@ -243,25 +250,26 @@ struct PatchArgs
   double omega;
 };
 
-// one patch per CTA: gather (2k-1)^2 nodes, apply the local inverse, scatter-add omega * result
+// one patch per warp (4 per CTA): gather (2k-1)^2 nodes into shared memory, apply the local
+// inverse, scatter-add omega * result (patches of one color are disjoint)
 template<typename T, bool DENSE>
 __global__ void __launch_bounds__(128) c0ip_patch_kernel(const PatchArgs a)
 {
   extern __shared__ unsigned char smraw[];
   const int m = a.m, m2 = m * m;
-  T *r = reinterpret_cast<T *>(smraw);
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  T *r = reinterpret_cast<T *>(smraw) + (size_t)warp * 2 * m2;
   T *w = r + m2;
   const T *tab = reinterpret_cast<const T *>(a.tab);
-  for(int64_t p = blockIdx.x; p < a.n_patches; p += gridDim.x)
+  for(int64_t p = (int64_t)blockIdx.x * 4 + warp; p < a.n_patches; p += (int64_t)gridDim.x * 4)
   {
     const int x0 = (a.vertex[2 * p] - 1) * a.k, y0 = (a.vertex[2 * p + 1] - 1) * a.k;
-    for(int l = threadIdx.x; l < m2; l += blockDim.x)
-      r[l] = T(a.src[(int64_t)(y0 + l / m) * a.n + x0 + l % m]);
-    __syncthreads();
+    for(int l = lane; l < m2; l += 32) r[l] = T(a.src[(int64_t)(y0 + l / m) * a.n + x0 + l % m]);
+    __syncwarp();
     if constexpr(DENSE)
     {
       const T *Ai = tab + (size_t)a.key[2 * p] * m2 * m2;
-      for(int i = threadIdx.x; i < m2; i += blockDim.x)
+      for(int i = lane; i < m2; i += 32)
       {
         T acc = 0;
         for(int j = 0; j < m2; ++j) acc += Ai[(size_t)j * m2 + i] * r[j];
@@ -272,44 +280,43 @@ __global__ void __launch_bounds__(128) c0ip_patch_kernel(const PatchArgs a)
     {
       // u = (Sy x Sx) diag(1 / (lx + ly)) (Sy x Sx)^T r; entry layout [S m x m][lambda m]
       const T *ex = tab + (size_t)a.key[2 * p] * (m * m + m), *ey = tab + (size_t)a.key[2 * p + 1] * (m * m + m);
-      for(int l = threadIdx.x; l < m2; l += blockDim.x)  // w = Sx^T along x
+      for(int l = lane; l < m2; l += 32)  // w = Sx^T along x
       {
         const int i = l % m, row = l - i;
         T s = 0;
         for(int j = 0; j < m; ++j) s += ex[j * m + i] * r[row + j];
         w[l] = s;
       }
-      __syncthreads();
-      for(int l = threadIdx.x; l < m2; l += blockDim.x)  // r = Sy^T along y, / eigenvalue sums
+      __syncwarp();
+      for(int l = lane; l < m2; l += 32)  // r = Sy^T along y, / eigenvalue sums
       {
         const int i = l % m, b = l / m;
         T s = 0;
         for(int j = 0; j < m; ++j) s += ey[j * m + b] * w[j * m + i];
         r[l] = s / (ex[m * m + i] + ey[m * m + b]);
       }
-      __syncthreads();
-      for(int l = threadIdx.x; l < m2; l += blockDim.x)  // w = Sx along x
+      __syncwarp();
+      for(int l = lane; l < m2; l += 32)  // w = Sx along x
       {
         const int i = l % m, row = l - i;
         T s = 0;
         for(int j = 0; j < m; ++j) s += ex[i * m + j] * r[row + j];
         w[l] = s;
       }
-      __syncthreads();
-      for(int l = threadIdx.x; l < m2; l += blockDim.x)  // r = Sy along y
+      __syncwarp();
+      for(int l = lane; l < m2; l += 32)  // r = Sy along y
       {
         const int i = l % m, b = l / m;
         T s = 0;
         for(int j = 0; j < m; ++j) s += ey[b * m + j] * w[j * m + i];
         r[l] = s;
       }
-      __syncthreads();
-      for(int l = threadIdx.x; l < m2; l += blockDim.x) w[l] = r[l];
+      __syncwarp();
+      for(int l = lane; l < m2; l += 32) w[l] = r[l];
     }
-    __syncthreads();
-    for(int l = threadIdx.x; l < m2; l += blockDim.x)
-      a.dst[(int64_t)(y0 + l / m) * a.n + x0 + l % m] += a.omega * double(w[l]);
-    __syncthreads();
+    __syncwarp();
+    for(int l = lane; l < m2; l += 32) a.dst[(int64_t)(y0 + l / m) * a.n + x0 + l % m] += a.omega * double(w[l]);
+    __syncwarp();
   }
 }
 
@@ -575,7 +582,7 @@ void smooth(const tpss_c0ip &c, const C0ipLevel &L, double *dst, const double *s
   const bool dense = c.desc.local_solver == TPSS_LOCAL_EXACT;
   const bool f32 = c.desc.precision == TPSS_FP32;
   const int m2 = c.m * c.m;
-  const size_t smem = (f32 ? sizeof(float) : sizeof(double)) * 2 * m2;
+  const size_t smem = (f32 ? sizeof(float) : sizeof(double)) * 2 * m2 * 4;  // 4 warps
   for(int color = 0; color < 4; ++color)
   {
     const int64_t b = L.color_start[color], e = L.color_start[color + 1];
@@ -591,7 +598,7 @@ void smooth(const tpss_c0ip &c, const C0ipLevel &L, double *dst, const double *s
     a.m = c.m;
     a.n_patches = e - b;
     a.omega = c.desc.relaxation;
-    const unsigned grid = (unsigned)std::min<int64_t>(a.n_patches, (int64_t)num_sms() * 16);
+    const unsigned grid = (unsigned)std::min<int64_t>((a.n_patches + 3) / 4, (int64_t)num_sms() * 16);
     if(dense && f32)
       c0ip_patch_kernel<float, true><<<grid, 128, smem, s>>>(a);
     else if(dense)

@@ -612,6 +612,179 @@ extern "C" int tpss_mg_cg_solve(tpss_mg *mg, double *u, const double *f, double 
   });
 }
 
+// ---- batched solves: CG on many independent hierarchies in lockstep ------------------------
+// Every round enqueues one CG iteration (V-cycle graph, operator, device-side alpha / beta) for
+// every active problem, then synchronizes once and reads all residual norms; a problem leaves
+// the batch when it meets its ReductionControl tolerance (apps/rt_parameter.h:39-41).
+struct tpss_batch
+{
+  std::vector<tpss_mg *> mg;
+  std::vector<cudaStream_t> streams;
+  ~tpss_batch()
+  {
+    for(tpss_mg *m : mg) delete m;
+    for(cudaStream_t s : streams) cudaStreamDestroy(s);
+  }
+};
+
+namespace
+{
+struct CgRun
+{
+  double *u = nullptr;
+  double tol = 0.0;
+  int it = 0;
+  bool done = false, converged = false;
+};
+
+void cg_start(tpss_mg *mg, double *u, const double *f, cudaStream_t s)
+{
+  MgLevel &top = mg->lv.back();
+  const int64_t n = top.L->n_dofs;
+  TPSS_CUDA(cudaMemsetAsync(u, 0, sizeof(double) * n, s));
+  TPSS_CUDA(cudaMemcpyAsync(mg->r.ptr, f, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+  vec_dot(n, mg->r.ptr, mg->r.ptr, mg->partial.ptr, mg->scal.ptr + 10, s);
+  TPSS_CUDA(cudaMemcpyAsync(mg->h_scal + 4, mg->scal.ptr + 10, sizeof(double), cudaMemcpyDeviceToHost, s));
+}
+
+// z = V(r), then p = z (first) or p = z + (rz_new / rz) p; rz updated
+void cg_precondition(tpss_mg *mg, bool first, cudaStream_t s)
+{
+  MgLevel &top = mg->lv.back();
+  const int64_t n = top.L->n_dofs;
+  double *d_rz = mg->scal.ptr + 8, *d_rz_new = mg->scal.ptr + 11;
+  TPSS_CUDA(cudaMemcpyAsync(top.b.ptr, mg->r.ptr, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+  vcycle(mg, s);
+  if(first)
+  {
+    TPSS_CUDA(cudaMemcpyAsync(mg->p.ptr, top.x.ptr, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+    vec_dot(n, mg->r.ptr, top.x.ptr, mg->partial.ptr, d_rz, s);
+  }
+  else
+  {
+    vec_dot(n, mg->r.ptr, top.x.ptr, mg->partial.ptr, d_rz_new, s);
+    cg_update_p<<<grid_for(n), 256, 0, s>>>(n, mg->p.ptr, top.x.ptr, d_rz_new, d_rz);
+    TPSS_CUDA(cudaMemcpyAsync(d_rz, d_rz_new, sizeof(double), cudaMemcpyDeviceToDevice, s));
+  }
+}
+
+// x += alpha p, r -= alpha A p, |r|^2 copied to the pinned host slot
+void cg_iterate(tpss_mg *mg, double *u, cudaStream_t s)
+{
+  MgLevel &top = mg->lv.back();
+  const int64_t n = top.L->n_dofs;
+  double *d_rz = mg->scal.ptr + 8, *d_pAp = mg->scal.ptr + 9, *d_rr = mg->scal.ptr + 10;
+  operator_apply(top.op, mg->Ap.ptr, mg->p.ptr, s);
+  vec_dot(n, mg->p.ptr, mg->Ap.ptr, mg->partial.ptr, d_pAp, s);
+  cg_update_xr<<<grid_for(n), 256, 0, s>>>(n, u, mg->r.ptr, mg->p.ptr, mg->Ap.ptr, d_rz, d_pAp);
+  vec_dot(n, mg->r.ptr, mg->r.ptr, mg->partial.ptr, d_rr, s);
+  TPSS_CUDA(cudaMemcpyAsync(mg->h_scal + 4, d_rr, sizeof(double), cudaMemcpyDeviceToHost, s));
+}
+}  // namespace
+
+extern "C" int tpss_batch_create(const tpss_mg_desc *descs, int n_problems, int n_streams, tpss_batch **out)
+{
+  return guarded([&] {
+    TPSS_REQUIRE(descs && out && n_problems >= 1 && n_streams >= 1 && n_streams <= 64, "invalid argument");
+    *out = nullptr;
+    auto b = std::make_unique<tpss_batch>();
+    for(int i = 0; i < n_problems; ++i)
+    {
+      tpss_mg *m = nullptr;
+      const int rc = tpss_mg_create(&descs[i], &m);
+      if(rc) fail(rc, std::string("problem ") + std::to_string(i) + ": " + tpss_last_error());
+      b->mg.push_back(m);
+    }
+    for(int i = 0; i < n_streams; ++i)
+    {
+      cudaStream_t s;
+      TPSS_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+      b->streams.push_back(s);
+    }
+    *out = b.release();
+  });
+}
+
+extern "C" int tpss_batch_problem(tpss_batch *b, int i, tpss_mg **mg)
+{
+  return guarded([&] {
+    TPSS_REQUIRE(b && mg && i >= 0 && i < (int)b->mg.size(), "invalid argument");
+    *mg = b->mg[i];
+  });
+}
+
+extern "C" int tpss_batch_solve(tpss_batch *b, double *const *u, const double *const *f, double rel_tol,
+                                double abs_tol, int max_iter, int *iterations, void *stream)
+{
+  return guarded([&] {
+    TPSS_REQUIRE(b && u && f && iterations && max_iter >= 0, "invalid argument");
+    const int P = (int)b->mg.size(), S = (int)b->streams.size();
+    cudaStream_t caller = as_stream(stream);
+    cudaEvent_t ev;
+    TPSS_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    TPSS_CUDA(cudaEventRecord(ev, caller));
+    for(cudaStream_t s : b->streams) TPSS_CUDA(cudaStreamWaitEvent(s, ev, 0));
+    std::vector<CgRun> run(P);
+    auto sync_all = [&]() {
+      for(cudaStream_t s : b->streams) TPSS_CUDA(cudaStreamSynchronize(s));
+    };
+    for(int i = 0; i < P; ++i)
+    {
+      TPSS_REQUIRE(u[i] && f[i], "null problem vector");
+      run[i].u = u[i];
+      cg_start(b->mg[i], u[i], f[i], b->streams[i % S]);
+    }
+    sync_all();
+    int active = 0;
+    for(int i = 0; i < P; ++i)
+    {
+      const double r0 = std::sqrt(b->mg[i]->h_scal[4]);
+      run[i].tol = std::max(abs_tol, rel_tol * r0);
+      run[i].done = run[i].converged = r0 <= run[i].tol;
+      if(!run[i].done)
+      {
+        cg_precondition(b->mg[i], true, b->streams[i % S]);
+        ++active;
+      }
+    }
+    while(active > 0)
+    {
+      for(int i = 0; i < P; ++i)
+        if(!run[i].done) cg_iterate(b->mg[i], run[i].u, b->streams[i % S]);
+      sync_all();
+      for(int i = 0; i < P; ++i)
+      {
+        if(run[i].done) continue;
+        ++run[i].it;
+        const double res = std::sqrt(b->mg[i]->h_scal[4]);
+        if(res <= run[i].tol || run[i].it >= max_iter)
+        {
+          run[i].done = true;
+          run[i].converged = res <= run[i].tol;
+          --active;
+        }
+        else
+          cg_precondition(b->mg[i], false, b->streams[i % S]);
+      }
+    }
+    for(cudaStream_t s : b->streams)
+    {
+      TPSS_CUDA(cudaEventRecord(ev, s));
+      TPSS_CUDA(cudaStreamWaitEvent(caller, ev, 0));
+    }
+    cudaEventDestroy(ev);
+    bool all = true;
+    for(int i = 0; i < P; ++i)
+    {
+      iterations[i] = run[i].converged ? run[i].it : -1;
+      all = all && run[i].converged;
+    }
+    if(!all) fail(TPSS_ERR_NOT_CONVERGED, "some problems of the batch did not converge");
+  });
+}
+
+extern "C" void tpss_batch_destroy(tpss_batch *b) { delete b; }
+
 extern "C" void tpss_mg_destroy(tpss_mg *mg) { delete mg; }
 
 extern "C" int tpss_mg_relaxation(const tpss_mg *mg, int level, double *relaxation, double *lambda_max)
