@@ -8,6 +8,8 @@
 //   SchwarzPreconditioner      preconditioner/schwarz_preconditioner.h:88-588
 //   SchwarzSmoother            smoother/schwarz_smoother.h:16-52, smoother_richardson.h:14-163
 //   MultigridSolver            apps/poisson_problem.h:642-755 (GMG + CG)
+//   C0IPBiharmonic             apps/biharmonic_problem.h, biharmonic_integrator.h (C0IP path)
+//   MLP, BatchSolver           no counterpart: learned local solver network, lockstep batches
 // Vectors are device pointers to FP64 arrays; streams are cudaStream_t passed as void*.
 // Header-only; link with libtpss_gpu.so.
 #pragma once
@@ -15,6 +17,7 @@
 #include <memory>
 #include <stdexcept>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "tpss_gpu.h"
@@ -172,6 +175,8 @@ public:
     bool check_finite = false;
     int kernel_variant = TPSS_KERNEL_AUTO;
     int stream_variant = 0;
+    int local_solver = TPSS_LOCAL_FD;  // TPSS_LOCAL_FD / EXACT / KSUM / LEARNED
+    const tpss_mlp *model = nullptr;   // trained network for TPSS_LOCAL_LEARNED
   };
 
   SchwarzPreconditioner() = default;
@@ -217,6 +222,11 @@ public:
   {
     check(tpss_precond_Tvmult(handle_, dst, src, stream));
   }
+  /* dst and src in host memory (pinned for the copies to overlap the kernel) */
+  void vmult_host(double *dst, const double *src, void *stream = nullptr) const
+  {
+    check(tpss_precond_vmult_host(handle_, dst, src, stream));
+  }
 
   /* times the kernel variants on (src -> dst), keeps the fastest; returns its index */
   int autotune(double *dst, const double *src, int reps = 5, void *stream = nullptr)
@@ -258,6 +268,8 @@ private:
     d.check_finite = ad.check_finite;
     d.kernel_variant = ad.kernel_variant;
     d.stream_variant = ad.stream_variant;
+    d.local_solver = ad.local_solver;
+    d.model = ad.model;
     return d;
   }
 
@@ -332,8 +344,104 @@ public:
     return it;
   }
 
+  /* damping of level 1..L and the lambda_max(P A) estimate it was scaled by */
+  std::pair<double, double> relaxation(int level) const
+  {
+    double w = 0, lam = 0;
+    check(tpss_mg_relaxation(handle_, level, &w, &lam));
+    return {w, lam};
+  }
+  tpss_mg *handle() const { return handle_; }
+
 private:
   tpss_mg *handle_ = nullptr;
+};
+
+/* fully connected tanh network of the learned local solver, trained on the GPU */
+class MLP
+{
+public:
+  MLP(int n_in, int n_out, int n_hidden = 64, int n_hidden_layers = 3, uint64_t seed = 0)
+  {
+    tpss_mlp_desc d{n_in, n_hidden, n_hidden_layers, n_out, seed};
+    check(tpss_mlp_create(&d, &handle_));
+  }
+  MLP(const MLP &) = delete;
+  ~MLP() { tpss_mlp_destroy(handle_); }
+  /* x, target: device FP32 [rows][n_in], [rows][n_out]; returns the loss after every epoch */
+  std::vector<double> train(const float *x, const float *target, int64_t rows, int epochs, int batch = 256,
+                            double lr = 1e-3, uint64_t seed = 0, void *stream = nullptr)
+  {
+    std::vector<double> hist(epochs > 0 ? epochs : 1);
+    check(tpss_mlp_train(handle_, x, target, rows, epochs, batch, lr, seed, hist.data(), stream));
+    hist.resize(epochs);
+    return hist;
+  }
+  void forward(const float *x, int64_t rows, float *y, void *stream = nullptr)
+  {
+    check(tpss_mlp_forward(handle_, x, rows, y, stream));
+  }
+  const tpss_mlp *handle() const { return handle_; }
+
+private:
+  tpss_mlp *handle_ = nullptr;
+};
+
+/* clamped C0IP biharmonic hierarchy on the unit square (apps/biharmonic_problem.h) */
+class C0IPBiharmonic
+{
+public:
+  explicit C0IPBiharmonic(const tpss_c0ip_desc &d) { check(tpss_c0ip_create(&d, &handle_)); }
+  C0IPBiharmonic(const C0IPBiharmonic &) = delete;
+  ~C0IPBiharmonic() { tpss_c0ip_destroy(handle_); }
+  int64_t n_dofs(int level = -1) const
+  {
+    int64_t n = 0;
+    check(tpss_c0ip_info(handle_, level, &n, nullptr));
+    return n;
+  }
+  void vmult(double *dst, const double *src, int level = -1, void *stream = nullptr) const
+  {
+    check(tpss_c0ip_operator_vmult(handle_, level, dst, src, stream));
+  }
+  void smooth(double *dst, const double *src, int level = -1, void *stream = nullptr) const
+  {
+    check(tpss_c0ip_smoother_vmult(handle_, level, dst, src, stream));
+  }
+  int solve(double *u, const double *f, double rel_tol, double abs_tol = 1e-14, int max_iter = 200,
+            void *stream = nullptr) const
+  {
+    int it = 0;
+    check(tpss_c0ip_cg_solve(handle_, u, f, rel_tol, abs_tol, max_iter, &it, nullptr, stream));
+    return it;
+  }
+
+private:
+  tpss_c0ip *handle_ = nullptr;
+};
+
+/* many independent CG + GMG problems solved in lockstep */
+class BatchSolver
+{
+public:
+  BatchSolver(const std::vector<tpss_mg_desc> &problems, int n_streams = 8)
+  {
+    check(tpss_batch_create(problems.data(), (int)problems.size(), n_streams, &handle_));
+    n_ = (int)problems.size();
+  }
+  BatchSolver(const BatchSolver &) = delete;
+  ~BatchSolver() { tpss_batch_destroy(handle_); }
+  std::vector<int> solve(const std::vector<double *> &u, const std::vector<const double *> &f, double rel_tol,
+                         double abs_tol = 1e-14, int max_iter = 200, void *stream = nullptr)
+  {
+    std::vector<int> its(n_);
+    check(tpss_batch_solve(handle_, u.data(), f.data(), rel_tol, abs_tol, max_iter, its.data(), stream));
+    return its;
+  }
+
+private:
+  tpss_batch *handle_ = nullptr;
+  int n_ = 0;
 };
 
 }  // namespace tpss_gpu
