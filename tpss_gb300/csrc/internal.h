@@ -259,7 +259,7 @@ struct PendingEvent
 // copy / compute / copy pipeline of the host-buffer smoother entry point
 struct HostPipe
 {
-  cudaStream_t up = nullptr, comp = nullptr, down = nullptr;
+  cudaStream_t up = nullptr, comp = nullptr, comp2 = nullptr, down = nullptr;
   std::vector<cudaEvent_t> ev;
   DeviceBuffer<double> src, dst;
   cudaEvent_t event(size_t i)
@@ -277,6 +277,7 @@ struct HostPipe
     if(up) return;
     TPSS_CUDA(cudaStreamCreateWithFlags(&up, cudaStreamNonBlocking));
     TPSS_CUDA(cudaStreamCreateWithFlags(&comp, cudaStreamNonBlocking));
+    TPSS_CUDA(cudaStreamCreateWithFlags(&comp2, cudaStreamNonBlocking));
     TPSS_CUDA(cudaStreamCreateWithFlags(&down, cudaStreamNonBlocking));
   }
   HostPipe() = default;
@@ -284,7 +285,7 @@ struct HostPipe
   ~HostPipe()
   {
     for(cudaEvent_t e : ev) cudaEventDestroy(e);
-    for(cudaStream_t s : {up, comp, down})
+    for(cudaStream_t s : {up, comp, comp2, down})
       if(s) cudaStreamDestroy(s);
   }
 };

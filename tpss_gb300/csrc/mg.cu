@@ -200,6 +200,8 @@ struct tpss_mg
   double *h_scal = nullptr;  // pinned
   const double *E = nullptr;
   cudaGraphExec_t g_full = nullptr, g_down = nullptr, g_up = nullptr;
+  cudaGraphExec_t g_iter = nullptr;  // one lockstep CG iteration of a batch (ub, r, p, ...)
+  DeviceBuffer<double> ub;           // batch solution vector the iteration graph updates
   // graphs are captured on and launched into a private stream (capture is not possible on
   // the legacy default stream); events order it after / before the caller's stream
   cudaStream_t gstream = nullptr;
@@ -213,6 +215,7 @@ struct tpss_mg
     if(g_full) cudaGraphExecDestroy(g_full);
     if(g_down) cudaGraphExecDestroy(g_down);
     if(g_up) cudaGraphExecDestroy(g_up);
+    if(g_iter) cudaGraphExecDestroy(g_iter);
     for(auto &l : lv)
     {
       tpss_precond_destroy(l.P);
@@ -613,9 +616,10 @@ extern "C" int tpss_mg_cg_solve(tpss_mg *mg, double *u, const double *f, double 
 }
 
 // ---- batched solves: CG on many independent hierarchies in lockstep ------------------------
-// Every round enqueues one CG iteration (V-cycle graph, operator, device-side alpha / beta) for
-// every active problem, then synchronizes once and reads all residual norms; a problem leaves
-// the batch when it meets its ReductionControl tolerance (apps/rt_parameter.h:39-41).
+// Every round launches, for every active problem, one CUDA graph holding a whole CG iteration
+// (operator, device-side alpha / beta, the next V-cycle), then synchronizes once and reads all
+// residual norms; a problem leaves the batch when it meets its ReductionControl tolerance
+// (apps/rt_parameter.h:39-41).
 struct tpss_batch
 {
   std::vector<tpss_mg *> mg;
@@ -682,6 +686,32 @@ void cg_iterate(tpss_mg *mg, double *u, cudaStream_t s)
 }
 }  // namespace
 
+// one lockstep iteration: cg_iterate on ub, then the next preconditioning (run also after the
+// last iteration; it changes p and the V-cycle vectors only), captured into one graph with the
+// V-cycle's kernels inline. Capture after the first V-cycle: its lazy set-up (scratch, lists)
+// is done by then.
+void batch_iteration(tpss_mg *mg, cudaStream_t s)
+{
+  cg_iterate(mg, mg->ub.ptr, s);
+  cg_precondition(mg, false, s);
+}
+
+void capture_iteration(tpss_mg *mg)
+{
+  const int use_graph = mg->desc.use_graph;
+  mg->desc.use_graph = 0;  // V-cycle kernels inline in this graph
+  try
+  {
+    capture(mg, batch_iteration, &mg->g_iter);
+  }
+  catch(...)
+  {
+    mg->desc.use_graph = use_graph;
+    throw;
+  }
+  mg->desc.use_graph = use_graph;
+}
+
 extern "C" int tpss_batch_create(const tpss_mg_desc *descs, int n_problems, int n_streams, tpss_batch **out)
 {
   return guarded([&] {
@@ -731,8 +761,11 @@ extern "C" int tpss_batch_solve(tpss_batch *b, double *const *u, const double *c
     for(int i = 0; i < P; ++i)
     {
       TPSS_REQUIRE(u[i] && f[i], "null problem vector");
+      tpss_mg *m = b->mg[i];
+      const size_t n = (size_t)m->lv.back().L->n_dofs;
+      if(m->ub.n < n) m->ub.resize(n);
       run[i].u = u[i];
-      cg_start(b->mg[i], u[i], f[i], b->streams[i % S]);
+      cg_start(m, m->ub.ptr, f[i], b->streams[i % S]);
     }
     sync_all();
     int active = 0;
@@ -747,10 +780,14 @@ extern "C" int tpss_batch_solve(tpss_batch *b, double *const *u, const double *c
         ++active;
       }
     }
+    // iteration graphs (captured once per problem, after its first V-cycle above)
+    sync_all();
+    for(int i = 0; i < P; ++i)
+      if(!run[i].done && !b->mg[i]->g_iter) capture_iteration(b->mg[i]);
     while(active > 0)
     {
       for(int i = 0; i < P; ++i)
-        if(!run[i].done) cg_iterate(b->mg[i], run[i].u, b->streams[i % S]);
+        if(!run[i].done) TPSS_CUDA(cudaGraphLaunch(b->mg[i]->g_iter, b->streams[i % S]));
       sync_all();
       for(int i = 0; i < P; ++i)
       {
@@ -763,9 +800,13 @@ extern "C" int tpss_batch_solve(tpss_batch *b, double *const *u, const double *c
           run[i].converged = res <= run[i].tol;
           --active;
         }
-        else
-          cg_precondition(b->mg[i], false, b->streams[i % S]);
       }
+    }
+    for(int i = 0; i < P; ++i)
+    {
+      tpss_mg *m = b->mg[i];
+      TPSS_CUDA(cudaMemcpyAsync(run[i].u, m->ub.ptr, sizeof(double) * m->lv.back().L->n_dofs,
+                                cudaMemcpyDeviceToDevice, b->streams[i % S]));
     }
     for(cudaStream_t s : b->streams)
     {

@@ -118,7 +118,10 @@ void launch_fixup_range(const stream::StreamArgs &a, const int64_t *rec, int64_t
 
 // src and dst in host memory: the level is cut into chunks of z-items; per chunk the cell layers
 // it reads are copied in (stream up), its items are solved and the shared cells of the layers it
-// completes are summed (stream comp), and those finished layers are copied out (stream down)
+// completes are summed (compute streams, alternating between two so that a chunk's items fill
+// the SMs left idle by the previous chunk's last wave), and those finished layers are copied out
+// (stream down). The fix-up of chunk c also waits for chunk c - 1's items: the cell layer
+// between them holds partials of both.
 template<class C>
 bool launch_stream_host(const tpss_layout &L, const StreamLaunch &l0, HostPipe &pp, double *h_dst,
                         const double *h_src, cudaStream_t caller)
@@ -139,10 +142,12 @@ bool launch_stream_host(const tpss_layout &L, const StreamLaunch &l0, HostPipe &
   size_t e = 0;
   cudaEvent_t start = pp.event(e++);
   TPSS_CUDA(cudaEventRecord(start, caller));
-  for(cudaStream_t st : {pp.up, pp.comp, pp.down}) TPSS_CUDA(cudaStreamWaitEvent(st, start, 0));
-  int copied = 0, fixed = 0;
-  for(int z0 = 0; z0 < T2; z0 += per)
+  for(cudaStream_t st : {pp.up, pp.comp, pp.comp2, pp.down}) TPSS_CUDA(cudaStreamWaitEvent(st, start, 0));
+  int copied = 0, fixed = 0, chunk = 0;
+  cudaEvent_t prev_items = nullptr;
+  for(int z0 = 0; z0 < T2; z0 += per, ++chunk)
   {
+    cudaStream_t cs = (chunk % 2) ? pp.comp2 : pp.comp;
     const int z1 = std::min(T2, z0 + per);
     const bool last = z1 == T2;
     const int need = last ? nz : std::min(z1 * C::BZ + 1, nz);  // cell layers read so far
@@ -152,17 +157,21 @@ bool launch_stream_host(const tpss_layout &L, const StreamLaunch &l0, HostPipe &
     copied = need;
     cudaEvent_t up_done = pp.event(e++);
     TPSS_CUDA(cudaEventRecord(up_done, pp.up));
-    TPSS_CUDA(cudaStreamWaitEvent(pp.comp, up_done, 0));
+    TPSS_CUDA(cudaStreamWaitEvent(cs, up_done, 0));
     a.item_begin = (int)(z0 * items_per_z);
     a.item_end = (int)(z1 * items_per_z);
     const int64_t n_items = a.item_end - a.item_begin;
-    stream::stream_kernel<C><<<(int)std::min(n_items, cap), C::THREADS, C::smem_bytes(), pp.comp>>>(a);
+    stream::stream_kernel<C><<<(int)std::min(n_items, cap), C::THREADS, C::smem_bytes(), cs>>>(a);
     TPSS_CUDA(cudaGetLastError());
+    cudaEvent_t items_done = pp.event(e++);
+    TPSS_CUDA(cudaEventRecord(items_done, cs));
+    if(prev_items) TPSS_CUDA(cudaStreamWaitEvent(cs, prev_items, 0));
+    prev_items = items_done;
     const int bound = last ? nz : z1 * C::BZ;  // cell layers final after this chunk
-    launch_fixup_range<C>(a, l.fix_rec->ptr + ls[fixed] * stream::kFixRec, ls[bound] - ls[fixed], pp.comp);
+    launch_fixup_range<C>(a, l.fix_rec->ptr + ls[fixed] * stream::kFixRec, ls[bound] - ls[fixed], cs);
     TPSS_CUDA(cudaGetLastError());
     cudaEvent_t comp_done = pp.event(e++);
-    TPSS_CUDA(cudaEventRecord(comp_done, pp.comp));
+    TPSS_CUDA(cudaEventRecord(comp_done, cs));
     TPSS_CUDA(cudaStreamWaitEvent(pp.down, comp_done, 0));
     if(bound > fixed)
       TPSS_CUDA(cudaMemcpyAsync(h_dst + fixed * layer, pp.dst.ptr + fixed * layer,
