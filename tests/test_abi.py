@@ -117,3 +117,31 @@ def test_null_arguments_return_status(tpss):
     assert lib.tpss_precond_vmult(None, None, None, None) == 1
     n = C.c_int(0)
     assert lib.tpss_mg_n_levels(None, C.byref(n)) == 1
+
+
+def test_new_entry_points_reject_invalid_input_before_gpu_work(tpss):
+    """C0IP, network, batch and local-solver options are validated on the host first."""
+    with pytest.raises(tpss.TPSSInvalidArgument, match="degree"):
+        tpss.C0IPBiharmonic(1, 2, 8)
+    with pytest.raises(tpss.TPSSInvalidArgument, match="n_rep"):
+        tpss.C0IPBiharmonic(3, 1, 8)
+    with pytest.raises(tpss.TPSSInvalidArgument, match="n_rep"):
+        tpss.C0IPBiharmonic(3, 2, 12)
+    with pytest.raises(tpss.TPSSInvalidArgument, match="local_solver"):
+        tpss.C0IPBiharmonic(3, 2, 8, local_solver=2)
+    with pytest.raises(tpss.TPSSInvalidArgument, match="sizes"):
+        tpss.MLP(0, 4)
+    ad = tpss.SubdomainHandler.AdditionalData(dim=2, degree=1, n_cells=(3, 3), patch_variant=1)
+    sh = tpss.SubdomainHandler(ad)
+    p = tpss.SchwarzPreconditioner()
+    with pytest.raises(tpss.TPSSInvalidArgument, match="trained model"):
+        p.initialize(sh, None, tpss.SchwarzPreconditioner.AdditionalData(local_solver=3))
+    with pytest.raises(tpss.TPSSInvalidArgument, match="local solver"):
+        p.initialize(sh, None, tpss.SchwarzPreconditioner.AdditionalData(local_solver=7))
+    with pytest.raises(tpss.TPSSNotImplemented, match="RAS"):
+        p.initialize(sh, None, tpss.SchwarzPreconditioner.AdditionalData(local_solver=1, use_ras_weights=True))
+    lib = tpss.load()
+    h = C.c_void_p()
+    assert lib.tpss_batch_create(None, 0, 1, C.byref(h)) == 1
+    assert lib.tpss_precond_vmult_host(None, None, None, None) == 1
+    assert lib.tpss_c0ip_cg_solve(None, None, None, 1e-8, 1e-14, 10, None, None, None) == 1
