@@ -32,8 +32,9 @@ sys.path.insert(0, ROOT)
 METRIC = "smoother DoF/s (SchwarzPreconditioner::vmult; CG+MG solve s to 1e-8 rel. residual and FP32 vs FP64 in 'solve')"
 
 
-# (BX, BY, BZ, pencils per thread) of the streamed kernel's four work decompositions, for k = 4
-VARIANT_SHAPES = ["4,4,8,4", "4,4,8,5", "4,4,4,4", "4,4,16,4"]
+# (BX, BY, BZ, pencils per thread[, a warp per patch]) of the streamed kernel's six work
+# decompositions, for k = 4
+VARIANT_SHAPES = ["4,4,8,4", "4,4,8,5", "4,4,4,4", "4,4,16,4", "4,4,8,4,true", "4,4,4,4,true"]
 
 def parse():
     ap = argparse.ArgumentParser()

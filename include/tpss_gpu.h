@@ -136,7 +136,7 @@ typedef struct tpss_precond_desc
                                   (one fused launch per color) or TPSS_KERNEL_STREAM (3D vertex
                                   patches, FP32, k <= 4: column-streamed, one pass) */
   int stream_variant;          /* initial work decomposition of the column-streamed kernel
-                                  (0..3, see tpss_precond_autotune); 0 by default */
+                                  (0..5, see tpss_precond_autotune); 0 by default */
   int local_solver;            /* TPSS_LOCAL_*: how the patch inverses are formed */
   const tpss_mlp *model;       /* trained network for TPSS_LOCAL_LEARNED, else NULL */
 } tpss_precond_desc;
@@ -197,7 +197,7 @@ int tpss_precond_vmult_static_scratch(tpss_precond *p, double *dst, const double
  * kernel for this level (for the column-streamed kernel: pencils per thread and vertex layers per
  * work item) on the caller's vectors, `reps` applications each, and keeps the fastest for later
  * vmult calls.  On return dst = P src, *chosen is the selected variant, ms_per_variant (optional,
- * >= 4 entries) the measured milliseconds per application and *n_variants their count (1 when the
+ * >= 6 entries) the measured milliseconds per application and *n_variants their count (1 when the
  * level has a single kernel). */
 /* vmult with dst and src in HOST memory (the reference's vmult on host vectors; the adapter
  * in INTEGRATION copies in, applies and copies out). For the streamed smoother the copies are

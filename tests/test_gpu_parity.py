@@ -420,7 +420,7 @@ def test_streamed_variants_and_autotune(tpss, oracle, cuda, k, nc):
     ad = tpss.SubdomainHandler.AdditionalData(dim=3, degree=k, n_cells=nc, patch_variant=1)
     sh = tpss.SubdomainHandler(ad)
     s = torch.tensor(src, dtype=torch.float64, device=cuda)
-    for v in range(4):
+    for v in range(6):
         p = tpss.SchwarzPreconditioner()
         p.initialize(sh, None, tpss.SchwarzPreconditioner.AdditionalData(
             relaxation=0.15, precision=1, kernel_variant=2, stream_variant=v))
@@ -429,7 +429,7 @@ def test_streamed_variants_and_autotune(tpss, oracle, cuda, k, nc):
         assert rel_err(d.cpu().numpy(), ref) <= 2e-5, v
     d = torch.full_like(s, float("nan"))
     chosen, ms = p.autotune(d, s, reps=2)
-    assert 0 <= chosen < 4 and len(ms) == 4 and all(t > 0 for t in ms)
+    assert 0 <= chosen < 6 and len(ms) == 6 and all(t > 0 for t in ms)
     assert rel_err(d.cpu().numpy(), ref) <= 2e-5
     d2 = torch.empty_like(s)
     p.vmult(d2, s)

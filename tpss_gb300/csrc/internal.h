@@ -299,9 +299,9 @@ struct tpss_precond
   tpss::DeviceBuffer<double> residual;  // multiplicative scratch
   tpss::DeviceBuffer<int> flag;         // finiteness check
   tpss::DeviceBuffer<float> halo;       // streamed kernel: partial sums of shared cells
-  tpss::DeviceBuffer<int64_t> fix_rec[4];  // streamed kernel: shared-cell list per variant
-  int64_t fix_n[4] = {-1, -1, -1, -1};
-  std::vector<int64_t> fix_layer[4];
+  tpss::DeviceBuffer<int64_t> fix_rec[6];  // streamed kernel: shared-cell list per variant
+  int64_t fix_n[6] = {-1, -1, -1, -1, -1, -1};
+  std::vector<int64_t> fix_layer[6];
   tpss::HostPipe pipe;                  // host-buffer entry point
   int stream_variant = 0;               // streamed kernel variant (autotuner)
   std::vector<tpss::TimerSlot> timers;

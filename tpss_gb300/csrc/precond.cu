@@ -287,7 +287,7 @@ void validate_desc(const tpss_precond_desc &d)
 {
   TPSS_REQUIRE(d.kernel_variant >= TPSS_KERNEL_AUTO && d.kernel_variant <= TPSS_KERNEL_STREAM,
                "invalid kernel variant");
-  TPSS_REQUIRE(d.stream_variant >= 0 && d.stream_variant <= 3, "stream_variant must be in 0..3");
+  TPSS_REQUIRE(d.stream_variant >= 0 && d.stream_variant <= 5, "stream_variant must be in 0..5");
   TPSS_REQUIRE(d.relaxation > 0.0, "Invalid relaxation factor.");
   TPSS_REQUIRE(d.precision == TPSS_FP64 || d.precision == TPSS_FP32, "invalid precision");
   TPSS_REQUIRE(d.local_solver >= TPSS_LOCAL_FD && d.local_solver <= TPSS_LOCAL_LEARNED,

@@ -221,7 +221,9 @@ bool stream_supported(const tpss_layout &L)
 //   1: 4x4 columns, 8 layers, 5 (k = 4) or 2 (k <= 3) pencils per thread
 //   2: 4x4 columns, 4 layers per item (more items, more z-shared layers)
 //   3: 4x4 columns, 16 layers per item (fewer items, fewer z-shared layers)
-int stream_variant_count(const tpss_layout &L) { return stream_supported(L) ? 4 : 0; }
+//   4: as 0 with a whole warp per patch (no two patches' pencils in one warp)
+//   5: as 2 with a whole warp per patch
+int stream_variant_count(const tpss_layout &L) { return stream_supported(L) ? 6 : 0; }
 
 template<int K1, int V>
 struct VariantCfg;
@@ -245,6 +247,19 @@ struct VariantCfg<K1, 3>
 {
   using type = stream::SCfg<K1, 4, 4, 16, 4>;
 };
+// pencils per thread that fill most of a warp with one patch: (2 (k+1))^2 / NPT <= 32
+template<int K1>
+constexpr int npt_warp() { return K1 == 5 ? 4 : K1 == 4 ? 2 : K1 == 3 ? 2 : 1; }
+template<int K1>
+struct VariantCfg<K1, 4>
+{
+  using type = stream::SCfg<K1, 4, 4, 8, npt_warp<K1>(), true>;
+};
+template<int K1>
+struct VariantCfg<K1, 5>
+{
+  using type = stream::SCfg<K1, 4, 4, 4, npt_warp<K1>(), true>;
+};
 
 template<int K1>
 bool launch_variant(const tpss_layout &L, const StreamLaunch &l, cudaStream_t s, int v)
@@ -255,6 +270,8 @@ bool launch_variant(const tpss_layout &L, const StreamLaunch &l, cudaStream_t s,
   case 1: return launch_stream<typename VariantCfg<K1, 1>::type>(L, l, s);
   case 2: return launch_stream<typename VariantCfg<K1, 2>::type>(L, l, s);
   case 3: return launch_stream<typename VariantCfg<K1, 3>::type>(L, l, s);
+  case 4: return launch_stream<typename VariantCfg<K1, 4>::type>(L, l, s);
+  case 5: return launch_stream<typename VariantCfg<K1, 5>::type>(L, l, s);
   default: return false;
   }
 }
@@ -269,6 +286,8 @@ bool launch_variant_host(const tpss_layout &L, const StreamLaunch &l, HostPipe &
   case 1: return launch_stream_host<typename VariantCfg<K1, 1>::type>(L, l, pp, h_dst, h_src, s);
   case 2: return launch_stream_host<typename VariantCfg<K1, 2>::type>(L, l, pp, h_dst, h_src, s);
   case 3: return launch_stream_host<typename VariantCfg<K1, 3>::type>(L, l, pp, h_dst, h_src, s);
+  case 4: return launch_stream_host<typename VariantCfg<K1, 4>::type>(L, l, pp, h_dst, h_src, s);
+  case 5: return launch_stream_host<typename VariantCfg<K1, 5>::type>(L, l, pp, h_dst, h_src, s);
   default: return false;
   }
 }

@@ -31,10 +31,11 @@ namespace stream
 using fd::cpow;
 using fd::Entry;
 
-template<int K1_, int BX_, int BY_, int BZ_, int NPT_>
+template<int K1_, int BX_, int BY_, int BZ_, int NPT_, bool WARP_PER_PATCH_ = false>
 struct SCfg
 {
   static constexpr int K1 = K1_, BX = BX_, BY = BY_, BZ = BZ_, NPT = NPT_;
+  static constexpr bool WARP_PER_PATCH = WARP_PER_PATCH_;
   static constexpr int N = 2 * K1;
   static constexpr int NLOC = N * N * N;
   static constexpr int NPENCIL = N * N;
@@ -42,7 +43,12 @@ struct SCfg
   static constexpr int TPP = NPENCIL / NPT;  // threads per patch
   static constexpr int CD = K1 * K1 * K1;     // DoFs per cell
   static constexpr int NPATCH = BX * BY;      // patches per vertex layer
-  static constexpr int THREADS = NPATCH * TPP;
+  // lanes per patch slot: TPP, or a whole warp per patch (lanes >= TPP idle in the FD passes),
+  // which keeps one patch's pencils alone in a warp and their shared-memory accesses in
+  // distinct banks
+  static_assert(!WARP_PER_PATCH_ || TPP <= 32, "a warp per patch needs TPP <= 32");
+  static constexpr int LPP = WARP_PER_PATCH_ ? 32 : TPP;
+  static constexpr int THREADS = NPATCH * LPP;
   static constexpr int CX = BX + 1, CY = BY + 1;
   static constexpr int LCELLS = CX * CY;  // cells per cell layer of a column
   static constexpr int LAYER = LCELLS * CD;
@@ -59,7 +65,9 @@ struct SCfg
   // distinct shared-memory banks in all three directions (at most 2-way conflicts)
   static constexpr int SX = N == 10 ? 13 : N == 8 ? 9 : N == 6 ? 6 : N == 4 ? 5 : N;
   static constexpr int SXY = N == 10 ? 137 : N == 8 ? 72 : N == 6 ? 39 : N == 4 ? 21 : N * N;
-  static constexpr int PSTRIDE = SXY * N;  // floats per patch work buffer
+  // floats per patch work buffer; for N = 8 two patches share a warp (TPP 16) and a stride of
+  // 576 = 0 mod 32 would put them on the same banks, so it is shifted by half a bank row
+  static constexpr int PSTRIDE = SXY * N + (N == 8 && !WARP_PER_PATCH_ && TPP == 16 ? 16 : 0);
   // element loops give every thread one fixed cell-local DoF e (no div/mod per element)
   static constexpr int G = THREADS / CD;   // thread groups sharing an e
   static_assert(G >= 1, "need at least one thread per cell DoF");
@@ -460,7 +468,7 @@ __global__ void __launch_bounds__(C::THREADS, 1) stream_kernel(StreamArgs a)
   float *s_acc = sm + C::OFF_ACC;
   float *s_work = sm + C::OFF_WORK;
   const int tid = threadIdx.x;
-  const int slot = tid / TPP, q = tid % TPP;  // FD passes: patch slot (px + BX py), pencil group
+  const int slot = tid / C::LPP, q = tid % C::LPP;  // FD passes: patch slot (px + BX py), pencil group
   const int px = slot % BX, py = slot / BX;
   // element loops: fixed cell-local DoF e and its patch-local offset
   const int e = tid % CD, g = tid / CD;
@@ -504,7 +512,7 @@ __global__ void __launch_bounds__(C::THREADS, 1) stream_kernel(StreamArgs a)
       const bool more = j + 2 <= bz;
       if(more) copy_layer_async<C>(a, x0, y0, bx, by, z0 + j + 2, s_raw + ((j + 2) % 3) * C::LAYER, e, g);
       const double *lo = s_raw + (j % 3) * C::LAYER, *hi = s_raw + ((j + 1) % 3) * C::LAYER;
-      const bool active = px < bx && py < by;
+      const bool active = px < bx && py < by && q < TPP;
       float *my = s_work + slot * PS;
       constexpr int ESL = C::ESLOT, HP = C::HPAD;
       const float *ex = s_fd + px * ESL, *ey = s_fd + (BX + py) * ESL, *ez = s_fd + (BX + BY + j) * ESL;
