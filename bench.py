@@ -153,7 +153,7 @@ def measured_peaks():
 
 
 def ncu_traffic(dim, k):
-    """DRAM bytes per launch of the FD color kernel from the committed ncu summary."""
+    """DRAM bytes per launch of the streamed kernel at 64^3 cells from the committed ncu summary."""
     path = os.path.join(ROOT, "profiles", f"stream_kernel_{dim}d_k{k}_48cubed.md")
     if not os.path.exists(path):
         return None
@@ -317,6 +317,10 @@ def run_ours(args):
     achieved_gbs = bytes_launch / per_launch / 1e9
     achieved_tf = flops_launch / per_launch / 1e12
     traffic = ncu_traffic(dim, k) if streamed else None
+    if traffic is not None:
+        # the committed figure is for 64^3 cells (scaled from a 48^3 capture by DoFs); traffic
+        # grows with the DoFs of the level
+        traffic *= W["N"] / (64 ** 3 * (k + 1) ** 3)
     roofline = {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
                 "frac": achieved_gbs / hbm_peak, "traffic": traffic,
                 "peak_source": f"{hbm_kind} (MEASURED_PEAKS.json hbm_gbs)",
