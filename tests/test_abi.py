@@ -145,3 +145,23 @@ def test_new_entry_points_reject_invalid_input_before_gpu_work(tpss):
     assert lib.tpss_batch_create(None, 0, 1, C.byref(h)) == 1
     assert lib.tpss_precond_vmult_host(None, None, None, None) == 1
     assert lib.tpss_c0ip_cg_solve(None, None, None, 1e-8, 1e-14, 10, None, None, None) == 1
+
+
+def test_ctypes_descriptors_match_the_c_structs(tpss):
+    """Field lists of the Python descriptors equal the C struct members (names, in order)."""
+    src = open(os.path.join(ROOT, "include", "tpss_gpu.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    from tpss_gb300 import _lib
+    for cname, pyname in (("tpss_layout_desc", "LayoutDesc"), ("tpss_precond_desc", "PrecondDesc"),
+                          ("tpss_mg_desc", "MgDesc"), ("tpss_c0ip_desc", "C0ipDesc"),
+                          ("tpss_mlp_desc", "MlpDesc")):
+        body = re.search(r"typedef struct %s\s*\{(.*?)\}\s*%s;" % (cname, cname), src, flags=re.S).group(1)
+        names = []
+        for decl in body.split(";"):
+            decl = decl.strip()
+            if not decl:
+                continue
+            for part in decl.split(","):
+                m = re.search(r"(\w+)\s*(\[\d+\])?\s*$", part.strip())
+                names.append(m.group(1))
+        assert [f[0] for f in getattr(_lib, pyname)._fields_] == names, cname

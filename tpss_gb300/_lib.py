@@ -58,8 +58,7 @@ class LayoutDesc(C.Structure):
                 ("patch_variant", C.c_int), ("smoother_variant", C.c_int),
                 ("n_cells", C.c_int * 3), ("cell_h", C.POINTER(C.c_double) * 3),
                 ("cell_dof_start", C.POINTER(C.c_int64)), ("patch_color", C.POINTER(C.c_int32)),
-                ("vertex_coords", C.POINTER(C.c_double)), ("surrogate_n_q", C.c_int),
-                ("local_solver", C.c_int), ("model", C.c_void_p), ("auto_relaxation", C.c_int)]
+                ("vertex_coords", C.POINTER(C.c_double)), ("surrogate_n_q", C.c_int)]
 
 
 class PrecondDesc(C.Structure):
