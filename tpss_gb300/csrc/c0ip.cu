@@ -10,8 +10,9 @@
 // Nodes: FE_Q Lagrange basis on Gauss-Lobatto points; u = 0 on boundary nodes; vectors hold
 // the (n k - 1)^2 interior nodes, x fastest.
 //
-// GB300 mapping: every 1-D matrix is banded (half bandwidth 2k), so the operator is two FP64
-// passes over the node grid (x then y), HBM-bound. A vertex patch holds the (2k-1)^2 nodes
+// GB300 mapping: every 1-D matrix is banded (half bandwidth 2k; also on the host, so set-up
+// memory grows linearly with the mesh), and the operator is two FP64 passes over the node grid
+// (x then y). A vertex patch holds the (2k-1)^2 nodes
 // strictly inside its 2 x 2 cells; patches of one color (vertex parity) are disjoint, so the
 // smoother is one kernel per color: a CTA gathers a patch into shared memory, applies the
 // local inverse and scatter-adds the damped result. Local solvers (the reference's
@@ -84,15 +85,32 @@ Poly1D make_poly(int k)
   return p;
 }
 
-// dense 1-D matrices (M, L, B) on nc uniform cells, all nc k + 1 nodes
-void global_1d(const Poly1D &p, int nc, double ip, std::vector<double> &M, std::vector<double> &L,
-               std::vector<double> &B)
+// banded 1-D matrix over all nodes: entry (i, j), |i - j| <= bw, at i (2 bw + 1) + j - i + bw
+struct Band1D
+{
+  int n = 0, bw = 0;
+  std::vector<double> v;
+  void init(int n_, int bw_)
+  {
+    n = n_;
+    bw = bw_;
+    v.assign((size_t)n * (2 * bw + 1), 0.0);
+  }
+  double &at(int i, int j) { return v[(size_t)i * (2 * bw + 1) + (j - i + bw)]; }
+  double get(int i, int j) const
+  {
+    return (j - i > bw || i - j > bw) ? 0.0 : v[(size_t)i * (2 * bw + 1) + (j - i + bw)];
+  }
+};
+
+// 1-D matrices (M, L, B) on nc uniform cells, all nc k + 1 nodes, half bandwidth 2k
+void global_1d(const Poly1D &p, int nc, double ip, Band1D &M, Band1D &L, Band1D &B)
 {
   const int k = p.k, np = k + 1, n = nc * k + 1;
   const double h = 1.0 / nc, gamma = k == 0 ? 1.0 : k * (k + 1.0);
-  M.assign((size_t)n * n, 0.0);
-  L = M;
-  B = M;
+  M.init(n, 2 * k);
+  L.init(n, 2 * k);
+  B.init(n, 2 * k);
   for(int c = 0; c < nc; ++c)
     for(int i = 0; i < np; ++i)
       for(int j = 0; j < np; ++j)
@@ -105,10 +123,9 @@ void global_1d(const Poly1D &p, int nc, double ip, std::vector<double> &M, std::
           l += w * p.d1[i * np + q] * p.d1[j * np + q] / (h * h);
           b += w * p.d2[i * np + q] * p.d2[j * np + q] / (h * h * h * h);
         }
-        const size_t at = (size_t)(c * k + i) * n + c * k + j;
-        M[at] += m;
-        L[at] += l;
-        B[at] += b;
+        M.at(c * k + i, c * k + j) += m;
+        L.at(c * k + i, c * k + j) += l;
+        B.at(c * k + i, c * k + j) += b;
       }
   // interior nodes: cell c (0, its right end) and c + 1 (1, its left end), normal +1
   for(int c = 0; c + 1 < nc; ++c)
@@ -127,8 +144,7 @@ void global_1d(const Poly1D &p, int nc, double ip, std::vector<double> &M, std::
     const double sig = ip * gamma * (2.0 / h) / 2.0;
     for(int a = 0; a < 2 * np; ++a)
       for(int b = 0; b < 2 * np; ++b)
-        B[(size_t)idx[a] * n + idx[b]] +=
-          -avg[a] * jump[b] - jump[a] * avg[b] + sig * jump[a] * jump[b];
+        B.at(idx[a], idx[b]) += -avg[a] * jump[b] - jump[a] * avg[b] + sig * jump[a] * jump[b];
   }
   // boundary nodes, outward normal
   for(int e = 0; e < 2; ++e)
@@ -141,13 +157,13 @@ void global_1d(const Poly1D &p, int nc, double ip, std::vector<double> &M, std::
       {
         const double ja = nrm * p.e1[side][a] / h, jb = nrm * p.e1[side][b] / h;
         const double aa = p.e2[side][a] / (h * h), ab = p.e2[side][b] / (h * h);
-        B[(size_t)(c * k + a) * n + c * k + b] += -aa * jb - ja * ab + sig * ja * jb;
+        B.at(c * k + a, c * k + b) += -aa * jb - ja * ab + sig * ja * jb;
       }
   }
 }
 
-// interior-node rows of a dense 1-D matrix as a band of half width bw: [row][2 bw + 1]
-std::vector<double> to_band(const std::vector<double> &A, int n_all, int bw)
+// interior-node rows of a 1-D matrix as a band of half width bw: [row][2 bw + 1]
+std::vector<double> to_band(const Band1D &A, int n_all, int bw)
 {
   const int n = n_all - 2, w = 2 * bw + 1;
   std::vector<double> out((size_t)n * w, 0.0);
@@ -156,17 +172,17 @@ std::vector<double> to_band(const std::vector<double> &A, int n_all, int bw)
     {
       const int j = i + o;
       if(j < 0 || j >= n) continue;
-      out[(size_t)i * w + o + bw] = A[(size_t)(i + 1) * n_all + j + 1];
+      out[(size_t)i * w + o + bw] = A.get(i + 1, j + 1);
     }
   return out;
 }
 
-// interior submatrix [x0, x0 + m) of a dense 1-D matrix (interior-node numbering)
-std::vector<double> sub_1d(const std::vector<double> &A, int n_all, int x0, int m)
+// interior submatrix [x0, x0 + m) of a 1-D matrix (interior-node numbering), dense
+std::vector<double> sub_1d(const Band1D &A, int x0, int m)
 {
   std::vector<double> out((size_t)m * m);
   for(int a = 0; a < m; ++a)
-    for(int b = 0; b < m; ++b) out[(size_t)a * m + b] = A[(size_t)(x0 + a + 1) * n_all + x0 + b + 1];
+    for(int b = 0; b < m; ++b) out[(size_t)a * m + b] = A.get(x0 + a + 1, x0 + b + 1);
   return out;
 }
 }  // namespace
@@ -423,7 +439,7 @@ void build_level(tpss_c0ip &c, C0ipLevel &L, const Poly1D &poly, int nc)
   const int k = d.degree, m = c.m, na = nc * k + 1, bw = c.bw;
   L.nc = nc;
   L.n = nc * k - 1;
-  std::vector<double> M, Lm, B;
+  Band1D M, Lm, B;
   global_1d(poly, nc, d.ip_factor, M, Lm, B);
   L.bandM.upload(to_band(M, na, bw).data(), (size_t)L.n * (2 * bw + 1));
   L.bandL.upload(to_band(Lm, na, bw).data(), (size_t)L.n * (2 * bw + 1));
@@ -474,10 +490,10 @@ void build_level(tpss_c0ip &c, C0ipLevel &L, const Poly1D &poly, int nc)
       {
         const int vx = rep(kx), vy = rep(ky);
         if(vx < 0 || vy < 0) continue;
-        const auto Mx = sub_1d(M, na, (vx - 1) * k, m), Lx = sub_1d(Lm, na, (vx - 1) * k, m),
-                   Bx = sub_1d(B, na, (vx - 1) * k, m);
-        const auto My = sub_1d(M, na, (vy - 1) * k, m), Ly = sub_1d(Lm, na, (vy - 1) * k, m),
-                   By = sub_1d(B, na, (vy - 1) * k, m);
+        const auto Mx = sub_1d(M, (vx - 1) * k, m), Lx = sub_1d(Lm, (vx - 1) * k, m),
+                   Bx = sub_1d(B, (vx - 1) * k, m);
+        const auto My = sub_1d(M, (vy - 1) * k, m), Ly = sub_1d(Lm, (vy - 1) * k, m),
+                   By = sub_1d(B, (vy - 1) * k, m);
         std::vector<double> K((size_t)m2 * m2);
         for(int b = 0; b < m; ++b)
           for(int a = 0; a < m; ++a)
@@ -498,7 +514,7 @@ void build_level(tpss_c0ip &c, C0ipLevel &L, const Poly1D &poly, int nc)
     for(int kk = 0; kk < 4; ++kk)
     {
       const int v = rep(kk) > 0 ? rep(kk) : 1;
-      const auto Mk = sub_1d(M, na, (v - 1) * k, m), Bk = sub_1d(B, na, (v - 1) * k, m);
+      const auto Mk = sub_1d(M, (v - 1) * k, m), Bk = sub_1d(B, (v - 1) * k, m);
       std::copy(Mk.begin(), Mk.end(), &Ms[(size_t)kk * m * m]);
       std::copy(Bk.begin(), Bk.end(), &As[(size_t)kk * m * m]);
     }
@@ -718,7 +734,7 @@ extern "C" int tpss_c0ip_create(const tpss_c0ip_desc *d, tpss_c0ip **out)
     {
       const int nc0 = d->n_rep, na = nc0 * d->degree + 1, n0 = nc0 * d->degree - 1, N0 = n0 * n0;
       TPSS_REQUIRE(N0 <= 4096, "C0IP: coarse level too large for the dense solve");
-      std::vector<double> M, Lm, B;
+      Band1D M, Lm, B;
       global_1d(poly, nc0, d->ip_factor, M, Lm, B);
       std::vector<double> A((size_t)N0 * N0);
       for(int y = 0; y < n0; ++y)
@@ -726,7 +742,7 @@ extern "C" int tpss_c0ip_create(const tpss_c0ip_desc *d, tpss_c0ip **out)
           for(int y2 = 0; y2 < n0; ++y2)
             for(int x2 = 0; x2 < n0; ++x2)
             {
-              auto at = [&](const std::vector<double> &X, int i, int j) { return X[(size_t)(i + 1) * na + j + 1]; };
+              auto at = [&](const Band1D &X, int i, int j) { return X.get(i + 1, j + 1); };
               A[(size_t)(y * n0 + x) * N0 + y2 * n0 + x2] = at(M, y, y2) * at(B, x, x2) +
                                                             2.0 * at(Lm, y, y2) * at(Lm, x, x2) +
                                                             at(B, y, y2) * at(M, x, x2);

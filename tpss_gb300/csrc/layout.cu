@@ -28,17 +28,21 @@ thread_local std::string g_last_error;
 void set_last_error(const std::string &msg) { g_last_error = msg; }
 const char *last_error_cstr() { return g_last_error.c_str(); }
 
+// SM count of the current device (queried once per device)
 int num_sms()
 {
-  static int sms = 0;
-  static std::once_flag once;
-  std::call_once(once, [] {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if(sms <= 0) sms = 1;
-  });
-  return sms;
+  static std::mutex mu;
+  static int sms[64] = {0};
+  int dev = 0;
+  if(cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 1;
+  std::lock_guard<std::mutex> lock(mu);
+  if(sms[dev] == 0)
+  {
+    int n = 0;
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    sms[dev] = n > 0 ? n : 1;
+  }
+  return sms[dev];
 }
 
 namespace

@@ -14,6 +14,8 @@
 // the 2^dim children (1-D embedding matrices E_0, E_1), restriction is its transpose.
 #include <mutex>
 
+#include <map>
+
 #include "internal.h"
 
 namespace tpss
@@ -498,21 +500,26 @@ extern "C" void tpss_operator_destroy(tpss_operator *op) { delete op; }
 
 namespace
 {
+// child-embedding table of degree k on the current device (one copy per device and degree,
+// kept for the lifetime of the process)
 const double *embedding_device(int k)
 {
   static std::mutex mu;
-  static double *tables[9] = {nullptr};
+  static std::map<std::pair<int, int>, double *> tables;
+  int dev = 0;
+  TPSS_CUDA(cudaGetDevice(&dev));
   std::lock_guard<std::mutex> lock(mu);
-  if(!tables[k])
+  double *&t = tables[{dev, k}];
+  if(!t)
   {
     const Shape1D s = make_shape_1d(k);
     const std::vector<double> E = embedding_1d(s);
     double *d = nullptr;
     TPSS_CUDA(cudaMalloc(&d, E.size() * sizeof(double)));
     TPSS_CUDA(cudaMemcpy(d, E.data(), E.size() * sizeof(double), cudaMemcpyHostToDevice));
-    tables[k] = d;  // kept for the lifetime of the process
+    t = d;
   }
-  return tables[k];
+  return t;
 }
 }  // namespace
 

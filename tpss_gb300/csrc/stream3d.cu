@@ -94,17 +94,23 @@ stream::StreamArgs make_args(const tpss_layout &L, const StreamLaunch &l)
 template<class C>
 int64_t stream_cap()
 {
-  static int per_sm = 0;
-  if(per_sm == 0)
+  // the shared-memory attribute and the occupancy are set / queried once per device
+  static std::mutex mu;
+  static int per_sm[64] = {0};
+  int dev = 0;
+  TPSS_CUDA(cudaGetDevice(&dev));
+  TPSS_REQUIRE(dev >= 0 && dev < 64, "device ordinal out of range");
+  std::lock_guard<std::mutex> lock(mu);
+  if(per_sm[dev] == 0)
   {
     TPSS_CUDA(cudaFuncSetAttribute(stream::stream_kernel<C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)C::smem_bytes()));
     int occ = 0;
     TPSS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, stream::stream_kernel<C>, C::THREADS,
                                                             C::smem_bytes()));
-    per_sm = occ < 1 ? 1 : occ;
+    per_sm[dev] = occ < 1 ? 1 : occ;
   }
-  return (int64_t)num_sms() * per_sm;
+  return (int64_t)num_sms() * per_sm[dev];
 }
 
 template<class C>
@@ -397,17 +403,8 @@ void launch_stream_static(const tpss_layout &L, const tpss_precond &p, const dou
            std::to_string(halo_floats) + " floats, the static scratch holds " +
            std::to_string(kStaticHaloFloats) + " (32 MiB)");
   a.halo = static_halo_address();
-  static int per_sm = 0;
   const size_t smem = C::smem_bytes();
-  if(per_sm == 0)
-  {
-    TPSS_CUDA(cudaFuncSetAttribute(stream::stream_kernel<C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)smem));
-    int occ = 0;
-    TPSS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, stream::stream_kernel<C>, C::THREADS, smem));
-    per_sm = occ < 1 ? 1 : occ;
-  }
-  const int64_t cap = (int64_t)num_sms() * per_sm;
+  const int64_t cap = stream_cap<C>();
   const int grid = (int)(n_items < cap ? n_items : cap);
   stream::stream_kernel<C><<<grid, C::THREADS, smem, s>>>(a);
   TPSS_CUDA(cudaGetLastError());
