@@ -77,7 +77,12 @@ struct SCfg
   static constexpr int OFF_RAW = ((OFF_SYM + (BX + BY + BZ) + 3) / 4) * 4;  // 3 FP64 layers
   static constexpr int OFF_ACC = OFF_RAW + 3 * 2 * LAYER;            // 2 FP32 layers
   static constexpr int OFF_WORK = OFF_ACC + 2 * LAYER;               // NPATCH patches
-  static constexpr int FLOATS = OFF_WORK + NPATCH * PSTRIDE;
+  // per-item cell tables (ints): global xy index of each column cell (-1 outside the item),
+  // its x/y-shared flag, and for each of the 2 LCELLS accumulator cells the offsets of the (up
+  // to) 4 patches of a vertex layer that touch it (-1: none)
+  static constexpr int OFF_TAB = ((OFF_WORK + NPATCH * PSTRIDE + 3) / 4) * 4;
+  static constexpr int OFF_AOFF = OFF_TAB + ((2 * LCELLS + 3) / 4) * 4;  // int4 aligned
+  static constexpr int FLOATS = OFF_AOFF + 8 * LCELLS;
   static constexpr size_t smem_bytes() { return (size_t)FLOATS * 4; }
 };
 
@@ -395,27 +400,28 @@ __device__ __forceinline__ void mpass_divide(float *__restrict__ data, const flo
   }
 }
 
+// first DoF of the cell with lexicographic index xy + nx ny cz
 template<class C>
-__device__ __forceinline__ int64_t cell_first(const StreamArgs &a, int cx, int cy, int cz)
+__device__ __forceinline__ int64_t cell_first_xy(const StreamArgs &a, int xy, int cz)
 {
-  const int64_t cell = cx + (int64_t)a.nc[0] * (cy + (int64_t)a.nc[1] * cz);
+  const int64_t cell = xy + (int64_t)a.nc[0] * a.nc[1] * cz;
   return a.cell_start ? a.cell_start[cell] : cell * C::CD;
 }
 
-// asynchronous copy (cp.async, 8 bytes) of cell layer cz of the column (cells x in
-// [x0, x0+bx], y in [y0, y0+by]) into the FP64 staging buffer; cells outside are zero-filled
+// asynchronous copy (cp.async, 8 bytes) of cell layer cz of the column (the item's cells of
+// the table cxy) into the FP64 staging buffer; cells outside are zero-filled
 template<class C>
-__device__ __forceinline__ void copy_layer_async(const StreamArgs &a, int x0, int y0, int bx, int by,
-                                                 int cz, double *raw, int e, int g)
+__device__ __forceinline__ void copy_layer_async(const StreamArgs &a, const int *cxy, int cz, double *raw,
+                                                 int e, int g)
 {
   if(g < C::G)
     for(int cell = g; cell < C::LCELLS; cell += C::G)
     {
-      const int lx = cell % C::CX, ly = cell / C::CX;
+      const int xy = cxy[cell];
       const int i = cell * C::CD + e;
-      if(lx <= bx && ly <= by)
+      if(xy >= 0)
       {
-        const double *src = a.src + cell_first<C>(a, x0 + lx, y0 + ly, cz) + e;
+        const double *src = a.src + cell_first_xy<C>(a, xy, cz) + e;
         const unsigned saddr = (unsigned)__cvta_generic_to_shared(raw + i);
         asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(saddr), "l"(src) : "memory");
       }
@@ -430,26 +436,26 @@ __device__ __forceinline__ void wait_async_all() { asm volatile("cp.async.wait_g
 // write one completed cell layer: cells owned by the item to dst, shared cells to the halo
 template<class C>
 __device__ __forceinline__ void write_layer(const StreamArgs &a, float *accl, int item, int lz, int cz,
-                                            bool zshared, int tx, int ty, int x0, int y0, int bx,
-                                            int by, int e, int g, bool clear)
+                                            bool zshared, const int *cxy, const int *cshared, int e,
+                                            int g, bool clear)
 {
   if(g >= C::G) return;
   for(int cell = g; cell < C::LCELLS; cell += C::G)
   {
-    const int lx = cell % C::CX, ly = cell / C::CX;
-    if(lx > bx || ly > by) continue;
+    const int xy = cxy[cell];
+    if(xy < 0) continue;
     const int i = cell * C::CD + e;
-    const bool xs = (lx == 0 && tx > 0) || (lx == bx && tx < a.T[0] - 1);
-    const bool ys = (ly == 0 && ty > 0) || (ly == by && ty < a.T[1] - 1);
     float v = accl[i];
-    if(xs || ys || zshared)
+    if(cshared[cell] || zshared)
       a.halo[((size_t)item * (C::BZ + 1) * C::LCELLS + (size_t)lz * C::LCELLS + cell) * C::CD + e] = v;
     else
     {
-      const int cx = x0 + lx, cy = y0 + ly;
       if(a.ras)
+      {
+        const int cx = xy % a.nc[0], cy = xy / a.nc[0];
         v /= multiplicity(cx, a.nc[0]) * multiplicity(cy, a.nc[1]) * multiplicity(cz, a.nc[2]);
-      a.dst[cell_first<C>(a, cx, cy, cz) + e] = double(v);
+      }
+      a.dst[cell_first_xy<C>(a, xy, cz) + e] = double(v);
     }
     if(clear) accl[i] = 0.f;
   }
@@ -467,6 +473,9 @@ __global__ void __launch_bounds__(C::THREADS, 1) stream_kernel(StreamArgs a)
   double *s_raw = reinterpret_cast<double *>(sm + C::OFF_RAW);
   float *s_acc = sm + C::OFF_ACC;
   float *s_work = sm + C::OFF_WORK;
+  int *s_cxy = reinterpret_cast<int *>(sm + C::OFF_TAB);
+  int *s_cshared = s_cxy + C::LCELLS;
+  int *s_aoff = reinterpret_cast<int *>(sm + C::OFF_AOFF);
   const int tid = threadIdx.x;
   const int slot = tid / C::LPP, q = tid % C::LPP;  // FD passes: patch slot (px + BX py), pencil group
   const int px = slot % BX, py = slot / BX;
@@ -500,8 +509,32 @@ __global__ void __launch_bounds__(C::THREADS, 1) stream_kernel(StreamArgs a)
       s_fd[i] = v;
       if(o == 0) s_sym[sl] = en >= 0 ? a.sym[en] : 0;
     }
-    copy_layer_async<C>(a, x0, y0, bx, by, z0, s_raw, e, g);
-    copy_layer_async<C>(a, x0, y0, bx, by, z0 + 1, s_raw + C::LAYER, e, g);
+    // cell tables of the item (read by the element loops below, which then need no index
+    // arithmetic of their own)
+    for(int i = tid; i < C::LCELLS; i += C::THREADS)
+    {
+      const int lx = i % C::CX, ly = i / C::CX;
+      s_cxy[i] = (lx <= bx && ly <= by) ? (x0 + lx) + a.nc[0] * (y0 + ly) : -1;
+      s_cshared[i] = (lx == 0 && tx > 0) || (lx == bx && tx < a.T[0] - 1) || (ly == 0 && ty > 0) ||
+                     (ly == by && ty < a.T[1] - 1);
+    }
+    for(int i = tid; i < 2 * C::LCELLS; i += C::THREADS)
+    {
+      const int L = i >= C::LCELLS, cell = i - L * C::LCELLS;
+      const int lx = cell % C::CX, ly = cell / C::CX;
+      int k = 0;
+      for(int oy = 1; oy >= 0; --oy)
+        for(int ox = 1; ox >= 0; --ox, ++k)
+        {
+          const int sx = lx - ox, sy = ly - oy;
+          s_aoff[4 * i + k] = (sx >= 0 && sx < bx && sy >= 0 && sy < by)
+                                ? (sx + BX * sy) * PS + K1 * (ox + SX * oy + SXY * L)
+                                : -1;
+        }
+    }
+    __syncthreads();
+    copy_layer_async<C>(a, s_cxy, z0, s_raw, e, g);
+    copy_layer_async<C>(a, s_cxy, z0 + 1, s_raw + C::LAYER, e, g);
     for(int i = tid; i < 2 * C::LAYER; i += C::THREADS) s_acc[i] = 0.f;
     wait_async_all();
     __syncthreads();
@@ -510,7 +543,7 @@ __global__ void __launch_bounds__(C::THREADS, 1) stream_kernel(StreamArgs a)
     {
       // layer j+2 streams in while this vertex layer is solved (its ring slot held layer j-1)
       const bool more = j + 2 <= bz;
-      if(more) copy_layer_async<C>(a, x0, y0, bx, by, z0 + j + 2, s_raw + ((j + 2) % 3) * C::LAYER, e, g);
+      if(more) copy_layer_async<C>(a, s_cxy, z0 + j + 2, s_raw + ((j + 2) % 3) * C::LAYER, e, g);
       const double *lo = s_raw + (j % 3) * C::LAYER, *hi = s_raw + ((j + 1) % 3) * C::LAYER;
       const bool active = px < bx && py < by && q < TPP;
       float *my = s_work + slot * PS;
@@ -564,28 +597,23 @@ __global__ void __launch_bounds__(C::THREADS, 1) stream_kernel(StreamArgs a)
         for(int cl = g; cl < 2 * C::LCELLS; cl += C::G)
         {
           const int L = cl >= C::LCELLS, cell = cl - L * C::LCELLS;
-          const int lx = cell % C::CX, ly = cell / C::CX;
+          const int4 o = reinterpret_cast<const int4 *>(s_aoff)[cl];
           float sum = 0.f;
-#pragma unroll
-          for(int oy = 1; oy >= 0; --oy)
-#pragma unroll
-            for(int ox = 1; ox >= 0; --ox)
-            {
-              const int sx = lx - ox, sy = ly - oy;
-              if(sx >= 0 && sx < bx && sy >= 0 && sy < by)
-                sum += s_work[(sx + BX * sy) * PS + e_patch + K1 * (ox + SX * oy + SXY * L)];
-            }
+          if(o.x >= 0) sum += s_work[o.x + e_patch];
+          if(o.y >= 0) sum += s_work[o.y + e_patch];
+          if(o.z >= 0) sum += s_work[o.z + e_patch];
+          if(o.w >= 0) sum += s_work[o.w + e_patch];
           (L ? ahi : alo)[cell * CD + e] += sum;
         }
       __syncthreads();
       // cell layer j is complete: write it, clear its accumulator for layer j+2
-      write_layer<C>(a, alo, item, j, z0 + j, j == 0 && tz > 0, tx, ty, x0, y0, bx, by, e, g, true);
+      write_layer<C>(a, alo, item, j, z0 + j, j == 0 && tz > 0, s_cxy, s_cshared, e, g, true);
       if(more) wait_async_all();
       __syncthreads();
     }
     // last cell layer of the item
-    write_layer<C>(a, s_acc + (bz % 2) * C::LAYER, item, bz, z0 + bz, tz < a.T[2] - 1, tx, ty, x0,
-                   y0, bx, by, e, g, false);
+    write_layer<C>(a, s_acc + (bz % 2) * C::LAYER, item, bz, z0 + bz, tz < a.T[2] - 1, s_cxy, s_cshared,
+                   e, g, false);
   }
 }
 
