@@ -400,6 +400,16 @@ __device__ __forceinline__ void mpass_divide(float *__restrict__ data, const flo
   }
 }
 
+// barrier between two FD passes: a warp that owns its patch alone only waits for itself
+template<class C>
+__device__ __forceinline__ void pass_sync()
+{
+  if constexpr(C::WARP_PER_PATCH)
+    __syncwarp();
+  else
+    __syncthreads();
+}
+
 // first DoF of the cell with lexicographic index xy + nx ny cz
 template<class C>
 __device__ __forceinline__ int64_t cell_first_xy(const StreamArgs &a, int xy, int cz)
@@ -560,31 +570,31 @@ __global__ void __launch_bounds__(C::THREADS, 1) stream_kernel(StreamArgs a)
         else
           mpass_x_from_layers<false, K1, N, SX, SXY, NPAD, HP, NPT, TPP, C::CX, CD>(my, lo, hi, ex, px, py, q);
       }
-      __syncthreads();
+      pass_sync<C>();
       if(active)
       {
         if(sy) spass<true, true, N, SX, SXY, NPAD, HP, 1, NPT, TPP>(my, ey, q, 1.f);
         else spass<false, true, N, SX, SXY, NPAD, HP, 1, NPT, TPP>(my, ey, q, 1.f);
       }
-      __syncthreads();
+      pass_sync<C>();
       if(active)
       {
         if(sz) mpass_divide<true, N, SX, SXY, NPAD, HP, NPT, TPP>(my, lamx, lamy, ez, lamz, q);
         else mpass_divide<false, N, SX, SXY, NPAD, HP, NPT, TPP>(my, lamx, lamy, ez, lamz, q);
       }
-      __syncthreads();
+      pass_sync<C>();
       if(active)
       {
         if(sz) spass<true, false, N, SX, SXY, NPAD, HP, 2, NPT, TPP>(my, ez, q, 1.f);
         else spass<false, false, N, SX, SXY, NPAD, HP, 2, NPT, TPP>(my, ez, q, 1.f);
       }
-      __syncthreads();
+      pass_sync<C>();
       if(active)
       {
         if(sy) spass<true, false, N, SX, SXY, NPAD, HP, 1, NPT, TPP>(my, ey, q, 1.f);
         else spass<false, false, N, SX, SXY, NPAD, HP, 1, NPT, TPP>(my, ey, q, 1.f);
       }
-      __syncthreads();
+      pass_sync<C>();
       if(active)
       {
         if(sx) spass<true, false, N, SX, SXY, NPAD, HP, 0, NPT, TPP>(my, ex, q, a.omega);
