@@ -343,21 +343,22 @@ __device__ __forceinline__ void mpass_x_from_layers(float *__restrict__ data, co
   }
 }
 
-// direction 2, forward: S^T along z, then division by the eigenvalue sums
-// lambda_x[i0] + lambda_y[i1] + lambda_z[i2]
+// direction 2 in registers: S^T along z, division by the eigenvalue sums, S along z -- the
+// pencil a thread transforms forward is the one it transforms back, so the intermediate never
+// goes through shared memory
 template<bool SYM, int N, int SX, int SXY, int NPAD, int HPAD, int NPT, int TPP>
-__device__ __forceinline__ void mpass_divide(float *__restrict__ data, const float *__restrict__ lamx,
-                                             const float *__restrict__ lamy, const float *__restrict__ ez,
-                                             const float *__restrict__ lamz, int q)
+__device__ __forceinline__ void zpass_solve(float *__restrict__ data, const float *__restrict__ lamx,
+                                            const float *__restrict__ lamy, const float *__restrict__ ez,
+                                            const float *__restrict__ lamz, int q)
 {
   constexpr int stride = SXY;
-  float r[NPT][N];
+  float r[NPT][N], t[NPT][N];
   float lxy[NPT];
   int base[NPT];
 #pragma unroll
   for(int j = 0; j < NPT; ++j)
   {
-    const int p = q + j * TPP;  // pencil along z: i0 + N i1
+    const int p = q + j * TPP;
     base[j] = pbase<N, SX, SXY, 2>(p);
     lxy[j] = lamx[p % N] + lamy[p / N];
 #pragma unroll
@@ -365,15 +366,19 @@ __device__ __forceinline__ void mpass_divide(float *__restrict__ data, const flo
   }
   if constexpr(SYM)
   {
-    float t[NPT][N];
     eo_forward<N / 2, HPAD, NPT>(r, ez, t);
 #pragma unroll
     for(int i = 0; i < N; ++i)
     {
       const float lz = lamz[i];
 #pragma unroll
-      for(int j = 0; j < NPT; ++j) data[base[j] + i * stride] = __fdividef(t[j][i], lxy[j] + lz);
+      for(int j = 0; j < NPT; ++j) t[j][i] = __fdividef(t[j][i], lxy[j] + lz);
     }
+    eo_backward<N / 2, HPAD, NPT>(t, ez, r);
+#pragma unroll
+    for(int j = 0; j < NPT; ++j)
+#pragma unroll
+      for(int i = 0; i < N; ++i) data[base[j] + i * stride] = r[j][i];
     return;
   }
 #pragma unroll
@@ -396,7 +401,28 @@ __device__ __forceinline__ void mpass_divide(float *__restrict__ data, const flo
     }
     const float lz = lamz[i];
 #pragma unroll
-    for(int j = 0; j < NPT; ++j) data[base[j] + i * stride] = __fdividef(acc[j], lxy[j] + lz);
+    for(int j = 0; j < NPT; ++j) t[j][i] = __fdividef(acc[j], lxy[j] + lz);
+  }
+#pragma unroll
+  for(int i = 0; i < N; ++i)
+  {
+    const float4 *row = reinterpret_cast<const float4 *>(ez + Entry<float, N>::S + i * NPAD);
+    float acc[NPT];
+#pragma unroll
+    for(int j = 0; j < NPT; ++j) acc[j] = 0.f;
+#pragma unroll
+    for(int m4 = 0; m4 < NPAD / 4; ++m4)
+    {
+      const float4 v = row[m4];
+      const float vv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+      for(int w = 0; w < 4; ++w)
+        if(m4 * 4 + w < N)
+#pragma unroll
+          for(int j = 0; j < NPT; ++j) acc[j] = fmaf(vv[w], t[j][m4 * 4 + w < N ? m4 * 4 + w : 0], acc[j]);
+    }
+#pragma unroll
+    for(int j = 0; j < NPT; ++j) data[base[j] + i * stride] = acc[j];
   }
 }
 
@@ -579,14 +605,8 @@ __global__ void __launch_bounds__(C::THREADS, 1) stream_kernel(StreamArgs a)
       pass_sync<C>();
       if(active)
       {
-        if(sz) mpass_divide<true, N, SX, SXY, NPAD, HP, NPT, TPP>(my, lamx, lamy, ez, lamz, q);
-        else mpass_divide<false, N, SX, SXY, NPAD, HP, NPT, TPP>(my, lamx, lamy, ez, lamz, q);
-      }
-      pass_sync<C>();
-      if(active)
-      {
-        if(sz) spass<true, false, N, SX, SXY, NPAD, HP, 2, NPT, TPP>(my, ez, q, 1.f);
-        else spass<false, false, N, SX, SXY, NPAD, HP, 2, NPT, TPP>(my, ez, q, 1.f);
+        if(sz) zpass_solve<true, N, SX, SXY, NPAD, HP, NPT, TPP>(my, lamx, lamy, ez, lamz, q);
+        else zpass_solve<false, N, SX, SXY, NPAD, HP, NPT, TPP>(my, lamx, lamy, ez, lamz, q);
       }
       pass_sync<C>();
       if(active)
