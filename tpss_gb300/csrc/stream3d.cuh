@@ -31,6 +31,40 @@ namespace stream
 using fd::cpow;
 using fd::Entry;
 
+// base offset of the pencil along DIR through (a, b) -- (y, z), (x, z) or (x, y) -- in the padded
+// layout x + SX y + SXY z
+template<int SX, int SXY>
+__host__ __device__ constexpr int pencil_addr(int dir, int a, int b)
+{
+  return dir == 0 ? SX * a + SXY * b : dir == 1 ? a + SXY * b : a + SX * b;
+}
+
+// the plain order puts the pencils of every warp instruction in distinct banks (one patch per warp)
+template<int N, int SX, int SXY, int NPT, int TPP, int DIR>
+__host__ __device__ constexpr bool plain_order_conflict_free()
+{
+  for(int j = 0; j < NPT; ++j)
+  {
+    int cnt[32] = {};
+    for(int q = 0; q < TPP; ++q)
+    {
+      const int p = q + j * TPP;
+      if(++cnt[pencil_addr<SX, SXY>(DIR, p % N, p / N) % 32] > 1) return false;
+    }
+  }
+  return true;
+}
+
+// no bank holds more than NPT pencils along DIR: the bank-sorted order is conflict free
+template<int N, int SX, int SXY, int NPT, int DIR>
+__host__ __device__ constexpr bool bank_order_conflict_free()
+{
+  int cnt[32] = {};
+  for(int p = 0; p < N * N; ++p)
+    if(++cnt[pencil_addr<SX, SXY>(DIR, p % N, p / N) % 32] > NPT) return false;
+  return true;
+}
+
 template<int K1_, int BX_, int BY_, int BZ_, int NPT_, bool WARP_PER_PATCH_ = false>
 struct SCfg
 {
@@ -82,7 +116,15 @@ struct SCfg
   // to) 4 patches of a vertex layer that touch it (-1: none)
   static constexpr int OFF_TAB = ((OFF_WORK + NPATCH * PSTRIDE + 3) / 4) * 4;
   static constexpr int OFF_AOFF = OFF_TAB + ((2 * LCELLS + 3) / 4) * 4;  // int4 aligned
-  static constexpr int FLOATS = OFF_AOFF + 8 * LCELLS;
+  // pencil order tables of the directions whose plain order has bank conflicts (warp per patch)
+  static constexpr bool MAP0 = WARP_PER_PATCH_ && !plain_order_conflict_free<N, SX, SXY, NPT, TPP, 0>() &&
+                               bank_order_conflict_free<N, SX, SXY, NPT, 0>();
+  static constexpr bool MAP1 = WARP_PER_PATCH_ && !plain_order_conflict_free<N, SX, SXY, NPT, TPP, 1>() &&
+                               bank_order_conflict_free<N, SX, SXY, NPT, 1>();
+  static constexpr bool MAP2 = WARP_PER_PATCH_ && !plain_order_conflict_free<N, SX, SXY, NPT, TPP, 2>() &&
+                               bank_order_conflict_free<N, SX, SXY, NPT, 2>();
+  static constexpr int OFF_PMAP = OFF_AOFF + 8 * LCELLS;
+  static constexpr int FLOATS = OFF_PMAP + (MAP0 || MAP1 || MAP2 ? 3 * NPENCIL : 0);
   static constexpr size_t smem_bytes() { return (size_t)FLOATS * 4; }
 };
 
@@ -129,17 +171,32 @@ __host__ __device__ __forceinline__ float multiplicity(int c, int n)
   return float((c >= 1 ? 1 : 0) + (c + 1 <= n - 1 ? 1 : 0));
 }
 
-// base offset of pencil p along DIR in the padded layout x + SX y + SXY z
-template<int N, int SX, int SXY, int DIR>
-__device__ __forceinline__ int pbase(int p)
+// Pencil idx = q + j TPP of a thread (pencil group q, j-th of its NPT pencils) along DIR. Plain
+// order: a = idx % N, b = idx / N. Mapped order (MAP): read from the table pm, which deals the
+// pencils sorted by shared-memory bank round-robin to the NPT groups, so that the TPP pencils one
+// warp instruction touches lie in distinct banks (entries: offset | a << 16 | b << 24).
+template<bool MAP, int N, int SX, int SXY, int DIR>
+__device__ __forceinline__ int pencil_of(const int *__restrict__ pm, int idx, int &a, int &b)
 {
-  const int a = p % N, b = p / N;
-  return DIR == 0 ? SX * a + SXY * b : DIR == 1 ? a + SXY * b : a + SX * b;
+  if constexpr(MAP)
+  {
+    const int v = pm[idx];
+    a = (v >> 16) & 0xff;
+    b = v >> 24;
+    return v & 0xffff;
+  }
+  else
+  {
+    a = idx % N;
+    b = idx / N;
+    return pencil_addr<SX, SXY>(DIR, a, b);
+  }
 }
 
-template<int N, int SX, int SXY, int NPAD, int DIR, int NPT, int TPP>
-__device__ __forceinline__ void mpass(float *__restrict__ data, const float *__restrict__ B, int q,
-                                      float scale)
+
+template<bool MAP, int N, int SX, int SXY, int NPAD, int DIR, int NPT, int TPP>
+__device__ __forceinline__ void mpass(float *__restrict__ data, const float *__restrict__ B,
+                                      const int *__restrict__ pm, int q, float scale)
 {
   constexpr int stride = DIR == 0 ? 1 : DIR == 1 ? SX : SXY;
   float r[NPT][N];
@@ -147,7 +204,8 @@ __device__ __forceinline__ void mpass(float *__restrict__ data, const float *__r
 #pragma unroll
   for(int j = 0; j < NPT; ++j)
   {
-    base[j] = pbase<N, SX, SXY, DIR>(q + j * TPP);
+    int pa, pb;
+    base[j] = pencil_of<MAP, N, SX, SXY, DIR>(pm, q + j * TPP, pa, pb);
 #pragma unroll
     for(int m = 0; m < N; ++m) r[j][m] = data[base[j] + m * stride];
   }
@@ -261,12 +319,13 @@ __device__ __forceinline__ void eo_backward(const float (&t)[NPT][2 * H], const 
 }
 
 // full or even/odd pass along DIR (in place in the padded patch layout)
-template<bool SYM, bool FWD, int N, int SX, int SXY, int NPAD, int HPAD, int DIR, int NPT, int TPP>
-__device__ __forceinline__ void spass(float *__restrict__ data, const float *__restrict__ ent, int q,
-                                      float scale)
+template<bool SYM, bool FWD, bool MAP, int N, int SX, int SXY, int NPAD, int HPAD, int DIR, int NPT, int TPP>
+__device__ __forceinline__ void spass(float *__restrict__ data, const float *__restrict__ ent,
+                                      const int *__restrict__ pm, int q, float scale)
 {
   if constexpr(!SYM)
-    mpass<N, SX, SXY, NPAD, DIR, NPT, TPP>(data, ent + (FWD ? Entry<float, N>::ST : Entry<float, N>::S), q, scale);
+    mpass<MAP, N, SX, SXY, NPAD, DIR, NPT, TPP>(data, ent + (FWD ? Entry<float, N>::ST : Entry<float, N>::S), pm, q,
+                                                scale);
   else
   {
     constexpr int H = N / 2;
@@ -276,7 +335,8 @@ __device__ __forceinline__ void spass(float *__restrict__ data, const float *__r
 #pragma unroll
     for(int j = 0; j < NPT; ++j)
     {
-      base[j] = pbase<N, SX, SXY, DIR>(q + j * TPP);
+      int pa, pb;
+      base[j] = pencil_of<MAP, N, SX, SXY, DIR>(pm, q + j * TPP, pa, pb);
 #pragma unroll
       for(int m = 0; m < N; ++m) r[j][m] = data[base[j] + m * stride];
     }
@@ -293,18 +353,19 @@ __device__ __forceinline__ void spass(float *__restrict__ data, const float *__r
 
 // direction 0, forward, reading the patch straight from the two staged FP64 cell layers:
 // pencil (y, z) of patch (px, py) covers cells (px, px+1) of row (py + y/K1) in layer z/K1
-template<bool SYM, int K1, int N, int SX, int SXY, int NPAD, int HPAD, int NPT, int TPP, int CX, int CD>
+template<bool SYM, bool MAP, int K1, int N, int SX, int SXY, int NPAD, int HPAD, int NPT, int TPP, int CX, int CD>
 __device__ __forceinline__ void mpass_x_from_layers(float *__restrict__ data, const double *__restrict__ lo,
                                                     const double *__restrict__ hi,
-                                                    const float *__restrict__ St, int px, int py, int q)
+                                                    const float *__restrict__ St, const int *__restrict__ pm,
+                                                    int px, int py, int q)
 {
   float r[NPT][N];
   int base[NPT];
 #pragma unroll
   for(int j = 0; j < NPT; ++j)
   {
-    const int p = q + j * TPP, y = p % N, z = p / N;
-    base[j] = SX * y + SXY * z;
+    int y, z;
+    base[j] = pencil_of<MAP, N, SX, SXY, 0>(pm, q + j * TPP, y, z);
     const double *layer = z >= K1 ? hi : lo;
     const int row = (px + CX * (py + y / K1)) * CD + K1 * (y % K1) + K1 * K1 * (z % K1);
 #pragma unroll
@@ -318,38 +379,40 @@ __device__ __forceinline__ void mpass_x_from_layers(float *__restrict__ data, co
     for(int j = 0; j < NPT; ++j)
 #pragma unroll
       for(int i = 0; i < N; ++i) data[base[j] + i] = t[j][i];
-    return;
   }
-#pragma unroll
-  for(int i = 0; i < N; ++i)
+  else
   {
-    const float4 *rw = reinterpret_cast<const float4 *>(St + i * NPAD);
-    float acc[NPT];
 #pragma unroll
-    for(int j = 0; j < NPT; ++j) acc[j] = 0.f;
-#pragma unroll
-    for(int m4 = 0; m4 < NPAD / 4; ++m4)
+    for(int i = 0; i < N; ++i)
     {
-      const float4 v = rw[m4];
-      const float vv[4] = {v.x, v.y, v.z, v.w};
+      const float4 *rw = reinterpret_cast<const float4 *>(St + i * NPAD);
+      float acc[NPT];
 #pragma unroll
-      for(int w = 0; w < 4; ++w)
-        if(m4 * 4 + w < N)
+      for(int j = 0; j < NPT; ++j) acc[j] = 0.f;
 #pragma unroll
-          for(int j = 0; j < NPT; ++j) acc[j] = fmaf(vv[w], r[j][m4 * 4 + w < N ? m4 * 4 + w : 0], acc[j]);
+      for(int m4 = 0; m4 < NPAD / 4; ++m4)
+      {
+        const float4 v = rw[m4];
+        const float vv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+        for(int w = 0; w < 4; ++w)
+          if(m4 * 4 + w < N)
+#pragma unroll
+            for(int j = 0; j < NPT; ++j) acc[j] = fmaf(vv[w], r[j][m4 * 4 + w < N ? m4 * 4 + w : 0], acc[j]);
+      }
+#pragma unroll
+      for(int j = 0; j < NPT; ++j) data[base[j] + i] = acc[j];
     }
-#pragma unroll
-    for(int j = 0; j < NPT; ++j) data[base[j] + i] = acc[j];
   }
 }
 
 // direction 2 in registers: S^T along z, division by the eigenvalue sums, S along z -- the
 // pencil a thread transforms forward is the one it transforms back, so the intermediate never
 // goes through shared memory
-template<bool SYM, int N, int SX, int SXY, int NPAD, int HPAD, int NPT, int TPP>
+template<bool SYM, bool MAP, int N, int SX, int SXY, int NPAD, int HPAD, int NPT, int TPP>
 __device__ __forceinline__ void zpass_solve(float *__restrict__ data, const float *__restrict__ lamx,
                                             const float *__restrict__ lamy, const float *__restrict__ ez,
-                                            const float *__restrict__ lamz, int q)
+                                            const float *__restrict__ lamz, const int *__restrict__ pm, int q)
 {
   constexpr int stride = SXY;
   float r[NPT][N], t[NPT][N];
@@ -358,9 +421,9 @@ __device__ __forceinline__ void zpass_solve(float *__restrict__ data, const floa
 #pragma unroll
   for(int j = 0; j < NPT; ++j)
   {
-    const int p = q + j * TPP;
-    base[j] = pbase<N, SX, SXY, 2>(p);
-    lxy[j] = lamx[p % N] + lamy[p / N];
+    int px_, py_;
+    base[j] = pencil_of<MAP, N, SX, SXY, 2>(pm, q + j * TPP, px_, py_);
+    lxy[j] = lamx[px_] + lamy[py_];
 #pragma unroll
     for(int m = 0; m < N; ++m) r[j][m] = data[base[j] + m * stride];
   }
@@ -379,50 +442,52 @@ __device__ __forceinline__ void zpass_solve(float *__restrict__ data, const floa
     for(int j = 0; j < NPT; ++j)
 #pragma unroll
       for(int i = 0; i < N; ++i) data[base[j] + i * stride] = r[j][i];
-    return;
   }
-#pragma unroll
-  for(int i = 0; i < N; ++i)
+  else
   {
-    const float4 *row = reinterpret_cast<const float4 *>(ez + Entry<float, N>::ST + i * NPAD);
-    float acc[NPT];
 #pragma unroll
-    for(int j = 0; j < NPT; ++j) acc[j] = 0.f;
-#pragma unroll
-    for(int m4 = 0; m4 < NPAD / 4; ++m4)
+    for(int i = 0; i < N; ++i)
     {
-      const float4 v = row[m4];
-      const float vv[4] = {v.x, v.y, v.z, v.w};
+      const float4 *row = reinterpret_cast<const float4 *>(ez + Entry<float, N>::ST + i * NPAD);
+      float acc[NPT];
 #pragma unroll
-      for(int w = 0; w < 4; ++w)
-        if(m4 * 4 + w < N)
+      for(int j = 0; j < NPT; ++j) acc[j] = 0.f;
 #pragma unroll
-          for(int j = 0; j < NPT; ++j) acc[j] = fmaf(vv[w], r[j][m4 * 4 + w < N ? m4 * 4 + w : 0], acc[j]);
-    }
-    const float lz = lamz[i];
+      for(int m4 = 0; m4 < NPAD / 4; ++m4)
+      {
+        const float4 v = row[m4];
+        const float vv[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
-    for(int j = 0; j < NPT; ++j) t[j][i] = __fdividef(acc[j], lxy[j] + lz);
-  }
+        for(int w = 0; w < 4; ++w)
+          if(m4 * 4 + w < N)
 #pragma unroll
-  for(int i = 0; i < N; ++i)
-  {
-    const float4 *row = reinterpret_cast<const float4 *>(ez + Entry<float, N>::S + i * NPAD);
-    float acc[NPT];
+            for(int j = 0; j < NPT; ++j) acc[j] = fmaf(vv[w], r[j][m4 * 4 + w < N ? m4 * 4 + w : 0], acc[j]);
+      }
+      const float lz = lamz[i];
 #pragma unroll
-    for(int j = 0; j < NPT; ++j) acc[j] = 0.f;
-#pragma unroll
-    for(int m4 = 0; m4 < NPAD / 4; ++m4)
-    {
-      const float4 v = row[m4];
-      const float vv[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-      for(int w = 0; w < 4; ++w)
-        if(m4 * 4 + w < N)
-#pragma unroll
-          for(int j = 0; j < NPT; ++j) acc[j] = fmaf(vv[w], t[j][m4 * 4 + w < N ? m4 * 4 + w : 0], acc[j]);
+      for(int j = 0; j < NPT; ++j) t[j][i] = __fdividef(acc[j], lxy[j] + lz);
     }
 #pragma unroll
-    for(int j = 0; j < NPT; ++j) data[base[j] + i * stride] = acc[j];
+    for(int i = 0; i < N; ++i)
+    {
+      const float4 *row = reinterpret_cast<const float4 *>(ez + Entry<float, N>::S + i * NPAD);
+      float acc[NPT];
+#pragma unroll
+      for(int j = 0; j < NPT; ++j) acc[j] = 0.f;
+#pragma unroll
+      for(int m4 = 0; m4 < NPAD / 4; ++m4)
+      {
+        const float4 v = row[m4];
+        const float vv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+        for(int w = 0; w < 4; ++w)
+          if(m4 * 4 + w < N)
+#pragma unroll
+            for(int j = 0; j < NPT; ++j) acc[j] = fmaf(vv[w], t[j][m4 * 4 + w < N ? m4 * 4 + w : 0], acc[j]);
+      }
+#pragma unroll
+      for(int j = 0; j < NPT; ++j) data[base[j] + i * stride] = acc[j];
+    }
   }
 }
 
@@ -512,6 +577,7 @@ __global__ void __launch_bounds__(C::THREADS, 1) stream_kernel(StreamArgs a)
   int *s_cxy = reinterpret_cast<int *>(sm + C::OFF_TAB);
   int *s_cshared = s_cxy + C::LCELLS;
   int *s_aoff = reinterpret_cast<int *>(sm + C::OFF_AOFF);
+  int *s_pmap = reinterpret_cast<int *>(sm + C::OFF_PMAP);
   const int tid = threadIdx.x;
   const int slot = tid / C::LPP, q = tid % C::LPP;  // FD passes: patch slot (px + BX py), pencil group
   const int px = slot % BX, py = slot / BX;
@@ -519,6 +585,28 @@ __global__ void __launch_bounds__(C::THREADS, 1) stream_kernel(StreamArgs a)
   const int e = tid % CD, g = tid / CD;
   const int e_patch = (e % K1) + SX * ((e / K1) % K1) + SXY * (e / (K1 * K1));
   const int n_items = a.T[0] * a.T[1] * a.T[2];
+  if constexpr(C::MAP0 || C::MAP1 || C::MAP2)
+  {
+    // pencil order tables: rank the pencils by (bank, index), deal rank i to thread q = i / NPT as
+    // its (i % NPT)-th pencil; a bank holds at most NPT pencils, so every warp instruction's
+    // pencils lie in distinct banks (read after the barrier at the top of the item loop)
+    constexpr int NP = C::NPENCIL;
+    for(int t = tid; t < 3 * NP; t += C::THREADS)
+    {
+      const int dir = t / NP, p = t % NP;
+      if(!(dir == 0 ? C::MAP0 : dir == 1 ? C::MAP1 : C::MAP2)) continue;
+      const int addr = pencil_addr<SX, SXY>(dir, p % N, p / N), bank = addr % 32;
+      int rank = 0;
+      for(int p2 = 0; p2 < NP; ++p2)
+      {
+        const int b2 = pencil_addr<SX, SXY>(dir, p2 % N, p2 / N) % 32;
+        rank += b2 < bank || (b2 == bank && p2 < p);
+      }
+      s_pmap[dir * NP + rank / NPT + (rank % NPT) * TPP] = addr | (p % N) << 16 | (p / N) << 24;
+    }
+  }
+  const int *pm0 = s_pmap, *pm1 = s_pmap + C::NPENCIL, *pm2 = s_pmap + 2 * C::NPENCIL;
+  constexpr bool M0 = C::MAP0, M1 = C::MAP1, M2 = C::MAP2;
 
   for(int item = a.item_begin + blockIdx.x; item < a.item_end && item < n_items; item += gridDim.x)
   {
@@ -592,33 +680,33 @@ __global__ void __launch_bounds__(C::THREADS, 1) stream_kernel(StreamArgs a)
       if(active)
       {
         if(sx)
-          mpass_x_from_layers<true, K1, N, SX, SXY, NPAD, HP, NPT, TPP, C::CX, CD>(my, lo, hi, ex, px, py, q);
+          mpass_x_from_layers<true, M0, K1, N, SX, SXY, NPAD, HP, NPT, TPP, C::CX, CD>(my, lo, hi, ex, pm0, px, py, q);
         else
-          mpass_x_from_layers<false, K1, N, SX, SXY, NPAD, HP, NPT, TPP, C::CX, CD>(my, lo, hi, ex, px, py, q);
+          mpass_x_from_layers<false, M0, K1, N, SX, SXY, NPAD, HP, NPT, TPP, C::CX, CD>(my, lo, hi, ex, pm0, px, py, q);
       }
       pass_sync<C>();
       if(active)
       {
-        if(sy) spass<true, true, N, SX, SXY, NPAD, HP, 1, NPT, TPP>(my, ey, q, 1.f);
-        else spass<false, true, N, SX, SXY, NPAD, HP, 1, NPT, TPP>(my, ey, q, 1.f);
+        if(sy) spass<true, true, M1, N, SX, SXY, NPAD, HP, 1, NPT, TPP>(my, ey, pm1, q, 1.f);
+        else spass<false, true, M1, N, SX, SXY, NPAD, HP, 1, NPT, TPP>(my, ey, pm1, q, 1.f);
       }
       pass_sync<C>();
       if(active)
       {
-        if(sz) zpass_solve<true, N, SX, SXY, NPAD, HP, NPT, TPP>(my, lamx, lamy, ez, lamz, q);
-        else zpass_solve<false, N, SX, SXY, NPAD, HP, NPT, TPP>(my, lamx, lamy, ez, lamz, q);
+        if(sz) zpass_solve<true, M2, N, SX, SXY, NPAD, HP, NPT, TPP>(my, lamx, lamy, ez, lamz, pm2, q);
+        else zpass_solve<false, M2, N, SX, SXY, NPAD, HP, NPT, TPP>(my, lamx, lamy, ez, lamz, pm2, q);
       }
       pass_sync<C>();
       if(active)
       {
-        if(sy) spass<true, false, N, SX, SXY, NPAD, HP, 1, NPT, TPP>(my, ey, q, 1.f);
-        else spass<false, false, N, SX, SXY, NPAD, HP, 1, NPT, TPP>(my, ey, q, 1.f);
+        if(sy) spass<true, false, M1, N, SX, SXY, NPAD, HP, 1, NPT, TPP>(my, ey, pm1, q, 1.f);
+        else spass<false, false, M1, N, SX, SXY, NPAD, HP, 1, NPT, TPP>(my, ey, pm1, q, 1.f);
       }
       pass_sync<C>();
       if(active)
       {
-        if(sx) spass<true, false, N, SX, SXY, NPAD, HP, 0, NPT, TPP>(my, ex, q, a.omega);
-        else spass<false, false, N, SX, SXY, NPAD, HP, 0, NPT, TPP>(my, ex, q, a.omega);
+        if(sx) spass<true, false, M0, N, SX, SXY, NPAD, HP, 0, NPT, TPP>(my, ex, pm0, q, a.omega);
+        else spass<false, false, M0, N, SX, SXY, NPAD, HP, 0, NPT, TPP>(my, ex, pm0, q, a.omega);
       }
       __syncthreads();
       // accumulate per cell: the (up to) 4 patches of this layer touching the cell, fixed order
