@@ -108,8 +108,14 @@ struct SCfg
   // shared memory carve-up (in floats; the staged FP64 cell layers take two floats per value)
   static constexpr int OFF_FD = 0;                                   // (BX + BY + BZ) entries
   static constexpr int OFF_SYM = OFF_FD + (BX + BY + BZ) * ESLOT;          // int flags
-  static constexpr int OFF_RAW = ((OFF_SYM + (BX + BY + BZ) + 3) / 4) * 4;  // 3 FP64 layers
-  static constexpr int OFF_ACC = OFF_RAW + 3 * 2 * LAYER;            // 2 FP32 layers
+  // cell layers are copied in as FP64 (two landing layers) and converted once to FP32 (two
+  // layers, rows of cells padded by RPAD floats so that the x pass reads conflict free)
+  static constexpr int RPAD = K1 == 5 ? 4 : K1 == 4 ? 1 : K1 == 3 ? (WARP_PER_PATCH_ ? 0 : 6) : (WARP_PER_PATCH_ ? 5 : 1);
+  static constexpr int RSTRIDE = CX * CD + RPAD;                     // floats per row of cells
+  static constexpr int LAYERF = ((CY * RSTRIDE + 3) / 4) * 4;        // floats per FP32 layer
+  static constexpr int OFF_RAW = ((OFF_SYM + (BX + BY + BZ) + 3) / 4) * 4;  // 2 FP64 layers
+  static constexpr int OFF_F32 = OFF_RAW + 2 * 2 * LAYER;            // 2 FP32 cell layers
+  static constexpr int OFF_ACC = OFF_F32 + 2 * LAYERF;               // 2 FP32 accumulator layers
   static constexpr int OFF_WORK = OFF_ACC + 2 * LAYER;               // NPATCH patches
   // per-item cell tables (ints): global xy index of each column cell (-1 outside the item),
   // its x/y-shared flag, and for each of the 2 LCELLS accumulator cells the offsets of the (up
@@ -126,6 +132,7 @@ struct SCfg
   static constexpr int OFF_PMAP = OFF_AOFF + 8 * LCELLS;
   static constexpr int FLOATS = OFF_PMAP + (MAP0 || MAP1 || MAP2 ? 3 * NPENCIL : 0);
   static constexpr size_t smem_bytes() { return (size_t)FLOATS * 4; }
+  static_assert((size_t)FLOATS * 4 <= 227 * 1024, "shared memory per CTA exceeds 227 KB");
 };
 
 struct StreamArgs
@@ -194,7 +201,7 @@ __device__ __forceinline__ int pencil_of(const int *__restrict__ pm, int idx, in
 }
 
 
-template<bool MAP, int N, int SX, int SXY, int NPAD, int DIR, int NPT, int TPP>
+template<bool MAP, bool SCALED, int N, int SX, int SXY, int NPAD, int DIR, int NPT, int TPP>
 __device__ __forceinline__ void mpass(float *__restrict__ data, const float *__restrict__ B,
                                       const int *__restrict__ pm, int q, float scale)
 {
@@ -228,7 +235,7 @@ __device__ __forceinline__ void mpass(float *__restrict__ data, const float *__r
           for(int j = 0; j < NPT; ++j) acc[j] = fmaf(vv[w], r[j][m4 * 4 + w < N ? m4 * 4 + w : 0], acc[j]);
     }
 #pragma unroll
-    for(int j = 0; j < NPT; ++j) data[base[j] + i * stride] = acc[j] * scale;
+    for(int j = 0; j < NPT; ++j) data[base[j] + i * stride] = SCALED ? acc[j] * scale : acc[j];
   }
 }
 
@@ -319,13 +326,15 @@ __device__ __forceinline__ void eo_backward(const float (&t)[NPT][2 * H], const 
 }
 
 // full or even/odd pass along DIR (in place in the padded patch layout)
-template<bool SYM, bool FWD, bool MAP, int N, int SX, int SXY, int NPAD, int HPAD, int DIR, int NPT, int TPP>
+// (SCALED: the outputs are multiplied by scale)
+template<bool SYM, bool FWD, bool MAP, bool SCALED, int N, int SX, int SXY, int NPAD, int HPAD, int DIR, int NPT,
+         int TPP>
 __device__ __forceinline__ void spass(float *__restrict__ data, const float *__restrict__ ent,
                                       const int *__restrict__ pm, int q, float scale)
 {
   if constexpr(!SYM)
-    mpass<MAP, N, SX, SXY, NPAD, DIR, NPT, TPP>(data, ent + (FWD ? Entry<float, N>::ST : Entry<float, N>::S), pm, q,
-                                                scale);
+    mpass<MAP, SCALED, N, SX, SXY, NPAD, DIR, NPT, TPP>(
+      data, ent + (FWD ? Entry<float, N>::ST : Entry<float, N>::S), pm, q, scale);
   else
   {
     constexpr int H = N / 2;
@@ -347,15 +356,15 @@ __device__ __forceinline__ void spass(float *__restrict__ data, const float *__r
 #pragma unroll
     for(int j = 0; j < NPT; ++j)
 #pragma unroll
-      for(int i = 0; i < N; ++i) data[base[j] + i * stride] = o[j][i] * scale;
+      for(int i = 0; i < N; ++i) data[base[j] + i * stride] = SCALED ? o[j][i] * scale : o[j][i];
   }
 }
 
 // direction 0, forward, reading the patch straight from the two staged FP64 cell layers:
 // pencil (y, z) of patch (px, py) covers cells (px, px+1) of row (py + y/K1) in layer z/K1
-template<bool SYM, bool MAP, int K1, int N, int SX, int SXY, int NPAD, int HPAD, int NPT, int TPP, int CX, int CD>
-__device__ __forceinline__ void mpass_x_from_layers(float *__restrict__ data, const double *__restrict__ lo,
-                                                    const double *__restrict__ hi,
+template<bool SYM, bool MAP, int K1, int N, int SX, int SXY, int NPAD, int HPAD, int NPT, int TPP, int RS, int CD>
+__device__ __forceinline__ void mpass_x_from_layers(float *__restrict__ data, const float *__restrict__ lo,
+                                                    const float *__restrict__ hi,
                                                     const float *__restrict__ St, const int *__restrict__ pm,
                                                     int px, int py, int q)
 {
@@ -366,10 +375,10 @@ __device__ __forceinline__ void mpass_x_from_layers(float *__restrict__ data, co
   {
     int y, z;
     base[j] = pencil_of<MAP, N, SX, SXY, 0>(pm, q + j * TPP, y, z);
-    const double *layer = z >= K1 ? hi : lo;
-    const int row = (px + CX * (py + y / K1)) * CD + K1 * (y % K1) + K1 * K1 * (z % K1);
+    const float *layer = z >= K1 ? hi : lo;
+    const int row = px * CD + RS * (py + y / K1) + K1 * (y % K1) + K1 * K1 * (z % K1);
 #pragma unroll
-    for(int m = 0; m < N; ++m) r[j][m] = float(layer[row + (m / K1) * CD + (m % K1)]);
+    for(int m = 0; m < N; ++m) r[j][m] = layer[row + (m / K1) * CD + (m % K1)];
   }
   if constexpr(SYM)
   {
@@ -534,6 +543,20 @@ __device__ __forceinline__ void copy_layer_async(const StreamArgs &a, const int 
 
 __device__ __forceinline__ void wait_async_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
+// FP64 landing layer -> FP32 cell layer (rows padded to RSTRIDE). Each thread converts the values
+// its own copy_layer_async put there (same cell/DoF assignment), so after its wait_async_all no
+// barrier is needed in between.
+template<class C>
+__device__ __forceinline__ void convert_layer(const double *raw, float *f32, int e, int g)
+{
+  if(g < C::G)
+    for(int cell = g; cell < C::LCELLS; cell += C::G)
+    {
+      const int lx = cell % C::CX, ly = cell / C::CX;
+      f32[lx * C::CD + ly * C::RSTRIDE + e] = float(raw[cell * C::CD + e]);
+    }
+}
+
 // write one completed cell layer: cells owned by the item to dst, shared cells to the halo
 template<class C>
 __device__ __forceinline__ void write_layer(const StreamArgs &a, float *accl, int item, int lz, int cz,
@@ -572,6 +595,7 @@ __global__ void __launch_bounds__(C::THREADS, 1) stream_kernel(StreamArgs a)
   float *s_fd = sm + C::OFF_FD;
   int *s_sym = reinterpret_cast<int *>(sm + C::OFF_SYM);
   double *s_raw = reinterpret_cast<double *>(sm + C::OFF_RAW);
+  float *s_f32 = sm + C::OFF_F32;
   float *s_acc = sm + C::OFF_ACC;
   float *s_work = sm + C::OFF_WORK;
   int *s_cxy = reinterpret_cast<int *>(sm + C::OFF_TAB);
@@ -661,14 +685,17 @@ __global__ void __launch_bounds__(C::THREADS, 1) stream_kernel(StreamArgs a)
     copy_layer_async<C>(a, s_cxy, z0 + 1, s_raw + C::LAYER, e, g);
     for(int i = tid; i < 2 * C::LAYER; i += C::THREADS) s_acc[i] = 0.f;
     wait_async_all();
+    convert_layer<C>(s_raw, s_f32, e, g);
+    convert_layer<C>(s_raw + C::LAYER, s_f32 + C::LAYERF, e, g);
     __syncthreads();
 
     for(int j = 0; j < bz; ++j)
     {
       // layer j+2 streams in while this vertex layer is solved (its ring slot held layer j-1)
       const bool more = j + 2 <= bz;
-      if(more) copy_layer_async<C>(a, s_cxy, z0 + j + 2, s_raw + ((j + 2) % 3) * C::LAYER, e, g);
-      const double *lo = s_raw + (j % 3) * C::LAYER, *hi = s_raw + ((j + 1) % 3) * C::LAYER;
+      // (cell layer j+2 lands in the FP64 slot of layer j, converted at the end of iteration j-2)
+      if(more) copy_layer_async<C>(a, s_cxy, z0 + j + 2, s_raw + (j % 2) * C::LAYER, e, g);
+      const float *lo = s_f32 + (j % 2) * C::LAYERF, *hi = s_f32 + ((j + 1) % 2) * C::LAYERF;
       const bool active = px < bx && py < by && q < TPP;
       float *my = s_work + slot * PS;
       constexpr int ESL = C::ESLOT, HP = C::HPAD;
@@ -680,15 +707,15 @@ __global__ void __launch_bounds__(C::THREADS, 1) stream_kernel(StreamArgs a)
       if(active)
       {
         if(sx)
-          mpass_x_from_layers<true, M0, K1, N, SX, SXY, NPAD, HP, NPT, TPP, C::CX, CD>(my, lo, hi, ex, pm0, px, py, q);
+          mpass_x_from_layers<true, M0, K1, N, SX, SXY, NPAD, HP, NPT, TPP, C::RSTRIDE, CD>(my, lo, hi, ex, pm0, px, py, q);
         else
-          mpass_x_from_layers<false, M0, K1, N, SX, SXY, NPAD, HP, NPT, TPP, C::CX, CD>(my, lo, hi, ex, pm0, px, py, q);
+          mpass_x_from_layers<false, M0, K1, N, SX, SXY, NPAD, HP, NPT, TPP, C::RSTRIDE, CD>(my, lo, hi, ex, pm0, px, py, q);
       }
       pass_sync<C>();
       if(active)
       {
-        if(sy) spass<true, true, M1, N, SX, SXY, NPAD, HP, 1, NPT, TPP>(my, ey, pm1, q, 1.f);
-        else spass<false, true, M1, N, SX, SXY, NPAD, HP, 1, NPT, TPP>(my, ey, pm1, q, 1.f);
+        if(sy) spass<true, true, M1, false, N, SX, SXY, NPAD, HP, 1, NPT, TPP>(my, ey, pm1, q, 1.f);
+        else spass<false, true, M1, false, N, SX, SXY, NPAD, HP, 1, NPT, TPP>(my, ey, pm1, q, 1.f);
       }
       pass_sync<C>();
       if(active)
@@ -699,14 +726,14 @@ __global__ void __launch_bounds__(C::THREADS, 1) stream_kernel(StreamArgs a)
       pass_sync<C>();
       if(active)
       {
-        if(sy) spass<true, false, M1, N, SX, SXY, NPAD, HP, 1, NPT, TPP>(my, ey, pm1, q, 1.f);
-        else spass<false, false, M1, N, SX, SXY, NPAD, HP, 1, NPT, TPP>(my, ey, pm1, q, 1.f);
+        if(sy) spass<true, false, M1, false, N, SX, SXY, NPAD, HP, 1, NPT, TPP>(my, ey, pm1, q, 1.f);
+        else spass<false, false, M1, false, N, SX, SXY, NPAD, HP, 1, NPT, TPP>(my, ey, pm1, q, 1.f);
       }
       pass_sync<C>();
       if(active)
       {
-        if(sx) spass<true, false, M0, N, SX, SXY, NPAD, HP, 0, NPT, TPP>(my, ex, pm0, q, a.omega);
-        else spass<false, false, M0, N, SX, SXY, NPAD, HP, 0, NPT, TPP>(my, ex, pm0, q, a.omega);
+        if(sx) spass<true, false, M0, true, N, SX, SXY, NPAD, HP, 0, NPT, TPP>(my, ex, pm0, q, a.omega);
+        else spass<false, false, M0, true, N, SX, SXY, NPAD, HP, 0, NPT, TPP>(my, ex, pm0, q, a.omega);
       }
       __syncthreads();
       // accumulate per cell: the (up to) 4 patches of this layer touching the cell, fixed order
@@ -726,7 +753,11 @@ __global__ void __launch_bounds__(C::THREADS, 1) stream_kernel(StreamArgs a)
       __syncthreads();
       // cell layer j is complete: write it, clear its accumulator for layer j+2
       write_layer<C>(a, alo, item, j, z0 + j, j == 0 && tz > 0, s_cxy, s_cshared, e, g, true);
-      if(more) wait_async_all();
+      if(more)
+      {
+        wait_async_all();
+        convert_layer<C>(s_raw + (j % 2) * C::LAYER, s_f32 + (j % 2) * C::LAYERF, e, g);
+      }
       __syncthreads();
     }
     // last cell layer of the item
