@@ -242,18 +242,34 @@ __device__ __forceinline__ void mpass(float *__restrict__ data, const float *__r
 // Even/odd passes of mirror-symmetric directions (n = 2h): forward t_e = Se^T (r_i + r_{n-1-i}),
 // t_o = So^T (r_i - r_{n-1-i}) stored at transformed positions [0,h) and [h,n); backward
 // u_i = Se t_e + So t_o, u_{n-1-i} = Se t_e - So t_o.  Half the FMAs of a full n x n pass.
-template<int H, int HPAD, int NPT>
-__device__ __forceinline__ void eo_forward(float (&r)[NPT][2 * H], const float *__restrict__ eo,
-                                           float (&t)[NPT][2 * H])
+// NPT pencils of N values in pairs of registers: pencils 2p and 2p+1 share the float2 v[p][m]
+// (for odd NPT the last pair's y half is a spare), so the even/odd passes below run on packed
+// FP32 instructions (FFMA2 / FADD2: two pencils per instruction, the same rounding as two scalar
+// operations)
+template<int NPT, int N>
+struct Pencils
 {
+  static constexpr int P = (NPT + 1) / 2;
+  float2 v[P][N];
+  __device__ __forceinline__ float &at(int j, int m) { return (j & 1) ? v[j >> 1][m].y : v[j >> 1][m].x; }
+};
+
+__device__ __forceinline__ float2 bcast2(float x) { return make_float2(x, x); }
+
+template<int H, int HPAD, int NPT>
+__device__ __forceinline__ void eo_forward(Pencils<NPT, 2 * H> &r, const float *__restrict__ eo,
+                                           Pencils<NPT, 2 * H> &t)
+{
+  constexpr int P = Pencils<NPT, 2 * H>::P;
+  const float2 m1 = bcast2(-1.f);
 #pragma unroll
-  for(int j = 0; j < NPT; ++j)
+  for(int p = 0; p < P; ++p)
 #pragma unroll
     for(int i = 0; i < H; ++i)
     {
-      const float a = r[j][i], b = r[j][2 * H - 1 - i];
-      r[j][i] = a + b;
-      r[j][2 * H - 1 - i] = a - b;  // odd part stored mirrored
+      const float2 a = r.v[p][i], b = r.v[p][2 * H - 1 - i];
+      r.v[p][i] = __fadd2_rn(a, b);
+      r.v[p][2 * H - 1 - i] = __ffma2_rn(b, m1, a);  // a - b, stored mirrored
     }
 #pragma unroll
   for(int par = 0; par < 2; ++par)
@@ -261,9 +277,9 @@ __device__ __forceinline__ void eo_forward(float (&r)[NPT][2 * H], const float *
     for(int k = 0; k < H; ++k)
     {
       const float4 *row = reinterpret_cast<const float4 *>(eo + (par * H + k) * HPAD);
-      float acc[NPT];
+      float2 acc[P];
 #pragma unroll
-      for(int j = 0; j < NPT; ++j) acc[j] = 0.f;
+      for(int p = 0; p < P; ++p) acc[p] = bcast2(0.f);
 #pragma unroll
       for(int m4 = 0; m4 < HPAD / 4; ++m4)
       {
@@ -273,31 +289,31 @@ __device__ __forceinline__ void eo_forward(float (&r)[NPT][2 * H], const float *
         for(int w = 0; w < 4; ++w)
           if(m4 * 4 + w < H)
           {
-            constexpr int dummy = 0;
-            (void)dummy;
             const int i = m4 * 4 + w < H ? m4 * 4 + w : 0;
+            const float2 c = bcast2(vv[w]);
 #pragma unroll
-            for(int j = 0; j < NPT; ++j)
-              acc[j] = fmaf(vv[w], par == 0 ? r[j][i] : r[j][2 * H - 1 - i], acc[j]);
+            for(int p = 0; p < P; ++p) acc[p] = __ffma2_rn(c, r.v[p][par == 0 ? i : 2 * H - 1 - i], acc[p]);
           }
       }
 #pragma unroll
-      for(int j = 0; j < NPT; ++j) t[j][par * H + k] = acc[j];
+      for(int p = 0; p < P; ++p) t.v[p][par * H + k] = acc[p];
     }
 }
 
 template<int H, int HPAD, int NPT>
-__device__ __forceinline__ void eo_backward(const float (&t)[NPT][2 * H], const float *__restrict__ eo,
-                                            float (&u)[NPT][2 * H])
+__device__ __forceinline__ void eo_backward(const Pencils<NPT, 2 * H> &t, const float *__restrict__ eo,
+                                            Pencils<NPT, 2 * H> &u)
 {
+  constexpr int P = Pencils<NPT, 2 * H>::P;
+  const float2 m1 = bcast2(-1.f);
 #pragma unroll
   for(int i = 0; i < H; ++i)
   {
     const float4 *re = reinterpret_cast<const float4 *>(eo + (2 * H + i) * HPAD);
     const float4 *ro = reinterpret_cast<const float4 *>(eo + (3 * H + i) * HPAD);
-    float E[NPT], O[NPT];
+    float2 E[P], O[P];
 #pragma unroll
-    for(int j = 0; j < NPT; ++j) E[j] = O[j] = 0.f;
+    for(int p = 0; p < P; ++p) E[p] = O[p] = bcast2(0.f);
 #pragma unroll
     for(int m4 = 0; m4 < HPAD / 4; ++m4)
     {
@@ -308,19 +324,20 @@ __device__ __forceinline__ void eo_backward(const float (&t)[NPT][2 * H], const 
         if(m4 * 4 + w < H)
         {
           const int k = m4 * 4 + w < H ? m4 * 4 + w : 0;
+          const float2 ce = bcast2(ee[w]), co = bcast2(oo[w]);
 #pragma unroll
-          for(int j = 0; j < NPT; ++j)
+          for(int p = 0; p < P; ++p)
           {
-            E[j] = fmaf(ee[w], t[j][k], E[j]);
-            O[j] = fmaf(oo[w], t[j][H + k], O[j]);
+            E[p] = __ffma2_rn(ce, t.v[p][k], E[p]);
+            O[p] = __ffma2_rn(co, t.v[p][H + k], O[p]);
           }
         }
     }
 #pragma unroll
-    for(int j = 0; j < NPT; ++j)
+    for(int p = 0; p < P; ++p)
     {
-      u[j][i] = E[j] + O[j];
-      u[j][2 * H - 1 - i] = E[j] - O[j];
+      u.v[p][i] = __fadd2_rn(E[p], O[p]);
+      u.v[p][2 * H - 1 - i] = __ffma2_rn(O[p], m1, E[p]);
     }
   }
 }
@@ -339,7 +356,7 @@ __device__ __forceinline__ void spass(float *__restrict__ data, const float *__r
   {
     constexpr int H = N / 2;
     constexpr int stride = DIR == 0 ? 1 : DIR == 1 ? SX : SXY;
-    float r[NPT][N], o[NPT][N];
+    Pencils<NPT, N> r, o;
     int base[NPT];
 #pragma unroll
     for(int j = 0; j < NPT; ++j)
@@ -347,8 +364,11 @@ __device__ __forceinline__ void spass(float *__restrict__ data, const float *__r
       int pa, pb;
       base[j] = pencil_of<MAP, N, SX, SXY, DIR>(pm, q + j * TPP, pa, pb);
 #pragma unroll
-      for(int m = 0; m < N; ++m) r[j][m] = data[base[j] + m * stride];
+      for(int m = 0; m < N; ++m) r.at(j, m) = data[base[j] + m * stride];
     }
+    if constexpr(NPT % 2 == 1)
+#pragma unroll
+      for(int m = 0; m < N; ++m) r.at(NPT, m) = 0.f;
     if constexpr(FWD)
       eo_forward<H, HPAD, NPT>(r, ent, o);
     else
@@ -356,7 +376,7 @@ __device__ __forceinline__ void spass(float *__restrict__ data, const float *__r
 #pragma unroll
     for(int j = 0; j < NPT; ++j)
 #pragma unroll
-      for(int i = 0; i < N; ++i) data[base[j] + i * stride] = SCALED ? o[j][i] * scale : o[j][i];
+      for(int i = 0; i < N; ++i) data[base[j] + i * stride] = SCALED ? o.at(j, i) * scale : o.at(j, i);
   }
 }
 
@@ -368,29 +388,39 @@ __device__ __forceinline__ void mpass_x_from_layers(float *__restrict__ data, co
                                                     const float *__restrict__ St, const int *__restrict__ pm,
                                                     int px, int py, int q)
 {
-  float r[NPT][N];
-  int base[NPT];
+  int base[NPT], row[NPT];
+  const float *layer[NPT];
 #pragma unroll
   for(int j = 0; j < NPT; ++j)
   {
     int y, z;
     base[j] = pencil_of<MAP, N, SX, SXY, 0>(pm, q + j * TPP, y, z);
-    const float *layer = z >= K1 ? hi : lo;
-    const int row = px * CD + RS * (py + y / K1) + K1 * (y % K1) + K1 * K1 * (z % K1);
-#pragma unroll
-    for(int m = 0; m < N; ++m) r[j][m] = layer[row + (m / K1) * CD + (m % K1)];
+    layer[j] = z >= K1 ? hi : lo;
+    row[j] = px * CD + RS * (py + y / K1) + K1 * (y % K1) + K1 * K1 * (z % K1);
   }
   if constexpr(SYM)
   {
-    float t[NPT][N];
+    Pencils<NPT, N> r, t;
+#pragma unroll
+    for(int j = 0; j < NPT; ++j)
+#pragma unroll
+      for(int m = 0; m < N; ++m) r.at(j, m) = layer[j][row[j] + (m / K1) * CD + (m % K1)];
+    if constexpr(NPT % 2 == 1)
+#pragma unroll
+      for(int m = 0; m < N; ++m) r.at(NPT, m) = 0.f;
     eo_forward<N / 2, HPAD, NPT>(r, St, t);
 #pragma unroll
     for(int j = 0; j < NPT; ++j)
 #pragma unroll
-      for(int i = 0; i < N; ++i) data[base[j] + i] = t[j][i];
+      for(int i = 0; i < N; ++i) data[base[j] + i] = t.at(j, i);
   }
   else
   {
+    float r[NPT][N];
+#pragma unroll
+    for(int j = 0; j < NPT; ++j)
+#pragma unroll
+      for(int m = 0; m < N; ++m) r[j][m] = layer[j][row[j] + (m / K1) * CD + (m % K1)];
 #pragma unroll
     for(int i = 0; i < N; ++i)
     {
@@ -424,7 +454,6 @@ __device__ __forceinline__ void zpass_solve(float *__restrict__ data, const floa
                                             const float *__restrict__ lamz, const int *__restrict__ pm, int q)
 {
   constexpr int stride = SXY;
-  float r[NPT][N], t[NPT][N];
   float lxy[NPT];
   int base[NPT];
 #pragma unroll
@@ -433,27 +462,38 @@ __device__ __forceinline__ void zpass_solve(float *__restrict__ data, const floa
     int px_, py_;
     base[j] = pencil_of<MAP, N, SX, SXY, 2>(pm, q + j * TPP, px_, py_);
     lxy[j] = lamx[px_] + lamy[py_];
-#pragma unroll
-    for(int m = 0; m < N; ++m) r[j][m] = data[base[j] + m * stride];
   }
   if constexpr(SYM)
   {
+    Pencils<NPT, N> r, t;
+#pragma unroll
+    for(int j = 0; j < NPT; ++j)
+#pragma unroll
+      for(int m = 0; m < N; ++m) r.at(j, m) = data[base[j] + m * stride];
+    if constexpr(NPT % 2 == 1)
+#pragma unroll
+      for(int m = 0; m < N; ++m) r.at(NPT, m) = 0.f;
     eo_forward<N / 2, HPAD, NPT>(r, ez, t);
 #pragma unroll
     for(int i = 0; i < N; ++i)
     {
       const float lz = lamz[i];
 #pragma unroll
-      for(int j = 0; j < NPT; ++j) t[j][i] = __fdividef(t[j][i], lxy[j] + lz);
+      for(int j = 0; j < NPT; ++j) t.at(j, i) = __fdividef(t.at(j, i), lxy[j] + lz);
     }
     eo_backward<N / 2, HPAD, NPT>(t, ez, r);
 #pragma unroll
     for(int j = 0; j < NPT; ++j)
 #pragma unroll
-      for(int i = 0; i < N; ++i) data[base[j] + i * stride] = r[j][i];
+      for(int i = 0; i < N; ++i) data[base[j] + i * stride] = r.at(j, i);
   }
   else
   {
+    float r[NPT][N], t[NPT][N];
+#pragma unroll
+    for(int j = 0; j < NPT; ++j)
+#pragma unroll
+      for(int m = 0; m < N; ++m) r[j][m] = data[base[j] + m * stride];
 #pragma unroll
     for(int i = 0; i < N; ++i)
     {
