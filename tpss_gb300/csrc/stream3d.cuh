@@ -445,6 +445,15 @@ __device__ __forceinline__ void mpass_x_from_layers(float *__restrict__ data, co
   }
 }
 
+// 1/x by the hardware's approximate reciprocal (PTX rcp.approx.ftz.f32, max. 1 ulp); the divisors
+// here are sums of positive eigenvalues
+__device__ __forceinline__ float rcp_approx(float x)
+{
+  float y;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
 // direction 2 in registers: S^T along z, division by the eigenvalue sums, S along z -- the
 // pencil a thread transforms forward is the one it transforms back, so the intermediate never
 // goes through shared memory
@@ -479,7 +488,7 @@ __device__ __forceinline__ void zpass_solve(float *__restrict__ data, const floa
     {
       const float lz = lamz[i];
 #pragma unroll
-      for(int j = 0; j < NPT; ++j) t.at(j, i) = __fdividef(t.at(j, i), lxy[j] + lz);
+      for(int j = 0; j < NPT; ++j) t.at(j, i) = t.at(j, i) * rcp_approx(lxy[j] + lz);
     }
     eo_backward<N / 2, HPAD, NPT>(t, ez, r);
 #pragma unroll
@@ -514,7 +523,7 @@ __device__ __forceinline__ void zpass_solve(float *__restrict__ data, const floa
       }
       const float lz = lamz[i];
 #pragma unroll
-      for(int j = 0; j < NPT; ++j) t[j][i] = __fdividef(acc[j], lxy[j] + lz);
+      for(int j = 0; j < NPT; ++j) t[j][i] = acc[j] * rcp_approx(lxy[j] + lz);
     }
 #pragma unroll
     for(int i = 0; i < N; ++i)
@@ -558,26 +567,40 @@ __device__ __forceinline__ int64_t cell_first_xy(const StreamArgs &a, int xy, in
   return a.cell_start ? a.cell_start[cell] : cell * C::CD;
 }
 
+// The element loops below give a thread the cells g, g + G, g + 2G, ... of a layer (DoF e of
+// each). They are unrolled in phases -- all shared-memory reads first, then the dependent work --
+// so that a thread's reads are in flight together instead of one round trip per cell.
+
 // asynchronous copy (cp.async, 8 bytes) of cell layer cz of the column (the item's cells of
 // the table cxy) into the FP64 staging buffer; cells outside are zero-filled
 template<class C>
 __device__ __forceinline__ void copy_layer_async(const StreamArgs &a, const int *cxy, int cz, double *raw,
                                                  int e, int g)
 {
+  constexpr int IT = (C::LCELLS + C::G - 1) / C::G;
   if(g < C::G)
-    for(int cell = g; cell < C::LCELLS; cell += C::G)
+  {
+    int xy[IT];
+#pragma unroll
+    for(int it = 0; it < IT; ++it)
     {
-      const int xy = cxy[cell];
-      const int i = cell * C::CD + e;
-      if(xy >= 0)
+      const int cell = g + it * C::G;
+      xy[it] = cell < C::LCELLS ? cxy[cell] : -2;
+    }
+#pragma unroll
+    for(int it = 0; it < IT; ++it)
+    {
+      const int cell = g + it * C::G, i = cell * C::CD + e;
+      if(xy[it] >= 0)
       {
-        const double *src = a.src + cell_first_xy<C>(a, xy, cz) + e;
+        const double *src = a.src + cell_first_xy<C>(a, xy[it], cz) + e;
         const unsigned saddr = (unsigned)__cvta_generic_to_shared(raw + i);
         asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(saddr), "l"(src) : "memory");
       }
-      else
+      else if(xy[it] == -1)
         raw[i] = 0.0;
     }
+  }
   asm volatile("cp.async.commit_group;\n" ::: "memory");
 }
 
@@ -589,12 +612,27 @@ __device__ __forceinline__ void wait_async_all() { asm volatile("cp.async.wait_g
 template<class C>
 __device__ __forceinline__ void convert_layer(const double *raw, float *f32, int e, int g)
 {
+  constexpr int IT = (C::LCELLS + C::G - 1) / C::G;
   if(g < C::G)
-    for(int cell = g; cell < C::LCELLS; cell += C::G)
+  {
+    double v[IT];
+#pragma unroll
+    for(int it = 0; it < IT; ++it)
     {
-      const int lx = cell % C::CX, ly = cell / C::CX;
-      f32[lx * C::CD + ly * C::RSTRIDE + e] = float(raw[cell * C::CD + e]);
+      const int cell = g + it * C::G;
+      v[it] = cell < C::LCELLS ? raw[cell * C::CD + e] : 0.0;
     }
+#pragma unroll
+    for(int it = 0; it < IT; ++it)
+    {
+      const int cell = g + it * C::G;
+      if(cell < C::LCELLS)
+      {
+        const int lx = cell % C::CX, ly = cell / C::CX;
+        f32[lx * C::CD + ly * C::RSTRIDE + e] = float(v[it]);
+      }
+    }
+  }
 }
 
 // write one completed cell layer: cells owned by the item to dst, shared cells to the halo
@@ -603,26 +641,40 @@ __device__ __forceinline__ void write_layer(const StreamArgs &a, float *accl, in
                                             bool zshared, const int *cxy, const int *cshared, int e,
                                             int g, bool clear)
 {
+  constexpr int IT = (C::LCELLS + C::G - 1) / C::G;
   if(g >= C::G) return;
-  for(int cell = g; cell < C::LCELLS; cell += C::G)
+  int xy[IT], sh[IT];
+  float v[IT];
+#pragma unroll
+  for(int it = 0; it < IT; ++it)
   {
-    const int xy = cxy[cell];
-    if(xy < 0) continue;
-    const int i = cell * C::CD + e;
-    float v = accl[i];
-    if(cshared[cell] || zshared)
-      a.halo[((size_t)item * (C::BZ + 1) * C::LCELLS + (size_t)lz * C::LCELLS + cell) * C::CD + e] = v;
+    const int cell = g + it * C::G;
+    xy[it] = cell < C::LCELLS ? cxy[cell] : -1;
+    sh[it] = cell < C::LCELLS ? cshared[cell] : 0;
+    v[it] = cell < C::LCELLS ? accl[cell * C::CD + e] : 0.f;
+  }
+#pragma unroll
+  for(int it = 0; it < IT; ++it)
+  {
+    const int cell = g + it * C::G;
+    if(xy[it] < 0) continue;
+    float w = v[it];
+    if(sh[it] || zshared)
+      a.halo[((size_t)item * (C::BZ + 1) * C::LCELLS + (size_t)lz * C::LCELLS + cell) * C::CD + e] = w;
     else
     {
       if(a.ras)
       {
-        const int cx = xy % a.nc[0], cy = xy / a.nc[0];
-        v /= multiplicity(cx, a.nc[0]) * multiplicity(cy, a.nc[1]) * multiplicity(cz, a.nc[2]);
+        const int cx = xy[it] % a.nc[0], cy = xy[it] / a.nc[0];
+        w /= multiplicity(cx, a.nc[0]) * multiplicity(cy, a.nc[1]) * multiplicity(cz, a.nc[2]);
       }
-      a.dst[cell_first_xy<C>(a, xy, cz) + e] = double(v);
+      a.dst[cell_first_xy<C>(a, xy[it], cz) + e] = double(w);
     }
-    if(clear) accl[i] = 0.f;
   }
+  if(clear)
+#pragma unroll
+    for(int it = 0; it < IT; ++it)
+      if(xy[it] >= 0) accl[(g + it * C::G) * C::CD + e] = 0.f;
 }
 
 template<class C>
@@ -779,17 +831,36 @@ __global__ void __launch_bounds__(C::THREADS, 1) stream_kernel(StreamArgs a)
       // accumulate per cell: the (up to) 4 patches of this layer touching the cell, fixed order
       float *alo = s_acc + (j % 2) * C::LAYER, *ahi = s_acc + ((j + 1) % 2) * C::LAYER;
       if(g < C::G)
-        for(int cl = g; cl < 2 * C::LCELLS; cl += C::G)
+      {
+        constexpr int IT = (2 * C::LCELLS + C::G - 1) / C::G;
+        float sum[IT], old[IT];
+#pragma unroll
+        for(int it = 0; it < IT; ++it)
         {
-          const int L = cl >= C::LCELLS, cell = cl - L * C::LCELLS;
-          const int4 o = reinterpret_cast<const int4 *>(s_aoff)[cl];
-          float sum = 0.f;
-          if(o.x >= 0) sum += s_work[o.x + e_patch];
-          if(o.y >= 0) sum += s_work[o.y + e_patch];
-          if(o.z >= 0) sum += s_work[o.z + e_patch];
-          if(o.w >= 0) sum += s_work[o.w + e_patch];
-          (L ? ahi : alo)[cell * CD + e] += sum;
+          const int cl = g + it * C::G;
+          sum[it] = 0.f;
+          if(cl < 2 * C::LCELLS)
+          {
+            const int4 o = reinterpret_cast<const int4 *>(s_aoff)[cl];
+            if(o.x >= 0) sum[it] += s_work[o.x + e_patch];
+            if(o.y >= 0) sum[it] += s_work[o.y + e_patch];
+            if(o.z >= 0) sum[it] += s_work[o.z + e_patch];
+            if(o.w >= 0) sum[it] += s_work[o.w + e_patch];
+          }
         }
+#pragma unroll
+        for(int it = 0; it < IT; ++it)
+        {
+          const int cl = g + it * C::G, L = cl >= C::LCELLS, cell = cl - L * C::LCELLS;
+          old[it] = cl < 2 * C::LCELLS ? (L ? ahi : alo)[cell * CD + e] : 0.f;
+        }
+#pragma unroll
+        for(int it = 0; it < IT; ++it)
+        {
+          const int cl = g + it * C::G, L = cl >= C::LCELLS, cell = cl - L * C::LCELLS;
+          if(cl < 2 * C::LCELLS) (L ? ahi : alo)[cell * CD + e] = old[it] + sum[it];
+        }
+      }
       __syncthreads();
       // cell layer j is complete: write it, clear its accumulator for layer j+2
       write_layer<C>(a, alo, item, j, z0 + j, j == 0 && tz > 0, s_cxy, s_cshared, e, g, true);
