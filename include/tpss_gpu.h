@@ -199,11 +199,14 @@ int tpss_precond_vmult_static_scratch(tpss_precond *p, double *dst, const double
  * vmult calls.  On return dst = P src, *chosen is the selected variant, ms_per_variant (optional,
  * >= 6 entries) the measured milliseconds per application and *n_variants their count (1 when the
  * level has a single kernel). */
-/* vmult with dst and src in HOST memory (the reference's vmult on host vectors; the adapter
- * in INTEGRATION copies in, applies and copies out). For the streamed smoother the copies are
- * pipelined with the kernel along z (three internal streams); otherwise copy-in, vmult,
- * copy-out on `stream`. Stream-ordered: dst is complete when `stream` reaches this point.
- * Pin the host buffers (cudaHostRegister / cudaMallocHost) for the copies to overlap. */
+/* vmult with dst and src in HOST memory (the reference's vmult on host vectors; a device-vector
+ * adapter would copy in, apply and copy out). For the streamed smoother the copies are pipelined
+ * with the kernel along z (three internal streams), in chunks of one work item deep; the pipeline
+ * runs the 4-layer-deep decomposition of the chosen kind (variant 5 when variant 4 or 5 is chosen,
+ * else 2) for a short fill and drain, so its result carries that variant's FP32 rounding.
+ * Otherwise copy-in, vmult, copy-out on `stream`. Stream-ordered: dst is complete when `stream`
+ * reaches this point. Pin the host buffers (cudaHostRegister / cudaMallocHost) for the copies to
+ * overlap. */
 int tpss_precond_vmult_host(tpss_precond *p, double *dst, const double *src, void *stream);
 int tpss_precond_autotune(tpss_precond *p, double *dst, const double *src, int reps, int *chosen,
                           double *ms_per_variant, int *n_variants, void *stream);

@@ -436,16 +436,20 @@ def test_streamed_variants_and_autotune(tpss, oracle, cuda, k, nc):
     assert rel_err(d2.cpu().numpy(), ref) <= 2e-5
 
 
-@pytest.mark.parametrize("k,nc,variant", [(4, (9, 6, 19), 0), (3, (7, 5, 33), 2), (2, (6, 6, 17), 3), (1, (5, 9, 40), 1)])
+@pytest.mark.parametrize("k,nc,variant", [(4, (9, 6, 19), 0), (3, (7, 5, 33), 2), (2, (6, 6, 17), 3), (1, (5, 9, 40), 1),
+                                         (4, (10, 7, 21), 4), (3, (6, 9, 18), 5)])
 def test_vmult_host_buffers_pipelined(tpss, oracle, cuda, k, nc, variant):
     """The host-buffer entry point (copies pipelined with the streamed kernel along z) gives
-    the oracle's result and the device path's bits; also for the per-color path."""
+    the oracle's result and the bits of the device path with the decomposition the pipeline
+    runs (the 4-layer-deep twin of the chosen one: 5 for the warp-per-patch variants 4 and 5,
+    2 otherwise); also for the per-color path."""
     import torch
     N = int(np.prod(nc)) * (k + 1) ** 3
     src = philox(500 + k, N)
     ref = oracle.schwarz_vmult(3, k, nc, src, patch_variant=1, omega=0.15)
     ad = tpss.SubdomainHandler.AdditionalData(dim=3, degree=k, n_cells=nc, patch_variant=1)
     sh = tpss.SubdomainHandler(ad)
+    host_variant = 5 if variant in (4, 5) else 2
     for kv in (2, 1):
         p = tpss.SchwarzPreconditioner()
         p.initialize(sh, None, tpss.SchwarzPreconditioner.AdditionalData(
@@ -454,8 +458,11 @@ def test_vmult_host_buffers_pipelined(tpss, oracle, cuda, k, nc, variant):
         h_dst = torch.full((N,), float("nan"), dtype=torch.float64).pin_memory()
         p.vmult_host(h_dst, h_src)
         torch.cuda.synchronize()
+        pd = tpss.SchwarzPreconditioner()
+        pd.initialize(sh, None, tpss.SchwarzPreconditioner.AdditionalData(
+            relaxation=0.15, precision=1, kernel_variant=kv, stream_variant=host_variant))
         d = torch.empty(N, dtype=torch.float64, device=cuda)
-        p.vmult(d, h_src.to(cuda))
+        pd.vmult(d, h_src.to(cuda))
         torch.cuda.synchronize()
         assert rel_err(h_dst.numpy(), ref) <= 2e-5
         assert np.array_equal(h_dst.numpy(), d.cpu().numpy())

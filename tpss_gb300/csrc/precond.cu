@@ -795,7 +795,15 @@ extern "C" int tpss_precond_vmult_host(tpss_precond *p, double *dst, const doubl
     ScopedTimer step(p, 4, s);
     if(L.smoother_variant == TPSS_ADDITIVE && use_stream(p) && !p->desc.check_finite)
     {
-      const StreamLaunch l = stream_launch(p, p->pipe.dst.ptr, p->pipe.src.ptr);
+      // The pipeline is copy-bound (262 MB each way at 64^3 DGQ4 against a 1.3 ms kernel); its
+      // fill and drain are one chunk of one z-item, so it runs the 4-layer-deep twin of the
+      // chosen decomposition (warp per patch: 4 -> 5, otherwise 2), which halves both.
+      StreamLaunch l = stream_launch(p, p->pipe.dst.ptr, p->pipe.src.ptr);
+      const int hv = (p->stream_variant == 4 || p->stream_variant == 5) ? 5 : 2;
+      l.variant = hv;
+      l.fix_rec = &p->fix_rec[hv];
+      l.fix_n = &p->fix_n[hv];
+      l.fix_layer = &p->fix_layer[hv];
       if(launch_stream3d_host(L, l, p->pipe, dst, src, s)) return;
     }
     TPSS_CUDA(cudaMemcpyAsync(p->pipe.src.ptr, src, sizeof(double) * N, cudaMemcpyHostToDevice, s));
