@@ -426,6 +426,16 @@ def operator_time(tpss, sh, src, W):
     e1.record()
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / reps
+    # the same product in FP32 arithmetic (the level operator of a single-precision V-cycle)
+    for _ in range(3):
+        op.vmult_fp32(dst, src)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(reps):
+        op.vmult_fp32(dst, src)
+    e1.record()
+    torch.cuda.synchronize()
+    ms32 = e0.elapsed_time(e1) / reps
     k, dim = sh.get_additional_data().degree, sh.get_additional_data().dim
     cells = W["N"] // (k + 1) ** dim
     npt = k + 1
@@ -434,7 +444,8 @@ def operator_time(tpss, sh, src, W):
     fma_cell = dim * npt ** (dim - 1) * (dim * npt * npt + 8 * npt)
     return {"ms": ms, "dof_per_s": W["N"] / (ms * 1e-3),
             "fp64_tflops": 2 * fma_cell * cells / (ms * 1e-3) / 1e12,
-            "algorithmic_fma_per_cell": fma_cell}
+            "algorithmic_fma_per_cell": fma_cell, "fp32_ms": ms32,
+            "fp32_tflops": 2 * fma_cell * cells / (ms32 * 1e-3) / 1e12}
 
 
 def solve_times(tpss, args):
@@ -445,9 +456,11 @@ def solve_times(tpss, args):
     n, k, dim = args.cells, args.degree, args.dim
     N = n ** dim * (k + 1) ** dim
     f = torch.tensor(philox_src(N, args.seed), dtype=torch.float64, device="cuda")
-    for name, prec in (("fp32", tpss.Precision.fp32), ("fp64", tpss.Precision.fp64)):
+    for name, prec, opp in (("fp32", tpss.Precision.fp32, tpss.Precision.fp64),
+                            ("fp32_vcycle", tpss.Precision.fp32, tpss.Precision.fp32),
+                            ("fp64", tpss.Precision.fp64, tpss.Precision.fp64)):
         mg = tpss.MultigridSolver(dim, k, 1, n, relaxation=args.omega, precision=prec,
-                                  coarse_solver=1, use_graph=True)
+                                  coarse_solver=1, use_graph=True, vcycle_precision=opp)
         u = torch.zeros_like(f)
         mg.vmult(u, f)  # warm-up: graph capture
         torch.cuda.synchronize()
@@ -458,8 +471,11 @@ def solve_times(tpss, args):
         res[name] = {"seconds": el, "iterations": it, "final_rel_residual": float(hist[-1] / hist[0])}
         del mg
     res["fp32_over_fp64_time"] = res["fp32"]["seconds"] / res["fp64"]["seconds"]
+    res["fp32_vcycle_over_fp64_time"] = res["fp32_vcycle"]["seconds"] / res["fp64"]["seconds"]
     res["workload"] = (f"CG + V-cycle (1 pre/1 post additive vertex-patch Schwarz step, omega "
-                       f"{args.omega}), 3D SIPG DGQ{k} {n}^3, f ~ U[-1,1], to 1e-8 rel. residual")
+                       f"{args.omega}), 3D SIPG DGQ{k} {n}^3, f ~ U[-1,1], to 1e-8 rel. residual; "
+                       f"fp32: FP32 smoothers; fp32_vcycle: FP32 smoothers and FP32 level operators "
+                       f"in the V-cycle (outer CG and coarse solve FP64); fp64: all FP64")
     return res
 
 

@@ -118,6 +118,11 @@ void tpss_layout_destroy(tpss_layout *layout);
 int tpss_operator_create(const tpss_layout *layout, double ip_factor, tpss_operator **out);
 /* MF::Operator::vmult (apps/laplace_integrator.h:578-598), FP64. */
 int tpss_operator_vmult(tpss_operator *op, double *dst, const double *src, void *stream);
+/* The same product in FP32 arithmetic on FP64 vectors (src is converted once into a scratch
+ * copy owned by the operator; dst is written in FP64): the level operator of a single-precision
+ * V-cycle (no counterpart in the reference, which runs its multigrid in the vector precision).
+ * Distorted (mapped) levels compute in FP64. */
+int tpss_operator_vmult_fp32(tpss_operator *op, double *dst, const double *src, void *stream);
 void tpss_operator_destroy(tpss_operator *op);
 
 /* SchwarzPreconditioner::AdditionalData (schwarz_preconditioner.h:495-515) plus the
@@ -269,6 +274,11 @@ typedef struct tpss_mg_desc
                                   2^dim is damped by relaxation * 2^dim / (1.05 lambda_max),
                                   lambda_max from 30 power steps at setup (no counterpart in
                                   the reference) */
+  int vcycle_precision;        /* TPSS_FP64 (the reference) or TPSS_FP32: inside the V-cycle the
+                                  level operators of the smoothing residuals and the transfers
+                                  compute in FP32 (tpss_operator_vmult_fp32); the outer CG
+                                  operator and the coarse solve stay FP64 (no counterpart in the
+                                  reference, whose multigrid runs in the vector precision) */
 } tpss_mg_desc;
 
 int tpss_mg_create(const tpss_mg_desc *desc, tpss_mg **out);

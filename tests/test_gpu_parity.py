@@ -191,6 +191,56 @@ def test_operator_parity(tpss, oracle, cuda, dim, k, nc, ip):
     assert rel_err(d.cpu().numpy(), ref) <= 1e-12
 
 
+@pytest.mark.parametrize("dim,k,nc,ip", [(2, 3, (5, 4), 1.0), (3, 2, (3, 4, 2), 2.5), (3, 4, (6, 5, 4), 1.0),
+                                         (2, 7, (3, 3), 1.0), (3, 1, (7, 3, 5), 1.0)])
+def test_operator_fp32_parity(tpss, oracle, cuda, dim, k, nc, ip):
+    """The single-precision level operator (FP32 arithmetic, FP64 vectors) against the FP64
+    oracle: relative error of FP32 rounding (tolerance 1e-5 in the 2-norm)."""
+    import torch
+    ad = tpss.SubdomainHandler.AdditionalData(dim=dim, degree=k, n_cells=nc, patch_variant=1)
+    sh = tpss.SubdomainHandler(ad)
+    op = tpss.LaplaceOperator(sh, ip)
+    src = philox(19, sh.n_dofs())
+    d = torch.full((sh.n_dofs(),), float("nan"), dtype=torch.float64, device=cuda)
+    op.vmult_fp32(d, torch.tensor(src, dtype=torch.float64, device=cuda))
+    ref = oracle.sipg_vmult(dim, k, nc, src, ip=ip)
+    err = rel_err(d.cpu().numpy(), ref)
+    assert 0.0 < err <= 1e-5, err
+
+
+def test_mg_fp32_vcycle_operator(tpss, oracle, xcheck, cuda):
+    """CG with a V-cycle whose smoothing residuals use the FP32 level operator (FP32 smoothers):
+    converges to the tolerance in at most two more iterations than the FP64 V-cycle operator."""
+    import torch
+    for c in json.load(open(os.path.join(GOLDEN, "mg_iterations.json"))):
+        if c["smoother_variant"] != 0:
+            continue
+        N = c["n_cells_fine"] ** c["dim"] * (c["k"] + 1) ** c["dim"]
+        if c["rhs"] == "random":
+            f = np.random.Generator(np.random.Philox(c["rhs_seed"])).uniform(-1, 1, N)
+        else:
+            f = xcheck.bells_load_vector(c["dim"], c["k"], c["n_cells_fine"])
+        its = {}
+        for opp in (0, 1):
+            mg = tpss.MultigridSolver(c["dim"], c["k"], c["n_rep"], c["n_cells_fine"],
+                                      patch_variant=c["patch_variant"], smoother_variant=0,
+                                      precision=1, coarse_solver=1, vcycle_precision=opp)
+            u = torch.zeros(N, dtype=torch.float64, device=cuda)
+            ft = torch.tensor(f, dtype=torch.float64, device=cuda)
+            it, hist = mg.solve(u, ft, rel_tol=c["rel_tol"])
+            assert hist[-1] <= c["rel_tol"] * hist[0] * (1 + 1e-12), (c, opp)
+            # true residual of the returned solution with the FP64 operator
+            sh = tpss.SubdomainHandler(tpss.SubdomainHandler.AdditionalData(
+                dim=c["dim"], degree=c["k"], n_cells=(c["n_cells_fine"],) * c["dim"], patch_variant=1))
+            A = tpss.LaplaceOperator(sh, 1.0)
+            r = torch.empty_like(u)
+            A.vmult(r, u)
+            true_rel = float(torch.linalg.norm(ft - r) / torch.linalg.norm(ft))
+            assert true_rel <= 2 * c["rel_tol"], (c, opp, true_rel)
+            its[opp] = it
+        assert its[1] <= its[0] + 2, (c, its)
+
+
 @pytest.mark.parametrize("dim,k,ncc", [(2, 3, (3, 2)), (3, 2, (2, 3, 2)), (3, 5, (2, 2, 2))])
 def test_transfer_parity(tpss, oracle, cuda, dim, k, ncc):
     import torch

@@ -219,6 +219,12 @@ class LaplaceOperator:
         n = self.m()
         check(load().tpss_operator_vmult(self._h, _ptr(dst, n), _ptr(src, n), _stream(stream)))
 
+    def vmult_fp32(self, dst, src, stream=None):
+        """The same product in FP32 arithmetic (FP64 vectors): the level operator of a
+        single-precision V-cycle."""
+        n = self.m()
+        check(load().tpss_operator_vmult_fp32(self._h, _ptr(dst, n), _ptr(src, n), _stream(stream)))
+
     def Tvmult(self, dst, src, stream=None):
         self.vmult(dst, src, stream)
 
@@ -624,7 +630,7 @@ class MultigridSolver:
                  smoother_variant=SmootherVariant.additive, relaxation=None, ip_factor=1.0,
                  precision=Precision.fp64, coarse_tol=1e-12, coarse_solver=0, use_graph=True,
                  vertex_coords=None, surrogate_n_q=5, local_solver=0, model=None,
-                 auto_relaxation=False):
+                 auto_relaxation=False, vcycle_precision=Precision.fp64):
         if relaxation is None:
             relaxation = lookup_damping_factor(patch_variant, smoother_variant, dim)
         d = _lib.MgDesc()
@@ -636,6 +642,7 @@ class MultigridSolver:
         d.local_solver = int(local_solver)
         d.model = model.handle if model is not None else None
         d.auto_relaxation = int(auto_relaxation)
+        d.vcycle_precision = int(vcycle_precision)
         self._model = model
         d.dim, d.degree, d.n_rep, d.n_cells_fine = dim, degree, n_rep, n_cells_fine
         d.ip_factor, d.patch_variant, d.smoother_variant = float(ip_factor), patch_variant, smoother_variant

@@ -91,7 +91,8 @@ class MgDesc(C.Structure):
                 ("relaxation", C.c_double), ("precision", C.c_int), ("coarse_tol", C.c_double),
                 ("coarse_solver", C.c_int), ("use_graph", C.c_int),
                 ("vertex_coords", C.POINTER(C.c_double)), ("surrogate_n_q", C.c_int),
-                ("local_solver", C.c_int), ("model", C.c_void_p), ("auto_relaxation", C.c_int)]
+                ("local_solver", C.c_int), ("model", C.c_void_p), ("auto_relaxation", C.c_int),
+                ("vcycle_precision", C.c_int)]
 
 
 _vp = C.c_void_p
@@ -106,6 +107,7 @@ SIGNATURES = {
     "tpss_layout_destroy": (None, [_vp]),
     "tpss_operator_create": (C.c_int, [_vp, C.c_double, C.POINTER(_vp)]),
     "tpss_operator_vmult": (C.c_int, [_vp, _vp, _vp, _vp]),
+    "tpss_operator_vmult_fp32": (C.c_int, [_vp, _vp, _vp, _vp]),
     "tpss_operator_destroy": (None, [_vp]),
     "tpss_precond_create": (C.c_int, [_vp, _vp, C.POINTER(PrecondDesc), C.POINTER(_vp)]),
     "tpss_precond_create_shallow": (C.c_int, [_vp, C.POINTER(PrecondDesc), C.POINTER(_vp)]),

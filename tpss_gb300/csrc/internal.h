@@ -211,6 +211,8 @@ struct tpss_operator
   double ip = 1.0;
   tpss::DeviceBuffer<double> d_mass[3], d_blk[3];
   tpss::DeviceBuffer<double> d_fac[3];  // operator_factors_1d per direction
+  tpss::DeviceBuffer<float> d_fac32[3];  // the same in FP32 (single-precision level operator)
+  tpss::DeviceBuffer<float> x32;         // FP32 copy of the source (single-precision operator)
   int nblk_cells[3] = {0, 0, 0};
   std::unique_ptr<tpss::MappedOperator> mapped;  // set on distorted levels
 };
@@ -362,8 +364,12 @@ void extract_local_matrices(const tpss_layout &L, const tpss_operator &op, int64
 
 // operator and transfer (operator.cu)
 void operator_apply(tpss_operator *op, double *dst, const double *src, cudaStream_t s);
+// the same operator in FP32 arithmetic (FP64 vectors; the source is converted once into a
+// scratch copy): for the residuals inside a single-precision V-cycle. Distorted levels keep FP64.
+void operator_apply_f32(tpss_operator *op, double *dst, const double *src, cudaStream_t s);
+// single: FP32 arithmetic on the FP64 vectors (the transfers of a single-precision V-cycle)
 void transfer_apply(int dim, int k, const int *ncc, const double *E_dev, bool restrict_mode,
-                    double *coarse, double *fine, cudaStream_t s);
+                    double *coarse, double *fine, cudaStream_t s, bool single = false);
 
 // vector kernels (operator.cu)
 void vec_axpby(int64_t n, double a, const double *x, double b, double *y, cudaStream_t s);  // y = a x + b y

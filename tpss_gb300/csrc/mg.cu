@@ -228,6 +228,16 @@ struct tpss_mg
 
 namespace
 {
+// level operator of a smoothing residual inside the V-cycle (FP32 arithmetic for a
+// single-precision V-cycle)
+void level_residual_op(tpss_mg *mg, MgLevel &c, cudaStream_t s)
+{
+  if(mg->desc.vcycle_precision == TPSS_FP32)
+    operator_apply_f32(c.op, c.t.ptr, c.x.ptr, s);
+  else
+    operator_apply(c.op, c.t.ptr, c.x.ptr, s);
+}
+
 void down_sweep(tpss_mg *mg, cudaStream_t s)
 {
   const int top = (int)mg->lv.size() - 1;
@@ -235,10 +245,11 @@ void down_sweep(tpss_mg *mg, cudaStream_t s)
   {
     MgLevel &c = mg->lv[l], &f = mg->lv[l - 1];
     precond_vmult(c.P, c.x.ptr, c.b.ptr, s);
-    operator_apply(c.op, c.t.ptr, c.x.ptr, s);
+    level_residual_op(mg, c, s);
     vec_sub(c.L->n_dofs, c.b.ptr, c.t.ptr, s);
     TPSS_CUDA(cudaMemsetAsync(f.b.ptr, 0, sizeof(double) * f.L->n_dofs, s));
-    transfer_apply(c.L->dim, c.L->k, f.L->nc, mg->E, true, f.b.ptr, c.t.ptr, s);
+    transfer_apply(c.L->dim, c.L->k, f.L->nc, mg->E, true, f.b.ptr, c.t.ptr, s,
+                   mg->desc.vcycle_precision == TPSS_FP32);
   }
 }
 
@@ -248,8 +259,9 @@ void up_sweep(tpss_mg *mg, cudaStream_t s)
   for(int l = 1; l <= top; ++l)
   {
     MgLevel &c = mg->lv[l], &f = mg->lv[l - 1];
-    transfer_apply(c.L->dim, c.L->k, f.L->nc, mg->E, false, f.x.ptr, c.x.ptr, s);
-    operator_apply(c.op, c.t.ptr, c.x.ptr, s);
+    transfer_apply(c.L->dim, c.L->k, f.L->nc, mg->E, false, f.x.ptr, c.x.ptr, s,
+                   mg->desc.vcycle_precision == TPSS_FP32);
+    level_residual_op(mg, c, s);
     vec_sub(c.L->n_dofs, c.b.ptr, c.t.ptr, s);
     precond_vmult(c.P, c.r.ptr, c.t.ptr, s);
     vec_axpby(c.L->n_dofs, 1.0, c.r.ptr, 1.0, c.x.ptr, s);
@@ -437,6 +449,8 @@ extern "C" int tpss_mg_create(const tpss_mg_desc *d, tpss_mg **out)
     for(int nc = d->n_rep; nc <= d->n_cells_fine; nc *= 2) ++nl;
     TPSS_REQUIRE((d->n_rep << (nl - 1)) == d->n_cells_fine, "n_cells_fine must be n_rep * 2^L");
     TPSS_REQUIRE(nl >= 2, "at least two levels are needed");
+    TPSS_REQUIRE(d->vcycle_precision == TPSS_FP64 || d->vcycle_precision == TPSS_FP32,
+                 "vcycle_precision must be TPSS_FP64 or TPSS_FP32");
     auto mg = std::make_unique<tpss_mg>();
     mg->desc = *d;
     mg->lv.resize(nl);

@@ -26,18 +26,18 @@ __host__ __device__ constexpr int cpow(int b, int e) { return e == 0 ? 1 : b * c
 
 // in-place pencil contraction along DIR of one (NP)^DIM block: x <- (I x..x B x..x I) x,
 // B row-major NP x NP (TRANS: B^T)
-template<int DIM, int NP, int DIR, bool TRANS>
-__device__ __forceinline__ void pencil(double *x, const double *B, int p)
+template<int DIM, int NP, int DIR, bool TRANS, typename T>
+__device__ __forceinline__ void pencil(T *x, const T *B, int p)
 {
   constexpr int stride = cpow(NP, DIR);
   const int base = (p % stride) + (p / stride) * stride * NP;
-  double r[NP], o[NP];
+  T r[NP], o[NP];
 #pragma unroll
   for(int m = 0; m < NP; ++m) r[m] = x[base + m * stride];
 #pragma unroll
   for(int i = 0; i < NP; ++i)
   {
-    double acc = 0.0;
+    T acc = T(0);
 #pragma unroll
     for(int m = 0; m < NP; ++m) acc = fma(TRANS ? B[m * NP + i] : B[i * NP + m], r[m], acc);
     o[i] = acc;
@@ -46,20 +46,23 @@ __device__ __forceinline__ void pencil(double *x, const double *B, int p)
   for(int i = 0; i < NP; ++i) x[base + i * stride] = o[i];
 }
 
-template<int DIM, int NP, bool TRANS>
-__device__ __forceinline__ void pencil_dir(int dir, double *x, const double *B, int p)
+template<int DIM, int NP, bool TRANS, typename T>
+__device__ __forceinline__ void pencil_dir(int dir, T *x, const T *B, int p)
 {
   if(dir == 0) pencil<DIM, NP, 0, TRANS>(x, B, p);
   else if(dir == 1) pencil<DIM, NP, 1, TRANS>(x, B, p);
   else if constexpr(DIM == 3) pencil<DIM, NP, 2, TRANS>(x, B, p);
 }
 
+// T: arithmetic, shared-memory and source type (double; float for the single-precision level
+// operator, whose source is a pre-converted FP32 copy). The result is stored in FP64.
+template<typename T>
 struct OpArgs
 {
-  const double *__restrict__ src;
+  const T *__restrict__ src;
   double *__restrict__ dst;
   const int64_t *__restrict__ cell_start;  // nullptr = lexicographic
-  const double *__restrict__ fac[3];       // operator_factors_1d per direction
+  const T *__restrict__ fac[3];            // operator_factors_1d per direction
   int nc[3];
   int64_t n_cells;
 };
@@ -79,14 +82,14 @@ struct OpCfg
 //   out += (mass along the other directions) X_d
 // The neighbour couplings are rank two, so a neighbour costs two dot products per pencil
 // instead of a full n x n contraction.
-template<int DIM, int NP>
-__global__ void __launch_bounds__(OpCfg<DIM, NP>::THREADS) sipg_kernel(OpArgs a)
+template<int DIM, int NP, typename T>
+__global__ void __launch_bounds__(OpCfg<DIM, NP>::THREADS) sipg_kernel(OpArgs<T> a)
 {
   using C = OpCfg<DIM, NP>;
   constexpr int ND = C::ND, CPB = C::CPB, NPENC = C::NPENC, FS = C::FS;
-  __shared__ double s_x[CPB * ND];
-  __shared__ double s_out[CPB * ND];
-  __shared__ double s_fac[CPB * DIM * FS];
+  __shared__ T s_x[CPB * ND];
+  __shared__ T s_out[CPB * ND];
+  __shared__ T s_fac[CPB * DIM * FS];
   __shared__ int64_t s_first[CPB][3][3];  // [cell][direction][left, self, right]
   const int tid = threadIdx.x, slot = tid / NPENC, p = tid % NPENC;
   for(int64_t c0 = (int64_t)blockIdx.x * CPB; c0 < a.n_cells; c0 += (int64_t)gridDim.x * CPB)
@@ -96,7 +99,7 @@ __global__ void __launch_bounds__(OpCfg<DIM, NP>::THREADS) sipg_kernel(OpArgs a)
     {
       const int s = i / (DIM * FS), d = (i / FS) % DIM, o = i % FS;
       const int64_t cell = c0 + s;
-      double v = 0.0;
+      T v = T(0);
       if(cell < a.n_cells)
       {
         const int cd = d == 0 ? (int)(cell % a.nc[0]) : d == 1 ? (int)((cell / a.nc[0]) % a.nc[1])
@@ -123,7 +126,7 @@ __global__ void __launch_bounds__(OpCfg<DIM, NP>::THREADS) sipg_kernel(OpArgs a)
       }
       s_first[s][d][o + 1] = f;
     }
-    for(int i = tid; i < CPB * ND; i += C::THREADS) s_out[i] = 0.0;
+    for(int i = tid; i < CPB * ND; i += C::THREADS) s_out[i] = T(0);
     __syncthreads();
     const bool active = slot < CPB && c0 + (slot < CPB ? slot : 0) < a.n_cells;
 #pragma unroll
@@ -133,17 +136,16 @@ __global__ void __launch_bounds__(OpCfg<DIM, NP>::THREADS) sipg_kernel(OpArgs a)
       {
         const int stride = d == 0 ? 1 : d == 1 ? NP : NP * NP;
         const int base = (p % stride) + (p / stride) * stride * NP;
-        const double *F = s_fac + (slot * DIM + d) * FS;
-        const double *Cm = F + NP * NP, *aL = F + 2 * NP * NP, *bL = aL + 2 * NP, *aR = bL + 2 * NP,
-                     *bR = aR + 2 * NP;
-        double u[NP], x[NP];
-        const double *uc = a.src + s_first[slot][d][1] + base;
+        const T *F = s_fac + (slot * DIM + d) * FS;
+        const T *Cm = F + NP * NP, *aL = F + 2 * NP * NP, *bL = aL + 2 * NP, *aR = bL + 2 * NP, *bR = aR + 2 * NP;
+        T u[NP], x[NP];
+        const T *uc = a.src + s_first[slot][d][1] + base;
 #pragma unroll
         for(int m = 0; m < NP; ++m) u[m] = uc[m * stride];
 #pragma unroll
         for(int i = 0; i < NP; ++i)
         {
-          double acc = 0.0;
+          T acc = T(0);
 #pragma unroll
           for(int m = 0; m < NP; ++m) acc = fma(Cm[i * NP + m], u[m], acc);
           x[i] = acc;
@@ -153,13 +155,13 @@ __global__ void __launch_bounds__(OpCfg<DIM, NP>::THREADS) sipg_kernel(OpArgs a)
         {
           const int64_t f = s_first[slot][d][side == 0 ? 0 : 2];
           if(f < 0) continue;
-          const double *an = side == 0 ? aL : aR, *bn = side == 0 ? bL : bR;
-          const double *un = a.src + f + base;
-          double t0 = 0.0, t1 = 0.0;
+          const T *an = side == 0 ? aL : aR, *bn = side == 0 ? bL : bR;
+          const T *un = a.src + f + base;
+          T t0 = T(0), t1 = T(0);
 #pragma unroll
           for(int m = 0; m < NP; ++m)
           {
-            const double v = un[m * stride];
+            const T v = un[m * stride];
             t0 = fma(bn[m], v, t0);
             t1 = fma(bn[NP + m], v, t1);
           }
@@ -182,14 +184,14 @@ __global__ void __launch_bounds__(OpCfg<DIM, NP>::THREADS) sipg_kernel(OpArgs a)
         {
           const int stride = e == 0 ? 1 : e == 1 ? NP : NP * NP;
           const int base = (p % stride) + (p / stride) * stride * NP;
-          const double *M = s_fac + (slot * DIM + e) * FS;
-          double r[NP];
+          const T *M = s_fac + (slot * DIM + e) * FS;
+          T r[NP];
 #pragma unroll
           for(int m = 0; m < NP; ++m) r[m] = s_x[slot * ND + base + m * stride];
 #pragma unroll
           for(int i = 0; i < NP; ++i)
           {
-            double acc = 0.0;
+            T acc = T(0);
 #pragma unroll
             for(int m = 0; m < NP; ++m) acc = fma(M[i * NP + m], r[m], acc);
             if(last)
@@ -205,20 +207,32 @@ __global__ void __launch_bounds__(OpCfg<DIM, NP>::THREADS) sipg_kernel(OpArgs a)
     {
       const int s = i / ND;
       const int64_t cell = c0 + s;
-      if(cell < a.n_cells) a.dst[s_first[s][0][1] + i % ND] = s_out[i];
+      if(cell < a.n_cells) a.dst[s_first[s][0][1] + i % ND] = double(s_out[i]);
     }
   }
 }
 
-template<int DIM, int NP>
-void launch_sipg(const OpArgs &a, cudaStream_t s)
+template<int DIM, int NP, typename T>
+void launch_sipg_t(const OpArgs<T> &a, cudaStream_t s)
 {
   using C = OpCfg<DIM, NP>;
   const int64_t blocks = (a.n_cells + C::CPB - 1) / C::CPB;
   const int64_t cap = (int64_t)num_sms() * 16;
   const int grid = (int)(blocks < cap ? blocks : cap);
-  sipg_kernel<DIM, NP><<<grid, C::THREADS, 0, s>>>(a);
+  sipg_kernel<DIM, NP, T><<<grid, C::THREADS, 0, s>>>(a);
   TPSS_CUDA(cudaGetLastError());
+}
+
+template<int DIM, int NP>
+void launch_sipg(const OpArgs<double> &a, cudaStream_t s)
+{
+  launch_sipg_t<DIM, NP, double>(a, s);
+}
+
+template<int DIM, int NP>
+void launch_sipg32(const OpArgs<float> &a, cudaStream_t s)
+{
+  launch_sipg_t<DIM, NP, float>(a, s);
 }
 
 // ---- transfer: one coarse cell per slot
@@ -231,27 +245,29 @@ struct TrArgs
   int64_t n_coarse;
 };
 
-template<int DIM, int NP, bool RESTRICT>
+// T: arithmetic and shared-memory type (float for the transfers of a single-precision V-cycle:
+// FP64 vectors, each value converted once on the way in and out)
+template<int DIM, int NP, bool RESTRICT, typename T>
 __global__ void __launch_bounds__(OpCfg<DIM, NP>::THREADS) transfer_kernel(TrArgs a)
 {
   using C = OpCfg<DIM, NP>;
   constexpr int ND = C::ND, CPB = C::CPB, NPENC = C::NPENC, NCH = 1 << DIM;
-  __shared__ double s_buf[CPB * ND];
-  __shared__ double s_acc[CPB * ND];
-  __shared__ double s_E[2 * NP * NP];
+  __shared__ T s_buf[CPB * ND];
+  __shared__ T s_acc[CPB * ND];
+  __shared__ T s_E[2 * NP * NP];
   const int tid = threadIdx.x, slot = tid / NPENC, p = tid % NPENC;
-  for(int i = tid; i < 2 * NP * NP; i += C::THREADS) s_E[i] = a.E[i];
+  for(int i = tid; i < 2 * NP * NP; i += C::THREADS) s_E[i] = T(a.E[i]);
   const int nf0 = 2 * a.ncc[0], nf1 = DIM > 1 ? 2 * a.ncc[1] : 1;
   for(int64_t c0 = (int64_t)blockIdx.x * CPB; c0 < a.n_coarse; c0 += (int64_t)gridDim.x * CPB)
   {
-    for(int i = tid; i < CPB * ND; i += C::THREADS) s_acc[i] = 0.0;
+    for(int i = tid; i < CPB * ND; i += C::THREADS) s_acc[i] = T(0);
     for(int ch = 0; ch < NCH; ++ch)
     {
       __syncthreads();
       for(int i = tid; i < CPB * ND; i += C::THREADS)
       {
         const int64_t cell = c0 + i / ND;
-        double v = 0.0;
+        T v = T(0);
         if(cell < a.n_coarse)
         {
           if(RESTRICT)
@@ -261,10 +277,10 @@ __global__ void __launch_bounds__(OpCfg<DIM, NP>::THREADS) transfer_kernel(TrArg
             const int f[3] = {2 * c[0] + (ch & 1), 2 * c[1] + ((ch >> 1) & 1),
                               DIM == 3 ? 2 * c[2] + ((ch >> 2) & 1) : 0};
             const int64_t fc = f[0] + (int64_t)nf0 * (f[1] + (int64_t)nf1 * f[2]);
-            v = a.fine[fc * ND + i % ND];
+            v = T(a.fine[fc * ND + i % ND]);
           }
           else
-            v = a.coarse[cell * ND + i % ND];
+            v = T(a.coarse[cell * ND + i % ND]);
         }
         s_buf[i] = v;
       }
@@ -289,7 +305,7 @@ __global__ void __launch_bounds__(OpCfg<DIM, NP>::THREADS) transfer_kernel(TrArg
           const int f[3] = {2 * c[0] + (ch & 1), 2 * c[1] + ((ch >> 1) & 1),
                             DIM == 3 ? 2 * c[2] + ((ch >> 2) & 1) : 0};
           const int64_t fc = f[0] + (int64_t)nf0 * (f[1] + (int64_t)nf1 * f[2]);
-          a.fine[fc * ND + i % ND] += s_buf[i];
+          a.fine[fc * ND + i % ND] += double(s_buf[i]);
         }
       }
     }
@@ -298,23 +314,30 @@ __global__ void __launch_bounds__(OpCfg<DIM, NP>::THREADS) transfer_kernel(TrArg
       for(int i = tid; i < CPB * ND; i += C::THREADS)
       {
         const int64_t cell = c0 + i / ND;
-        if(cell < a.n_coarse) a.coarse[cell * ND + i % ND] += s_acc[i];
+        if(cell < a.n_coarse) a.coarse[cell * ND + i % ND] += double(s_acc[i]);
       }
     __syncthreads();
   }
 }
 
 template<int DIM, int NP>
-void launch_transfer(const TrArgs &a, bool restrict_mode, cudaStream_t s)
+void launch_transfer(const TrArgs &a, bool restrict_mode, bool single, cudaStream_t s)
 {
   using C = OpCfg<DIM, NP>;
   const int64_t blocks = (a.n_coarse + C::CPB - 1) / C::CPB;
   const int64_t cap = (int64_t)num_sms() * 16;
   const int grid = (int)(blocks < cap ? blocks : cap);
-  if(restrict_mode)
-    transfer_kernel<DIM, NP, true><<<grid, C::THREADS, 0, s>>>(a);
+  if(single)
+  {
+    if(restrict_mode)
+      transfer_kernel<DIM, NP, true, float><<<grid, C::THREADS, 0, s>>>(a);
+    else
+      transfer_kernel<DIM, NP, false, float><<<grid, C::THREADS, 0, s>>>(a);
+  }
+  else if(restrict_mode)
+    transfer_kernel<DIM, NP, true, double><<<grid, C::THREADS, 0, s>>>(a);
   else
-    transfer_kernel<DIM, NP, false><<<grid, C::THREADS, 0, s>>>(a);
+    transfer_kernel<DIM, NP, false, double><<<grid, C::THREADS, 0, s>>>(a);
   TPSS_CUDA(cudaGetLastError());
 }
 
@@ -353,6 +376,12 @@ __global__ void sub_kernel(int64_t n, const double *__restrict__ a, double *__re
 {
   for(int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     y[i] = a[i] - y[i];
+}
+
+__global__ void d2f_kernel(int64_t n, const double *__restrict__ x, float *__restrict__ y)
+{
+  for(int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    y[i] = float(x[i]);
 }
 
 constexpr int kDotBlocks = 1024, kDotThreads = 256;
@@ -405,7 +434,7 @@ void operator_apply(tpss_operator *op, double *dst, const double *src, cudaStrea
     mapped_apply(*op, dst, src, s);
     return;
   }
-  OpArgs a;
+  OpArgs<double> a;
   a.src = src;
   a.dst = dst;
   a.cell_start = L.lexicographic ? nullptr : L.d_cell_start.ptr;
@@ -418,8 +447,34 @@ void operator_apply(tpss_operator *op, double *dst, const double *src, cudaStrea
   TPSS_DISPATCH_NP(L.dim, L.np, launch_sipg, a, s);
 }
 
+void operator_apply_f32(tpss_operator *op, double *dst, const double *src, cudaStream_t s)
+{
+  const tpss_layout &L = *op->layout;
+  TPSS_REQUIRE(dst && src && dst != src, "operator: invalid vectors");
+  if(op->mapped)
+  {
+    mapped_apply(*op, dst, src, s);
+    return;
+  }
+  const int64_t n = L.n_dofs;
+  if(op->x32.n < (size_t)n) op->x32.resize(n);
+  d2f_kernel<<<vec_grid(n), 256, 0, s>>>(n, src, op->x32.ptr);
+  TPSS_CUDA(cudaGetLastError());
+  OpArgs<float> a;
+  a.src = op->x32.ptr;
+  a.dst = dst;
+  a.cell_start = L.lexicographic ? nullptr : L.d_cell_start.ptr;
+  for(int d = 0; d < 3; ++d)
+  {
+    a.fac[d] = op->d_fac32[d].ptr;
+    a.nc[d] = L.nc[d];
+  }
+  a.n_cells = L.n_cells;
+  TPSS_DISPATCH_NP(L.dim, L.np, launch_sipg32, a, s);
+}
+
 void transfer_apply(int dim, int k, const int *ncc, const double *E_dev, bool restrict_mode,
-                    double *coarse, double *fine, cudaStream_t s)
+                    double *coarse, double *fine, cudaStream_t s, bool single)
 {
   TrArgs a;
   a.coarse = coarse;
@@ -431,7 +486,7 @@ void transfer_apply(int dim, int k, const int *ncc, const double *E_dev, bool re
     a.ncc[d] = d < dim ? ncc[d] : 1;
     a.n_coarse *= a.ncc[d];
   }
-  TPSS_DISPATCH_NP(dim, k + 1, launch_transfer, a, restrict_mode, s);
+  TPSS_DISPATCH_NP(dim, k + 1, launch_transfer, a, restrict_mode, single, s);
 }
 
 void vec_axpby(int64_t n, double a, const double *x, double b, double *y, cudaStream_t s)
@@ -482,6 +537,8 @@ extern "C" int tpss_operator_create(const tpss_layout *layout, double ip_factor,
     {
       const std::vector<double> fac = operator_factors_1d(s, layout->nc[d], layout->h[d].data(), ip_factor);
       op->d_fac[d].upload(fac.data(), fac.size());
+      const std::vector<float> fac32(fac.begin(), fac.end());
+      op->d_fac32[d].upload(fac32.data(), fac32.size());
       op->nblk_cells[d] = layout->nc[d];
     }
     *out = op.release();
@@ -493,6 +550,14 @@ extern "C" int tpss_operator_vmult(tpss_operator *op, double *dst, const double 
   return guarded([&] {
     TPSS_REQUIRE(op, "null operator");
     operator_apply(op, dst, src, as_stream(stream));
+  });
+}
+
+extern "C" int tpss_operator_vmult_fp32(tpss_operator *op, double *dst, const double *src, void *stream)
+{
+  return guarded([&] {
+    TPSS_REQUIRE(op, "null operator");
+    operator_apply_f32(op, dst, src, as_stream(stream));
   });
 }
 
