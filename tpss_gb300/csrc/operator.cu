@@ -91,36 +91,39 @@ __global__ void __launch_bounds__(OpCfg<DIM, NP>::THREADS) sipg_kernel(OpArgs<T>
   __shared__ T s_out[CPB * ND];
   __shared__ T s_fac[CPB * DIM * FS];
   __shared__ int64_t s_first[CPB][3][3];  // [cell][direction][left, self, right]
+  __shared__ int s_cc[CPB][3];             // cell coordinates
   const int tid = threadIdx.x, slot = tid / NPENC, p = tid % NPENC;
   for(int64_t c0 = (int64_t)blockIdx.x * CPB; c0 < a.n_cells; c0 += (int64_t)gridDim.x * CPB)
   {
     __syncthreads();
+    // cell coordinates of the block's cells (one 64-bit division per cell, not per element)
+    if(tid < CPB)
+    {
+      const int64_t cell = c0 + tid;
+      s_cc[tid][0] = (int)(cell % a.nc[0]);
+      s_cc[tid][1] = (int)((cell / a.nc[0]) % a.nc[1]);
+      s_cc[tid][2] = (int)(cell / ((int64_t)a.nc[0] * a.nc[1]));
+    }
+    __syncthreads();
     for(int i = tid; i < CPB * DIM * FS; i += C::THREADS)
     {
       const int s = i / (DIM * FS), d = (i / FS) % DIM, o = i % FS;
-      const int64_t cell = c0 + s;
       T v = T(0);
-      if(cell < a.n_cells)
-      {
-        const int cd = d == 0 ? (int)(cell % a.nc[0]) : d == 1 ? (int)((cell / a.nc[0]) % a.nc[1])
-                                                               : (int)(cell / ((int64_t)a.nc[0] * a.nc[1]));
-        v = a.fac[d][(size_t)cd * FS + o];
-      }
+      if(c0 + s < a.n_cells) v = a.fac[d][(size_t)s_cc[s][d] * FS + o];
       s_fac[i] = v;
     }
     for(int i3 = tid; i3 < CPB * DIM * 3; i3 += C::THREADS)
     {
       const int s = i3 / (DIM * 3), d = (i3 / 3) % DIM, o = i3 % 3 - 1;
-      const int64_t cell = c0 + s;
       int64_t f = -1;
-      if(cell < a.n_cells)
+      if(c0 + s < a.n_cells)
       {
-        int c[3] = {(int)(cell % a.nc[0]), (int)((cell / a.nc[0]) % a.nc[1]),
-                    (int)(cell / ((int64_t)a.nc[0] * a.nc[1]))};
-        c[d] += o;
-        if(c[d] >= 0 && c[d] < a.nc[d])
+        const int cx = s_cc[s][0] + (d == 0 ? o : 0), cy = s_cc[s][1] + (d == 1 ? o : 0),
+                  cz = s_cc[s][2] + (d == 2 ? o : 0);
+        const int cdir = d == 0 ? cx : d == 1 ? cy : cz;
+        if(cdir >= 0 && cdir < a.nc[d])
         {
-          const int64_t nb = c[0] + (int64_t)a.nc[0] * (c[1] + (int64_t)a.nc[1] * c[2]);
+          const int64_t nb = cx + (int64_t)a.nc[0] * (cy + (int64_t)a.nc[1] * cz);
           f = a.cell_start ? a.cell_start[nb] : nb * ND;
         }
       }
@@ -257,9 +260,18 @@ __global__ void __launch_bounds__(OpCfg<DIM, NP>::THREADS) transfer_kernel(TrArg
   __shared__ T s_E[2 * NP * NP];
   const int tid = threadIdx.x, slot = tid / NPENC, p = tid % NPENC;
   for(int i = tid; i < 2 * NP * NP; i += C::THREADS) s_E[i] = T(a.E[i]);
+  __shared__ int s_cc[CPB][3];  // coarse cell coordinates
   const int nf0 = 2 * a.ncc[0], nf1 = DIM > 1 ? 2 * a.ncc[1] : 1;
   for(int64_t c0 = (int64_t)blockIdx.x * CPB; c0 < a.n_coarse; c0 += (int64_t)gridDim.x * CPB)
   {
+    __syncthreads();
+    if(tid < CPB)
+    {
+      const int64_t cell = c0 + tid;
+      s_cc[tid][0] = (int)(cell % a.ncc[0]);
+      s_cc[tid][1] = (int)((cell / a.ncc[0]) % a.ncc[1]);
+      s_cc[tid][2] = (int)(cell / ((int64_t)a.ncc[0] * a.ncc[1]));
+    }
     for(int i = tid; i < CPB * ND; i += C::THREADS) s_acc[i] = T(0);
     for(int ch = 0; ch < NCH; ++ch)
     {
@@ -272,8 +284,7 @@ __global__ void __launch_bounds__(OpCfg<DIM, NP>::THREADS) transfer_kernel(TrArg
         {
           if(RESTRICT)
           {
-            const int c[3] = {(int)(cell % a.ncc[0]), (int)((cell / a.ncc[0]) % a.ncc[1]),
-                              (int)(cell / ((int64_t)a.ncc[0] * a.ncc[1]))};
+            const int *c = s_cc[i / ND];
             const int f[3] = {2 * c[0] + (ch & 1), 2 * c[1] + ((ch >> 1) & 1),
                               DIM == 3 ? 2 * c[2] + ((ch >> 2) & 1) : 0};
             const int64_t fc = f[0] + (int64_t)nf0 * (f[1] + (int64_t)nf1 * f[2]);
@@ -300,8 +311,7 @@ __global__ void __launch_bounds__(OpCfg<DIM, NP>::THREADS) transfer_kernel(TrArg
           s_acc[i] += s_buf[i];
         else
         {
-          const int c[3] = {(int)(cell % a.ncc[0]), (int)((cell / a.ncc[0]) % a.ncc[1]),
-                            (int)(cell / ((int64_t)a.ncc[0] * a.ncc[1]))};
+          const int *c = s_cc[i / ND];
           const int f[3] = {2 * c[0] + (ch & 1), 2 * c[1] + ((ch >> 1) & 1),
                             DIM == 3 ? 2 * c[2] + ((ch >> 2) & 1) : 0};
           const int64_t fc = f[0] + (int64_t)nf0 * (f[1] + (int64_t)nf1 * f[2]);
