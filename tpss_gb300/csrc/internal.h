@@ -213,6 +213,7 @@ struct tpss_operator
   tpss::DeviceBuffer<double> d_fac[3];  // operator_factors_1d per direction
   tpss::DeviceBuffer<float> d_fac32[3];  // the same in FP32 (single-precision level operator)
   tpss::DeviceBuffer<float> x32;         // FP32 copy of the source (single-precision operator)
+  bool sparse_faces = false;             // face couplings with unit value vectors (operator.cu)
   int nblk_cells[3] = {0, 0, 0};
   std::unique_ptr<tpss::MappedOperator> mapped;  // set on distorted levels
 };

@@ -65,6 +65,7 @@ struct OpArgs
   const T *__restrict__ fac[3];            // operator_factors_1d per direction
   int nc[3];
   int64_t n_cells;
+  bool sparse_faces;  // face couplings have unit value vectors (xdir)
 };
 
 template<int DIM, int NP>
@@ -82,12 +83,106 @@ struct OpCfg
 //   out += (mass along the other directions) X_d
 // The neighbour couplings are rank two, so a neighbour costs two dot products per pencil
 // instead of a full n x n contraction.
-template<int DIM, int NP, typename T>
+// X_d of one pencil along d (the cell's own 1-D block and the rank-2 couplings to the two
+// neighbours along d) written to buf. SPARSE: the couplings' value vectors are unit vectors at the
+// shared face node (nodal basis with a node on each face, as FE_DGQ on Gauss-Lobatto points):
+// aL = aL[0] e_0, bL[n..2n) = c e_(n-1), aR = aR[n-1] e_(n-1), bR[n..2n) = c e_0, which saves
+// 2 n - 2 multiply-adds per neighbour and pencil.
+template<int DIM, int NP, int D, bool SPARSE, typename T>
+__device__ __forceinline__ void xdir(const OpArgs<T> &a, const T *fac, const int64_t *first, int p, T *buf)
+{
+  constexpr int FS = OpCfg<DIM, NP>::FS;
+  constexpr int stride = D == 0 ? 1 : D == 1 ? NP : NP * NP;
+  const int base = (p % stride) + (p / stride) * stride * NP;
+  const T *F = fac + D * FS;
+  const T *Cm = F + NP * NP, *aL = F + 2 * NP * NP, *bL = aL + 2 * NP, *aR = bL + 2 * NP, *bR = aR + 2 * NP;
+  T u[NP], x[NP];
+  const T *uc = a.src + first[1] + base;
+#pragma unroll
+  for(int m = 0; m < NP; ++m) u[m] = uc[m * stride];
+#pragma unroll
+  for(int i = 0; i < NP; ++i)
+  {
+    T acc = T(0);
+#pragma unroll
+    for(int m = 0; m < NP; ++m) acc = fma(Cm[i * NP + m], u[m], acc);
+    x[i] = acc;
+  }
+#pragma unroll
+  for(int side = 0; side < 2; ++side)
+  {
+    const int64_t f = first[side == 0 ? 0 : 2];
+    if(f < 0) continue;
+    const T *an = side == 0 ? aL : aR, *bn = side == 0 ? bL : bR;
+    const T *un = a.src + f + base;
+    if constexpr(SPARSE)
+    {
+      const int jn = side == 0 ? NP - 1 : 0;  // neighbour's node on the shared face
+      const int jc = side == 0 ? 0 : NP - 1;  // own node on the shared face
+      T v[NP];
+#pragma unroll
+      for(int m = 0; m < NP; ++m) v[m] = un[m * stride];
+      T t0 = T(0);
+#pragma unroll
+      for(int m = 0; m < NP; ++m) t0 = fma(bn[m], v[m], t0);
+      const T t1 = bn[NP + jn] * v[jn];
+#pragma unroll
+      for(int i = 0; i < NP; ++i) x[i] = fma(an[NP + i], t1, x[i]);
+      x[jc] = fma(an[jc], t0, x[jc]);
+    }
+    else
+    {
+      T t0 = T(0), t1 = T(0);
+#pragma unroll
+      for(int m = 0; m < NP; ++m)
+      {
+        const T v = un[m * stride];
+        t0 = fma(bn[m], v, t0);
+        t1 = fma(bn[NP + m], v, t1);
+      }
+#pragma unroll
+      for(int i = 0; i < NP; ++i) x[i] = fma(an[i], t0, fma(an[NP + i], t1, x[i]));
+    }
+  }
+#pragma unroll
+  for(int i = 0; i < NP; ++i) buf[base + i * stride] = x[i];
+}
+
+enum MassMode
+{
+  MASS_WRITE,
+  MASS_ADD
+};
+
+// out = (mass along E) in, one pencil along E (out may be in, pencil by pencil)
+template<int NP, int E, int MODE, typename T>
+__device__ __forceinline__ void mass_pass(const T *M, const T *in, T *out, int p)
+{
+  constexpr int stride = E == 0 ? 1 : E == 1 ? NP : NP * NP;
+  const int base = (p % stride) + (p / stride) * stride * NP;
+  T r[NP];
+#pragma unroll
+  for(int m = 0; m < NP; ++m) r[m] = in[base + m * stride];
+#pragma unroll
+  for(int i = 0; i < NP; ++i)
+  {
+    T acc = T(0);
+#pragma unroll
+    for(int m = 0; m < NP; ++m) acc = fma(M[i * NP + m], r[m], acc);
+    if(MODE == MASS_ADD)
+      out[base + i * stride] += acc;
+    else
+      out[base + i * stride] = acc;
+  }
+}
+
+template<int DIM, int NP, typename T, bool SPARSE>
 __global__ void __launch_bounds__(OpCfg<DIM, NP>::THREADS) sipg_kernel(OpArgs<T> a)
 {
   using C = OpCfg<DIM, NP>;
   constexpr int ND = C::ND, CPB = C::CPB, NPENC = C::NPENC, FS = C::FS;
   __shared__ T s_x[CPB * ND];
+  __shared__ T s_y[CPB * ND];
   __shared__ T s_out[CPB * ND];
   __shared__ T s_fac[CPB * DIM * FS];
   __shared__ int64_t s_first[CPB][3][3];  // [cell][direction][left, self, right]
@@ -129,82 +224,31 @@ __global__ void __launch_bounds__(OpCfg<DIM, NP>::THREADS) sipg_kernel(OpArgs<T>
       }
       s_first[s][d][o + 1] = f;
     }
-    for(int i = tid; i < CPB * ND; i += C::THREADS) s_out[i] = T(0);
     __syncthreads();
     const bool active = slot < CPB && c0 + (slot < CPB ? slot : 0) < a.n_cells;
-#pragma unroll
-    for(int d = 0; d < DIM; ++d)
+    T *bx = s_x + slot * ND, *by = s_y + slot * ND, *bo = s_out + slot * ND;
+    const T *fac = s_fac + slot * DIM * FS;
+    // sum_d (masses along e != d) X_d with the masses shared between terms:
+    //   2D: out = M_1 X_0 + M_0 X_1
+    //   3D: out = M_2 (M_1 X_0 + M_0 X_1) + M_1 (M_0 X_2)   (5 mass passes instead of 6)
+    if(active) xdir<DIM, NP, 0, SPARSE>(a, fac, s_first[slot][0], p, bx);
+    __syncthreads();
+    if(active) mass_pass<NP, 1, MASS_WRITE>(fac + 1 * FS, bx, DIM == 2 ? bo : by, p);
+    __syncthreads();
+    if(active) xdir<DIM, NP, 1, SPARSE>(a, fac, s_first[slot][1], p, bx);
+    __syncthreads();
+    if(active) mass_pass<NP, 0, MASS_ADD>(fac, bx, DIM == 2 ? bo : by, p);
+    __syncthreads();
+    if constexpr(DIM == 3)
     {
-      if(active)
-      {
-        const int stride = d == 0 ? 1 : d == 1 ? NP : NP * NP;
-        const int base = (p % stride) + (p / stride) * stride * NP;
-        const T *F = s_fac + (slot * DIM + d) * FS;
-        const T *Cm = F + NP * NP, *aL = F + 2 * NP * NP, *bL = aL + 2 * NP, *aR = bL + 2 * NP, *bR = aR + 2 * NP;
-        T u[NP], x[NP];
-        const T *uc = a.src + s_first[slot][d][1] + base;
-#pragma unroll
-        for(int m = 0; m < NP; ++m) u[m] = uc[m * stride];
-#pragma unroll
-        for(int i = 0; i < NP; ++i)
-        {
-          T acc = T(0);
-#pragma unroll
-          for(int m = 0; m < NP; ++m) acc = fma(Cm[i * NP + m], u[m], acc);
-          x[i] = acc;
-        }
-#pragma unroll
-        for(int side = 0; side < 2; ++side)
-        {
-          const int64_t f = s_first[slot][d][side == 0 ? 0 : 2];
-          if(f < 0) continue;
-          const T *an = side == 0 ? aL : aR, *bn = side == 0 ? bL : bR;
-          const T *un = a.src + f + base;
-          T t0 = T(0), t1 = T(0);
-#pragma unroll
-          for(int m = 0; m < NP; ++m)
-          {
-            const T v = un[m * stride];
-            t0 = fma(bn[m], v, t0);
-            t1 = fma(bn[NP + m], v, t1);
-          }
-#pragma unroll
-          for(int i = 0; i < NP; ++i) x[i] = fma(an[i], t0, fma(an[NP + i], t1, x[i]));
-        }
-#pragma unroll
-        for(int i = 0; i < NP; ++i) s_x[slot * ND + base + i * stride] = x[i];
-      }
+      if(active) mass_pass<NP, 2, MASS_WRITE>(fac + 2 * FS, by, bo, p);
       __syncthreads();
-      // masses along the other directions; the last one accumulates into out
-      int done = 0;
-#pragma unroll
-      for(int e = 0; e < DIM; ++e)
-      {
-        if(e == d) continue;
-        ++done;
-        const bool last = done == DIM - 1;
-        if(active)
-        {
-          const int stride = e == 0 ? 1 : e == 1 ? NP : NP * NP;
-          const int base = (p % stride) + (p / stride) * stride * NP;
-          const T *M = s_fac + (slot * DIM + e) * FS;
-          T r[NP];
-#pragma unroll
-          for(int m = 0; m < NP; ++m) r[m] = s_x[slot * ND + base + m * stride];
-#pragma unroll
-          for(int i = 0; i < NP; ++i)
-          {
-            T acc = T(0);
-#pragma unroll
-            for(int m = 0; m < NP; ++m) acc = fma(M[i * NP + m], r[m], acc);
-            if(last)
-              s_out[slot * ND + base + i * stride] += acc;
-            else
-              s_x[slot * ND + base + i * stride] = acc;
-          }
-        }
-        __syncthreads();
-      }
+      if(active) xdir<DIM, NP, 2, SPARSE>(a, fac, s_first[slot][2], p, bx);
+      __syncthreads();
+      if(active) mass_pass<NP, 0, MASS_WRITE>(fac, bx, by, p);
+      __syncthreads();
+      if(active) mass_pass<NP, 1, MASS_ADD>(fac + 1 * FS, by, bo, p);
+      __syncthreads();
     }
     for(int i = tid; i < CPB * ND; i += C::THREADS)
     {
@@ -222,7 +266,10 @@ void launch_sipg_t(const OpArgs<T> &a, cudaStream_t s)
   const int64_t blocks = (a.n_cells + C::CPB - 1) / C::CPB;
   const int64_t cap = (int64_t)num_sms() * 16;
   const int grid = (int)(blocks < cap ? blocks : cap);
-  sipg_kernel<DIM, NP, T><<<grid, C::THREADS, 0, s>>>(a);
+  if(a.sparse_faces)
+    sipg_kernel<DIM, NP, T, true><<<grid, C::THREADS, 0, s>>>(a);
+  else
+    sipg_kernel<DIM, NP, T, false><<<grid, C::THREADS, 0, s>>>(a);
   TPSS_CUDA(cudaGetLastError());
 }
 
@@ -445,6 +492,7 @@ void operator_apply(tpss_operator *op, double *dst, const double *src, cudaStrea
     return;
   }
   OpArgs<double> a;
+  a.sparse_faces = op->sparse_faces;
   a.src = src;
   a.dst = dst;
   a.cell_start = L.lexicographic ? nullptr : L.d_cell_start.ptr;
@@ -471,6 +519,7 @@ void operator_apply_f32(tpss_operator *op, double *dst, const double *src, cudaS
   d2f_kernel<<<vec_grid(n), 256, 0, s>>>(n, src, op->x32.ptr);
   TPSS_CUDA(cudaGetLastError());
   OpArgs<float> a;
+  a.sparse_faces = op->sparse_faces;
   a.src = op->x32.ptr;
   a.dst = dst;
   a.cell_start = L.lexicographic ? nullptr : L.d_cell_start.ptr;
@@ -543,9 +592,21 @@ extern "C" int tpss_operator_create(const tpss_layout *layout, double ip_factor,
       return;
     }
     const Shape1D s = make_shape_1d(layout->k);
+    op->sparse_faces = true;
     for(int d = 0; d < layout->dim; ++d)
     {
       const std::vector<double> fac = operator_factors_1d(s, layout->nc[d], layout->h[d].data(), ip_factor);
+      // unit value vectors at the shared face nodes (see xdir)
+      const int np = layout->np, q2 = np * np, fs = 2 * q2 + 8 * np;
+      for(int c = 0; c < layout->nc[d]; ++c)
+      {
+        const double *aL = &fac[(size_t)c * fs + 2 * q2], *bL = aL + 2 * np, *aR = bL + 2 * np, *bR = aR + 2 * np;
+        for(int i = 0; i < np; ++i)
+        {
+          if(i != 0 && (aL[i] != 0.0 || bR[np + i] != 0.0)) op->sparse_faces = false;
+          if(i != np - 1 && (aR[i] != 0.0 || bL[np + i] != 0.0)) op->sparse_faces = false;
+        }
+      }
       op->d_fac[d].upload(fac.data(), fac.size());
       const std::vector<float> fac32(fac.begin(), fac.end());
       op->d_fac32[d].upload(fac32.data(), fac32.size());
