@@ -144,6 +144,11 @@ public:
   {
     check(tpss_operator_vmult(handle_, dst, src, stream));
   }
+  // the same product in FP32 arithmetic (level operator of a single-precision V-cycle)
+  void vmult_fp32(double *dst, const double *src, void *stream = nullptr) const
+  {
+    check(tpss_operator_vmult_fp32(handle_, dst, src, stream));
+  }
   void Tvmult(double *dst, const double *src, void *stream = nullptr) const { vmult(dst, src, stream); }
   tpss_operator *handle() const { return handle_; }
 
