@@ -364,10 +364,13 @@ void extract_local_matrices(const tpss_layout &L, const tpss_operator &op, int64
                             double *out_dev);
 
 // operator and transfer (operator.cu)
-void operator_apply(tpss_operator *op, double *dst, const double *src, cudaStream_t s);
+// dst = A src, or with rhs the residual dst = rhs - A src
+void operator_apply(tpss_operator *op, double *dst, const double *src, cudaStream_t s,
+                    const double *rhs = nullptr);
 // the same operator in FP32 arithmetic (FP64 vectors; the source is converted once into a
 // scratch copy): for the residuals inside a single-precision V-cycle. Distorted levels keep FP64.
-void operator_apply_f32(tpss_operator *op, double *dst, const double *src, cudaStream_t s);
+void operator_apply_f32(tpss_operator *op, double *dst, const double *src, cudaStream_t s,
+                        const double *rhs = nullptr);
 // single: FP32 arithmetic on the FP64 vectors (the transfers of a single-precision V-cycle)
 void transfer_apply(int dim, int k, const int *ncc, const double *E_dev, bool restrict_mode,
                     double *coarse, double *fine, cudaStream_t s, bool single = false);

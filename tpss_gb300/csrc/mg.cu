@@ -228,14 +228,14 @@ struct tpss_mg
 
 namespace
 {
-// level operator of a smoothing residual inside the V-cycle (FP32 arithmetic for a
-// single-precision V-cycle)
+// smoothing residual inside the V-cycle, t = b - A x in one pass over the level (FP32
+// arithmetic for a single-precision V-cycle)
 void level_residual_op(tpss_mg *mg, MgLevel &c, cudaStream_t s)
 {
   if(mg->desc.vcycle_precision == TPSS_FP32)
-    operator_apply_f32(c.op, c.t.ptr, c.x.ptr, s);
+    operator_apply_f32(c.op, c.t.ptr, c.x.ptr, s, c.b.ptr);
   else
-    operator_apply(c.op, c.t.ptr, c.x.ptr, s);
+    operator_apply(c.op, c.t.ptr, c.x.ptr, s, c.b.ptr);
 }
 
 void down_sweep(tpss_mg *mg, cudaStream_t s)
@@ -246,7 +246,6 @@ void down_sweep(tpss_mg *mg, cudaStream_t s)
     MgLevel &c = mg->lv[l], &f = mg->lv[l - 1];
     precond_vmult(c.P, c.x.ptr, c.b.ptr, s);
     level_residual_op(mg, c, s);
-    vec_sub(c.L->n_dofs, c.b.ptr, c.t.ptr, s);
     TPSS_CUDA(cudaMemsetAsync(f.b.ptr, 0, sizeof(double) * f.L->n_dofs, s));
     transfer_apply(c.L->dim, c.L->k, f.L->nc, mg->E, true, f.b.ptr, c.t.ptr, s,
                    mg->desc.vcycle_precision == TPSS_FP32);
@@ -262,7 +261,6 @@ void up_sweep(tpss_mg *mg, cudaStream_t s)
     transfer_apply(c.L->dim, c.L->k, f.L->nc, mg->E, false, f.x.ptr, c.x.ptr, s,
                    mg->desc.vcycle_precision == TPSS_FP32);
     level_residual_op(mg, c, s);
-    vec_sub(c.L->n_dofs, c.b.ptr, c.t.ptr, s);
     precond_vmult(c.P, c.r.ptr, c.t.ptr, s);
     vec_axpby(c.L->n_dofs, 1.0, c.r.ptr, 1.0, c.x.ptr, s);
   }

@@ -65,7 +65,8 @@ struct OpArgs
   const T *__restrict__ fac[3];            // operator_factors_1d per direction
   int nc[3];
   int64_t n_cells;
-  bool sparse_faces;  // face couplings have unit value vectors (xdir)
+  bool sparse_faces;                   // face couplings have unit value vectors (xdir)
+  const double *__restrict__ rhs;      // non-null: dst = rhs - A src (the residual)
 };
 
 template<int DIM, int NP>
@@ -254,7 +255,11 @@ __global__ void __launch_bounds__(OpCfg<DIM, NP>::THREADS) sipg_kernel(OpArgs<T>
     {
       const int s = i / ND;
       const int64_t cell = c0 + s;
-      if(cell < a.n_cells) a.dst[s_first[s][0][1] + i % ND] = double(s_out[i]);
+      if(cell < a.n_cells)
+      {
+        const int64_t g = s_first[s][0][1] + i % ND;
+        a.dst[g] = a.rhs ? a.rhs[g] - double(s_out[i]) : double(s_out[i]);
+      }
     }
   }
 }
@@ -482,53 +487,60 @@ int vec_grid(int64_t n)
 }
 }  // namespace
 
-void operator_apply(tpss_operator *op, double *dst, const double *src, cudaStream_t s)
+namespace
 {
-  const tpss_layout &L = *op->layout;
-  TPSS_REQUIRE(dst && src && dst != src, "operator: invalid vectors");
-  if(op->mapped)
-  {
-    mapped_apply(*op, dst, src, s);
-    return;
-  }
-  OpArgs<double> a;
-  a.sparse_faces = op->sparse_faces;
+template<typename T>
+OpArgs<T> op_args(const tpss_operator &op, const T *src, double *dst, const double *rhs)
+{
+  const tpss_layout &L = *op.layout;
+  OpArgs<T> a;
+  a.sparse_faces = op.sparse_faces;
+  a.rhs = rhs;
   a.src = src;
   a.dst = dst;
   a.cell_start = L.lexicographic ? nullptr : L.d_cell_start.ptr;
   for(int d = 0; d < 3; ++d)
   {
-    a.fac[d] = op->d_fac[d].ptr;
+    if constexpr(sizeof(T) == 8)
+      a.fac[d] = op.d_fac[d].ptr;
+    else
+      a.fac[d] = op.d_fac32[d].ptr;
     a.nc[d] = L.nc[d];
   }
   a.n_cells = L.n_cells;
-  TPSS_DISPATCH_NP(L.dim, L.np, launch_sipg, a, s);
+  return a;
 }
+}  // namespace
 
-void operator_apply_f32(tpss_operator *op, double *dst, const double *src, cudaStream_t s)
+void operator_apply(tpss_operator *op, double *dst, const double *src, cudaStream_t s, const double *rhs)
 {
   const tpss_layout &L = *op->layout;
   TPSS_REQUIRE(dst && src && dst != src, "operator: invalid vectors");
   if(op->mapped)
   {
     mapped_apply(*op, dst, src, s);
+    if(rhs) vec_sub(L.n_dofs, rhs, dst, s);
+    return;
+  }
+  const OpArgs<double> a = op_args<double>(*op, src, dst, rhs);
+  TPSS_DISPATCH_NP(L.dim, L.np, launch_sipg, a, s);
+}
+
+void operator_apply_f32(tpss_operator *op, double *dst, const double *src, cudaStream_t s, const double *rhs)
+{
+  const tpss_layout &L = *op->layout;
+  TPSS_REQUIRE(dst && src && dst != src, "operator: invalid vectors");
+  if(op->mapped)
+  {
+    mapped_apply(*op, dst, src, s);
+    if(rhs) vec_sub(L.n_dofs, rhs, dst, s);
     return;
   }
   const int64_t n = L.n_dofs;
   if(op->x32.n < (size_t)n) op->x32.resize(n);
   d2f_kernel<<<vec_grid(n), 256, 0, s>>>(n, src, op->x32.ptr);
   TPSS_CUDA(cudaGetLastError());
-  OpArgs<float> a;
-  a.sparse_faces = op->sparse_faces;
-  a.src = op->x32.ptr;
-  a.dst = dst;
-  a.cell_start = L.lexicographic ? nullptr : L.d_cell_start.ptr;
-  for(int d = 0; d < 3; ++d)
-  {
-    a.fac[d] = op->d_fac32[d].ptr;
-    a.nc[d] = L.nc[d];
-  }
-  a.n_cells = L.n_cells;
+  const OpArgs<float> a = op_args<float>(*op, op->x32.ptr, dst, rhs);
   TPSS_DISPATCH_NP(L.dim, L.np, launch_sipg32, a, s);
 }
 
