@@ -439,9 +439,12 @@ def operator_time(tpss, sh, src, W):
     k, dim = sh.get_additional_data().degree, sh.get_additional_data().dim
     cells = W["N"] // (k + 1) ** dim
     npt = k + 1
-    # per direction and pencil: own 1-D block (np^2), two rank-2 neighbour couplings (8 np),
-    # dim-1 mass contractions (np^2 each)
-    fma_cell = dim * npt ** (dim - 1) * (dim * npt * npt + 8 * npt)
+    # multiply-adds per cell of the evaluation the kernel performs: per direction and pencil the
+    # own 1-D block (np^2) and two neighbour couplings with unit face-value vectors (2 np + 2
+    # each); mass contractions shared between the direction terms (2 in 2D, 5 in 3D, np^2 per
+    # pencil)
+    mass_passes = 2 if dim == 2 else 5
+    fma_cell = npt ** (dim - 1) * (dim * npt * npt + mass_passes * npt * npt + dim * 2 * (2 * npt + 2))
     return {"ms": ms, "dof_per_s": W["N"] / (ms * 1e-3),
             "fp64_tflops": 2 * fma_cell * cells / (ms * 1e-3) / 1e12,
             "algorithmic_fma_per_cell": fma_cell, "fp32_ms": ms32,
