@@ -300,20 +300,55 @@ struct TrArgs
   int64_t n_coarse;
 };
 
+// out (=, or += with ACC) (I x .. x B x .. x I) in along DIR for one pencil p, B row-major NP x NP
+// (TRANS: B^T)
+template<int NP, int DIR, bool TRANS, bool ACC, typename T>
+__device__ __forceinline__ void pencil_io(const T *in, T *out, const T *B, int p)
+{
+  constexpr int stride = cpow(NP, DIR);
+  const int base = (p % stride) + (p / stride) * stride * NP;
+  T r[NP];
+#pragma unroll
+  for(int m = 0; m < NP; ++m) r[m] = in[base + m * stride];
+#pragma unroll
+  for(int i = 0; i < NP; ++i)
+  {
+    T acc = T(0);
+#pragma unroll
+    for(int m = 0; m < NP; ++m) acc = fma(TRANS ? B[m * NP + i] : B[i * NP + m], r[m], acc);
+    if(ACC)
+      out[base + i * stride] += acc;
+    else
+      out[base + i * stride] = acc;
+  }
+}
+
+// Transfers between a coarse cell and its 2^dim children with the child embeddings E_b along
+// each direction (b = the child's bit in that direction), sum-factorized depth first so that the
+// contractions are shared between children: prolongation applies E_bx along x (2 passes), E_by
+// along y (4) and E_bz along z (8) instead of 3 passes per child (24); restriction runs the
+// transposed tree (z: 8, y: 4, x: 2), summing the children on the way up.
 // T: arithmetic and shared-memory type (float for the transfers of a single-precision V-cycle:
 // FP64 vectors, each value converted once on the way in and out)
 template<int DIM, int NP, bool RESTRICT, typename T>
 __global__ void __launch_bounds__(OpCfg<DIM, NP>::THREADS) transfer_kernel(TrArgs a)
 {
   using C = OpCfg<DIM, NP>;
-  constexpr int ND = C::ND, CPB = C::CPB, NPENC = C::NPENC, NCH = 1 << DIM;
-  __shared__ T s_buf[CPB * ND];
-  __shared__ T s_acc[CPB * ND];
+  constexpr int ND = C::ND, CPB = C::CPB, NPENC = C::NPENC;
+  __shared__ T s_u[CPB * ND];   // coarse cell
+  __shared__ T s_s[CPB * ND];   // after the x level of the tree
+  __shared__ T s_t[CPB * ND];   // after the y level (3D)
+  __shared__ T s_c[CPB * ND];   // one child
   __shared__ T s_E[2 * NP * NP];
+  __shared__ int s_cc[CPB][3];  // coarse cell coordinates
   const int tid = threadIdx.x, slot = tid / NPENC, p = tid % NPENC;
   for(int i = tid; i < 2 * NP * NP; i += C::THREADS) s_E[i] = T(a.E[i]);
-  __shared__ int s_cc[CPB][3];  // coarse cell coordinates
   const int nf0 = 2 * a.ncc[0], nf1 = DIM > 1 ? 2 * a.ncc[1] : 1;
+  // fine cell index of child (bx, by, bz) of block cell s
+  auto child = [&](int s, int bx, int by, int bz) {
+    const int *c = s_cc[s];
+    return (int64_t)(2 * c[0] + bx) + (int64_t)nf0 * ((2 * c[1] + by) + (int64_t)nf1 * (DIM == 3 ? 2 * c[2] + bz : 0));
+  };
   for(int64_t c0 = (int64_t)blockIdx.x * CPB; c0 < a.n_coarse; c0 += (int64_t)gridDim.x * CPB)
   {
     __syncthreads();
@@ -324,61 +359,109 @@ __global__ void __launch_bounds__(OpCfg<DIM, NP>::THREADS) transfer_kernel(TrArg
       s_cc[tid][1] = (int)((cell / a.ncc[0]) % a.ncc[1]);
       s_cc[tid][2] = (int)(cell / ((int64_t)a.ncc[0] * a.ncc[1]));
     }
-    for(int i = tid; i < CPB * ND; i += C::THREADS) s_acc[i] = T(0);
-    for(int ch = 0; ch < NCH; ++ch)
+    const bool active = slot < CPB && c0 + (slot < CPB ? slot : 0) < a.n_coarse;
+    T *u = s_u + slot * ND, *sx = s_s + slot * ND, *ty = s_t + slot * ND, *ch = s_c + slot * ND;
+    // a child's values in s_c <-> the fine vector
+    auto load_child = [&](int bx, int by, int bz) {
+      for(int i = tid; i < CPB * ND; i += C::THREADS)
+      {
+        const int s = i / ND;
+        s_c[i] = c0 + s < a.n_coarse ? T(a.fine[child(s, bx, by, bz) * ND + i % ND]) : T(0);
+      }
+    };
+    auto add_child = [&](int bx, int by, int bz) {
+      for(int i = tid; i < CPB * ND; i += C::THREADS)
+      {
+        const int s = i / ND;
+        if(c0 + s < a.n_coarse) a.fine[child(s, bx, by, bz) * ND + i % ND] += double(s_c[i]);
+      }
+    };
+    if constexpr(!RESTRICT)
     {
       __syncthreads();
       for(int i = tid; i < CPB * ND; i += C::THREADS)
+        s_u[i] = c0 + i / ND < a.n_coarse ? T(a.coarse[(c0 + i / ND) * ND + i % ND]) : T(0);
+      __syncthreads();
+      for(int bx = 0; bx < 2; ++bx)
       {
-        const int64_t cell = c0 + i / ND;
-        T v = T(0);
-        if(cell < a.n_coarse)
+        if(active) pencil_io<NP, 0, false, false>(u, sx, s_E + bx * NP * NP, p);
+        __syncthreads();
+        for(int by = 0; by < 2; ++by)
         {
-          if(RESTRICT)
+          if constexpr(DIM == 2)
           {
-            const int *c = s_cc[i / ND];
-            const int f[3] = {2 * c[0] + (ch & 1), 2 * c[1] + ((ch >> 1) & 1),
-                              DIM == 3 ? 2 * c[2] + ((ch >> 2) & 1) : 0};
-            const int64_t fc = f[0] + (int64_t)nf0 * (f[1] + (int64_t)nf1 * f[2]);
-            v = T(a.fine[fc * ND + i % ND]);
+            if(active) pencil_io<NP, 1, false, false>(sx, ch, s_E + by * NP * NP, p);
+            __syncthreads();
+            add_child(bx, by, 0);
+            __syncthreads();
           }
           else
-            v = T(a.coarse[cell * ND + i % ND]);
-        }
-        s_buf[i] = v;
-      }
-      __syncthreads();
-      const bool active = slot < CPB && c0 + (slot < CPB ? slot : 0) < a.n_coarse;
-#pragma unroll
-      for(int e = 0; e < DIM; ++e)
-      {
-        if(active) pencil_dir<DIM, NP, RESTRICT>(e, s_buf + slot * ND, s_E + ((ch >> e) & 1) * NP * NP, p);
-        __syncthreads();
-      }
-      for(int i = tid; i < CPB * ND; i += C::THREADS)
-      {
-        const int64_t cell = c0 + i / ND;
-        if(cell >= a.n_coarse) continue;
-        if(RESTRICT)
-          s_acc[i] += s_buf[i];
-        else
-        {
-          const int *c = s_cc[i / ND];
-          const int f[3] = {2 * c[0] + (ch & 1), 2 * c[1] + ((ch >> 1) & 1),
-                            DIM == 3 ? 2 * c[2] + ((ch >> 2) & 1) : 0};
-          const int64_t fc = f[0] + (int64_t)nf0 * (f[1] + (int64_t)nf1 * f[2]);
-          a.fine[fc * ND + i % ND] += double(s_buf[i]);
+          {
+            if(active) pencil_io<NP, 1, false, false>(sx, ty, s_E + by * NP * NP, p);
+            __syncthreads();
+            for(int bz = 0; bz < 2; ++bz)
+            {
+              if(active) pencil_io<NP, 2, false, false>(ty, ch, s_E + bz * NP * NP, p);
+              __syncthreads();
+              add_child(bx, by, bz);
+              __syncthreads();
+            }
+          }
         }
       }
     }
-    __syncthreads();
-    if(RESTRICT)
+    else
+    {
+      for(int bx = 0; bx < 2; ++bx)
+      {
+        for(int by = 0; by < 2; ++by)
+        {
+          if constexpr(DIM == 2)
+          {
+            __syncthreads();
+            load_child(bx, by, 0);
+            __syncthreads();
+            if(active)
+            {
+              if(by == 0) pencil_io<NP, 1, true, false>(ch, sx, s_E, p);
+              else pencil_io<NP, 1, true, true>(ch, sx, s_E + NP * NP, p);
+            }
+          }
+          else
+          {
+            for(int bz = 0; bz < 2; ++bz)
+            {
+              __syncthreads();
+              load_child(bx, by, bz);
+              __syncthreads();
+              if(active)
+              {
+                if(bz == 0) pencil_io<NP, 2, true, false>(ch, ty, s_E, p);
+                else pencil_io<NP, 2, true, true>(ch, ty, s_E + NP * NP, p);
+              }
+            }
+            __syncthreads();
+            if(active)
+            {
+              if(by == 0) pencil_io<NP, 1, true, false>(ty, sx, s_E, p);
+              else pencil_io<NP, 1, true, true>(ty, sx, s_E + NP * NP, p);
+            }
+          }
+        }
+        __syncthreads();
+        if(active)
+        {
+          if(bx == 0) pencil_io<NP, 0, true, false>(sx, u, s_E, p);
+          else pencil_io<NP, 0, true, true>(sx, u, s_E + NP * NP, p);
+        }
+      }
+      __syncthreads();
       for(int i = tid; i < CPB * ND; i += C::THREADS)
       {
         const int64_t cell = c0 + i / ND;
-        if(cell < a.n_coarse) a.coarse[cell * ND + i % ND] += double(s_acc[i]);
+        if(cell < a.n_coarse) a.coarse[cell * ND + i % ND] += double(s_u[i]);
       }
-    __syncthreads();
+    }
   }
 }
 
