@@ -518,15 +518,17 @@ def distorted_section(tpss, args):
     X = distorted_cube(dim, [n] * dim, 7, fac)
     N = n ** dim * (k + 1) ** dim
     f = torch.tensor(philox_src(N, args.seed), dtype=torch.float64, device="cuda")
-    runs = (("surrogate_fp64", tpss.LocalSolver.fd, tpss.Precision.fp64, None),
-            ("surrogate_fp32", tpss.LocalSolver.fd, tpss.Precision.fp32, None),
-            ("ksum_fp32", tpss.LocalSolver.ksum, tpss.Precision.fp32, None),
-            ("learned_fp32", tpss.LocalSolver.learned, tpss.Precision.fp32, m))
-    for name, ls, prec, model in runs:
+    fp64, fp32 = tpss.Precision.fp64, tpss.Precision.fp32
+    runs = (("surrogate_fp64", tpss.LocalSolver.fd, fp64, None, fp64),
+            ("surrogate_fp32", tpss.LocalSolver.fd, fp32, None, fp64),
+            ("ksum_fp32", tpss.LocalSolver.ksum, fp32, None, fp64),
+            ("learned_fp32", tpss.LocalSolver.learned, fp32, m, fp64),
+            ("learned_fp32_vcycle", tpss.LocalSolver.learned, fp32, m, fp32))
+    for name, ls, prec, model, vprec in runs:
         ts = time.perf_counter()
         mg = tpss.MultigridSolver(dim, k, 2, n, relaxation=0.15, precision=prec, coarse_solver=1,
                                   use_graph=True, vertex_coords=X, local_solver=ls, model=model,
-                                  auto_relaxation=True)
+                                  auto_relaxation=True, vcycle_precision=vprec)
         torch.cuda.synchronize()
         setup = time.perf_counter() - ts
         u = torch.zeros_like(f)
@@ -541,9 +543,11 @@ def distorted_section(tpss, args):
         except tpss.TPSSNotConverged:
             out[name] = {"setup_seconds": setup, "iterations": "not converged in 300"}
         del mg
-    a, b = out["learned_fp32"], out["surrogate_fp64"]
-    if "seconds" in a and "seconds" in b:
-        out["learned_fp32_over_surrogate_fp64_time"] = a["seconds"] / b["seconds"]
+    b = out["surrogate_fp64"]
+    for name in ("learned_fp32", "learned_fp32_vcycle"):
+        a = out[name]
+        if "seconds" in a and "seconds" in b:
+            out[f"{name}_over_surrogate_fp64_time"] = a["seconds"] / b["seconds"]
     return out
 
 

@@ -121,7 +121,7 @@ int tpss_operator_vmult(tpss_operator *op, double *dst, const double *src, void 
 /* The same product in FP32 arithmetic on FP64 vectors (src is converted once into a scratch
  * copy owned by the operator; dst is written in FP64): the level operator of a single-precision
  * V-cycle (no counterpart in the reference, which runs its multigrid in the vector precision).
- * Distorted (mapped) levels compute in FP64. */
+ * On distorted (mapped) levels the block-sparse matrix gets an FP32 copy on first use. */
 int tpss_operator_vmult_fp32(tpss_operator *op, double *dst, const double *src, void *stream);
 void tpss_operator_destroy(tpss_operator *op);
 

@@ -49,6 +49,23 @@ def test_mapped_operator_vs_quadrature(tpss, oracle, mapped, cuda, dim, k, nc, s
     assert rel_err(dst.cpu().numpy(), A @ x) <= 1e-12
 
 
+@pytest.mark.parametrize("dim,k,nc,seed,amp", [(2, 3, (4, 5), 2, 0.25), (3, 3, (3, 3, 2), 6, 0.25)])
+def test_mapped_operator_fp32(tpss, oracle, mapped, cuda, dim, k, nc, seed, amp):
+    """The single-precision product on a distorted level (FP32 copy of the block-sparse matrix)
+    against the quadrature matrix: FP32 rounding only (1e-5 relative), and the residual form
+    dst = rhs - A src through the single-precision V-cycle is covered by the MG tests."""
+    import torch
+    X = oracle.distorted_coords(dim, list(nc), seed, amp)
+    A = mapped.sipg_matrix_mapped(dim, k, list(nc), X, 1.0)
+    x = philox(seed + 10, A.shape[0])
+    sh, op = _op(tpss, dim, k, nc, X)
+    src = torch.tensor(x, dtype=torch.float64, device=cuda)
+    dst = torch.full_like(src, float("nan"))
+    op.vmult_fp32(dst, src)
+    err = rel_err(dst.cpu().numpy(), A @ x)
+    assert 0.0 < err <= 1e-5, err
+
+
 @pytest.mark.parametrize("dim,k,nc", [(2, 3, (6, 5)), (3, 2, (4, 3, 3))])
 def test_mapped_operator_on_cartesian_coords_equals_tensor_operator(tpss, mapped, cuda, dim, k, nc):
     import torch
@@ -115,3 +132,27 @@ def test_mg_scaled_relaxation_on_distorted_mesh(tpss, oracle, mapped, cuda, dim,
     it, hist = mg.solve(u, torch.tensor(f, dtype=torch.float64, device=cuda), max_iter=300)
     assert it == it_ref > 0
     assert rel_err(u.cpu().numpy(), u_ref) <= 1e-8
+
+
+def test_mg_fp32_vcycle_on_distorted_mesh(tpss, oracle, mapped, cuda):
+    """Single-precision V-cycle on a distorted hierarchy (FP32 block-sparse level operators and
+    transfers, FP32 smoothers): converges within two iterations of the FP64 V-cycle, and the
+    returned solution meets the tolerance with the FP64 operator."""
+    import torch
+    from tpss_gb300.mesh import distorted_cube
+    dim, k, ncf = 3, 2, 8
+    X = distorted_cube(dim, [ncf] * dim, 7, 0.15)
+    N = ncf ** dim * (k + 1) ** dim
+    f = torch.tensor(philox(8, N), dtype=torch.float64, device=cuda)
+    its = {}
+    for vp in (0, 1):
+        mg = tpss.MultigridSolver(dim, k, 2, ncf, relaxation=0.15, precision=1, coarse_solver=1,
+                                  vertex_coords=X, auto_relaxation=True, vcycle_precision=vp)
+        u = torch.zeros(N, dtype=torch.float64, device=cuda)
+        it, hist = mg.solve(u, f, rel_tol=1e-8, max_iter=300)
+        sh, op = _op(tpss, dim, k, (ncf,) * dim, X)
+        r = torch.empty_like(u)
+        op.vmult(r, u)
+        assert float(torch.linalg.norm(f - r) / torch.linalg.norm(f)) <= 2e-8, vp
+        its[vp] = it
+    assert its[1] <= its[0] + 2, its

@@ -201,6 +201,7 @@ struct MappedOperator
   int64_t n_cells = 0;
   DeviceBuffer<double> coords;  // vertex coordinates
   DeviceBuffer<double> vals;    // n_cells * nb blocks of nd x nd, entry (i, j) at j * nd + i
+  DeviceBuffer<float> vals32;   // FP32 copy (single-precision V-cycle), made on first use
   DeviceBuffer<int32_t> col;    // n_cells * nb column cell (lexicographic), -1 = none
 };
 }  // namespace tpss
@@ -333,7 +334,11 @@ bool launch_fd_f64(int dim, int k, int ncp, const FdLaunch &a, cudaStream_t s);
 // mapped (distorted) levels (mapped.cu)
 size_t mapped_smem_bytes(int dim, int np);
 void mapped_build(tpss_operator &op, const tpss_layout &L, double ip);
-void mapped_apply(const tpss_operator &op, double *dst, const double *src, cudaStream_t s);
+void mapped_apply(const tpss_operator &op, double *dst, const double *src, cudaStream_t s,
+                  const double *rhs = nullptr);
+// FP32 blocks and source, FP64 result (the level operator of a single-precision V-cycle)
+void mapped_apply_f32(tpss_operator &op, double *dst, const double *src, cudaStream_t s,
+                      const double *rhs = nullptr);
 std::vector<double> mapped_dense(const tpss_operator &op);
 // FD setup helpers (precond.cu, eigen.cu)
 void gen_eig_batched(int n, int n_problems, const std::vector<double> &Ms,
@@ -368,7 +373,8 @@ void extract_local_matrices(const tpss_layout &L, const tpss_operator &op, int64
 void operator_apply(tpss_operator *op, double *dst, const double *src, cudaStream_t s,
                     const double *rhs = nullptr);
 // the same operator in FP32 arithmetic (FP64 vectors; the source is converted once into a
-// scratch copy): for the residuals inside a single-precision V-cycle. Distorted levels keep FP64.
+// scratch copy): for the residuals inside a single-precision V-cycle (distorted levels: FP32
+// copy of the block-sparse matrix)
 void operator_apply_f32(tpss_operator *op, double *dst, const double *src, cudaStream_t s,
                         const double *rhs = nullptr);
 // single: FP32 arithmetic on the FP64 vectors (the transfers of a single-precision V-cycle)

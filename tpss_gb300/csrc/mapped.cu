@@ -356,18 +356,23 @@ __global__ void __launch_bounds__(256) assemble_kernel(const AsmArgs a, const Ma
     }
 }
 
+// T: value, source and accumulation type (float: the level operator of a single-precision
+// V-cycle, on an FP32 copy of the blocks and of the source); the result is stored in FP64
+template<typename T>
 struct MvArgs
 {
-  const double *vals;
+  const T *vals;
   const int32_t *col;
   const int64_t *cell_start;  // null: lexicographic blocks of nd
-  const double *src;
+  const T *src;
   double *dst;
+  const double *rhs;          // non-null: dst = rhs - A src
   int64_t n_rows;
   int nd, nb;
 };
 
-__global__ void __launch_bounds__(256) bsr_vmult_kernel(const MvArgs a)
+template<typename T>
+__global__ void __launch_bounds__(256) bsr_vmult_kernel(const MvArgs<T> a)
 {
   for(int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < a.n_rows;
       r += (int64_t)gridDim.x * blockDim.x)
@@ -375,17 +380,24 @@ __global__ void __launch_bounds__(256) bsr_vmult_kernel(const MvArgs a)
     const int64_t cell = r / a.nd;
     const int i = int(r % a.nd);
     const size_t bsz = (size_t)a.nd * a.nd;
-    double acc = 0.0;
+    T acc = T(0);
     for(int s = 0; s < a.nb; ++s)
     {
       const int32_t cc = a.col[cell * a.nb + s];
       if(cc < 0) continue;
-      const double *x = a.src + (a.cell_start ? a.cell_start[cc] : (int64_t)cc * a.nd);
-      const double *blk = a.vals + (cell * a.nb + s) * bsz + i;
+      const T *x = a.src + (a.cell_start ? a.cell_start[cc] : (int64_t)cc * a.nd);
+      const T *blk = a.vals + (cell * a.nb + s) * bsz + i;
       for(int j = 0; j < a.nd; ++j) acc += blk[(size_t)j * a.nd] * __ldg(x + j);
     }
-    a.dst[(a.cell_start ? a.cell_start[cell] : cell * a.nd) + i] = acc;
+    const int64_t g = (a.cell_start ? a.cell_start[cell] : cell * a.nd) + i;
+    a.dst[g] = a.rhs ? a.rhs[g] - double(acc) : double(acc);
   }
+}
+
+__global__ void d2f_copy_kernel(int64_t n, const double *__restrict__ x, float *__restrict__ y)
+{
+  for(int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    y[i] = float(x[i]);
 }
 
 MapTab make_tab(int k)
@@ -462,23 +474,57 @@ void mapped_build(tpss_operator &op, const tpss_layout &L, double ip)
   op.mapped = std::move(M);
 }
 
-void mapped_apply(const tpss_operator &op, double *dst, const double *src, cudaStream_t s)
+namespace
+{
+template<typename T>
+void launch_bsr(const tpss_operator &op, const T *vals, const T *src, double *dst, const double *rhs,
+                cudaStream_t s)
 {
   const tpss_layout &L = *op.layout;
   const MappedOperator &M = *op.mapped;
-  MvArgs a;
-  a.vals = M.vals.ptr;
+  MvArgs<T> a;
+  a.vals = vals;
   a.col = M.col.ptr;
   a.cell_start = L.lexicographic ? nullptr : L.d_cell_start.ptr;
   a.src = src;
   a.dst = dst;
+  a.rhs = rhs;
   a.n_rows = M.n_cells * M.nd;
   a.nd = M.nd;
   a.nb = M.nb;
   const int64_t blocks = (a.n_rows + 255) / 256;
   const int64_t cap = (int64_t)num_sms() * 16;
-  bsr_vmult_kernel<<<(unsigned)(blocks < cap ? blocks : cap), 256, 0, s>>>(a);
+  bsr_vmult_kernel<T><<<(unsigned)(blocks < cap ? blocks : cap), 256, 0, s>>>(a);
   TPSS_CUDA(cudaGetLastError());
+}
+
+int d2f_grid(int64_t n)
+{
+  const int64_t b = (n + 255) / 256, cap = (int64_t)num_sms() * 8;
+  return (int)(b < cap ? (b > 0 ? b : 1) : cap);
+}
+}  // namespace
+
+void mapped_apply(const tpss_operator &op, double *dst, const double *src, cudaStream_t s, const double *rhs)
+{
+  launch_bsr<double>(op, op.mapped->vals.ptr, src, dst, rhs, s);
+}
+
+void mapped_apply_f32(tpss_operator &op, double *dst, const double *src, cudaStream_t s, const double *rhs)
+{
+  MappedOperator &M = *op.mapped;
+  if(M.vals32.n != M.vals.n)
+  {
+    // FP32 copy of the blocks, made on first use (half the bytes the FP64 blocks stream)
+    M.vals32.resize(M.vals.n);
+    d2f_copy_kernel<<<d2f_grid((int64_t)M.vals.n), 256, 0, s>>>((int64_t)M.vals.n, M.vals.ptr, M.vals32.ptr);
+    TPSS_CUDA(cudaGetLastError());
+  }
+  const int64_t n = op.layout->n_dofs;
+  if(op.x32.n < (size_t)n) op.x32.resize(n);
+  d2f_copy_kernel<<<d2f_grid(n), 256, 0, s>>>(n, src, op.x32.ptr);
+  TPSS_CUDA(cudaGetLastError());
+  launch_bsr<float>(op, M.vals32.ptr, op.x32.ptr, dst, rhs, s);
 }
 
 std::vector<double> mapped_dense(const tpss_operator &op)

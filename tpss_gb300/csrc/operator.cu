@@ -601,8 +601,7 @@ void operator_apply(tpss_operator *op, double *dst, const double *src, cudaStrea
   TPSS_REQUIRE(dst && src && dst != src, "operator: invalid vectors");
   if(op->mapped)
   {
-    mapped_apply(*op, dst, src, s);
-    if(rhs) vec_sub(L.n_dofs, rhs, dst, s);
+    mapped_apply(*op, dst, src, s, rhs);
     return;
   }
   const OpArgs<double> a = op_args<double>(*op, src, dst, rhs);
@@ -615,8 +614,7 @@ void operator_apply_f32(tpss_operator *op, double *dst, const double *src, cudaS
   TPSS_REQUIRE(dst && src && dst != src, "operator: invalid vectors");
   if(op->mapped)
   {
-    mapped_apply(*op, dst, src, s);
-    if(rhs) vec_sub(L.n_dofs, rhs, dst, s);
+    mapped_apply_f32(*op, dst, src, s, rhs);
     return;
   }
   const int64_t n = L.n_dofs;
