@@ -577,6 +577,7 @@ def c0ip_section(tpss, args):
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1) / 20
         u = torch.zeros_like(f)
+        P.solve(u, f, rel_tol=0.5, max_iter=200)  # warm-up: captures the V-cycle graph
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         it, hist = P.solve(u, f, rel_tol=1e-8, max_iter=200)

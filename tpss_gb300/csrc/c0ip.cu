@@ -389,6 +389,20 @@ struct tpss_c0ip
   int bw = 0, m = 0;
   std::vector<C0ipLevel> lv;
   tpss::DeviceBuffer<double> coarse_inv, partial, scal, cr, cp, cAp, cz;
+  // the CG preconditioner step (z = V-cycle(r)) as one CUDA graph, captured on a private stream
+  // at the first solve and launched into the caller's stream order through two events
+  cudaStream_t gstream = nullptr;
+  cudaEvent_t ev_in = nullptr, ev_out = nullptr;
+  cudaGraphExec_t g_pre = nullptr;
+  tpss_c0ip() = default;
+  tpss_c0ip(const tpss_c0ip &) = delete;
+  ~tpss_c0ip()
+  {
+    if(g_pre) cudaGraphExecDestroy(g_pre);
+    if(ev_in) cudaEventDestroy(ev_in);
+    if(ev_out) cudaEventDestroy(ev_out);
+    if(gstream) cudaStreamDestroy(gstream);
+  }
 };
 
 namespace tpss
@@ -649,6 +663,32 @@ void restrict_to(const C0ipLevel &F, const C0ipLevel &Cl, double *coarse, const 
   TPSS_CUDA(cudaGetLastError());
 }
 
+// CG scalars on the device (no host round trip per iteration but the convergence check):
+// sc[0] rz, sc[1] pAp, sc[2] rr, sc[3] rz_new, sc[4] alpha, sc[5] -alpha, sc[6] beta, sc[7] 1
+__global__ void c0ip_cg_scalars(double *sc, int which)
+{
+  if(which == 0)
+  {
+    sc[4] = sc[0] / sc[1];
+    sc[5] = -sc[4];
+    sc[7] = 1.0;
+  }
+  else
+  {
+    sc[6] = sc[3] / sc[0];
+    sc[0] = sc[3];
+  }
+}
+
+// y = a x + b y with a, b in device memory (the arithmetic of vec_axpby)
+__global__ void c0ip_axpby_dev(int64_t n, const double *__restrict__ pa, const double *__restrict__ x,
+                               const double *__restrict__ pb, double *__restrict__ y)
+{
+  const double a = *pa, b = *pb;
+  for(int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    y[i] = a * x[i] + b * y[i];
+}
+
 double dot(tpss_c0ip &c, int64_t n, const double *x, const double *y, cudaStream_t s)
 {
   vec_dot(n, x, y, c.partial.ptr, c.scal.ptr, s);
@@ -752,7 +792,7 @@ extern "C" int tpss_c0ip_create(const tpss_c0ip_desc *d, tpss_c0ip **out)
     }
     const int64_t nt = (int64_t)c->lv.back().n * c->lv.back().n;
     c->partial.resize(dot_partials());
-    c->scal.resize(4);
+    c->scal.resize(16);
     for(auto *b : {&c->cr, &c->cp, &c->cAp, &c->cz}) b->resize(nt);
     *out = c.release();
   });
@@ -811,21 +851,60 @@ extern "C" int tpss_c0ip_cg_solve(tpss_c0ip *c, double *u, const double *f, doub
     bool converged = res <= tol;
     if(!converged)
     {
+      auto precondition_on = [&](cudaStream_t st) {
+        TPSS_CUDA(cudaMemcpyAsync(T.b.ptr, c->cr.ptr, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
+        vcycle(*c, top, st);
+        TPSS_CUDA(cudaMemcpyAsync(c->cz.ptr, T.x.ptr, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
+      };
       auto precondition = [&]() {
-        TPSS_CUDA(cudaMemcpyAsync(T.b.ptr, c->cr.ptr, sizeof(double) * N, cudaMemcpyDeviceToDevice, s));
-        vcycle(*c, top, s);
-        TPSS_CUDA(cudaMemcpyAsync(c->cz.ptr, T.x.ptr, sizeof(double) * N, cudaMemcpyDeviceToDevice, s));
+        if(!c->g_pre)
+        {
+          precondition_on(s);  // eager first application (lazy scratch allocations happen here)
+          TPSS_CUDA(cudaStreamSynchronize(s));
+          if(!c->gstream)
+          {
+            TPSS_CUDA(cudaStreamCreateWithFlags(&c->gstream, cudaStreamNonBlocking));
+            TPSS_CUDA(cudaEventCreateWithFlags(&c->ev_in, cudaEventDisableTiming));
+            TPSS_CUDA(cudaEventCreateWithFlags(&c->ev_out, cudaEventDisableTiming));
+          }
+          cudaGraph_t g = nullptr;
+          TPSS_CUDA(cudaStreamBeginCapture(c->gstream, cudaStreamCaptureModeThreadLocal));
+          try
+          {
+            precondition_on(c->gstream);
+          }
+          catch(...)
+          {
+            cudaStreamEndCapture(c->gstream, &g);
+            if(g) cudaGraphDestroy(g);
+            throw;
+          }
+          TPSS_CUDA(cudaStreamEndCapture(c->gstream, &g));
+          const cudaError_t e = cudaGraphInstantiate(&c->g_pre, g, 0);
+          cudaGraphDestroy(g);
+          TPSS_CUDA(e);
+          return;
+        }
+        TPSS_CUDA(cudaEventRecord(c->ev_in, s));
+        TPSS_CUDA(cudaStreamWaitEvent(c->gstream, c->ev_in, 0));
+        TPSS_CUDA(cudaGraphLaunch(c->g_pre, c->gstream));
+        TPSS_CUDA(cudaEventRecord(c->ev_out, c->gstream));
+        TPSS_CUDA(cudaStreamWaitEvent(s, c->ev_out, 0));
       };
       precondition();
       TPSS_CUDA(cudaMemcpyAsync(c->cp.ptr, c->cz.ptr, sizeof(double) * N, cudaMemcpyDeviceToDevice, s));
-      double rz = dot(*c, N, c->cr.ptr, c->cz.ptr, s);
+      double *sc = c->scal.ptr + 8;
+      vec_dot(N, c->cr.ptr, c->cz.ptr, c->partial.ptr, sc + 0, s);  // rz
+      const unsigned vg = (unsigned)std::min<int64_t>((N + 255) / 256, (int64_t)num_sms() * 8);
       for(it = 1; it <= max_iter; ++it)
       {
         op_apply(*c, T, c->cAp.ptr, c->cp.ptr, s);
-        const double alpha = rz / dot(*c, N, c->cp.ptr, c->cAp.ptr, s);
-        vec_axpby(N, alpha, c->cp.ptr, 1.0, u, s);
-        vec_axpby(N, -alpha, c->cAp.ptr, 1.0, c->cr.ptr, s);
-        res = std::sqrt(dot(*c, N, c->cr.ptr, c->cr.ptr, s));
+        vec_dot(N, c->cp.ptr, c->cAp.ptr, c->partial.ptr, sc + 1, s);  // pAp
+        c0ip_cg_scalars<<<1, 1, 0, s>>>(sc, 0);                          // alpha = rz / pAp
+        c0ip_axpby_dev<<<vg, 256, 0, s>>>(N, sc + 4, c->cp.ptr, sc + 7, u);
+        c0ip_axpby_dev<<<vg, 256, 0, s>>>(N, sc + 5, c->cAp.ptr, sc + 7, c->cr.ptr);
+        TPSS_CUDA(cudaGetLastError());
+        res = std::sqrt(dot(*c, N, c->cr.ptr, c->cr.ptr, s));  // the one host round trip
         if(res_history) res_history[it] = res;
         if(res <= tol)
         {
@@ -833,9 +912,10 @@ extern "C" int tpss_c0ip_cg_solve(tpss_c0ip *c, double *u, const double *f, doub
           break;
         }
         precondition();
-        const double rzn = dot(*c, N, c->cr.ptr, c->cz.ptr, s);
-        vec_axpby(N, 1.0, c->cz.ptr, rzn / rz, c->cp.ptr, s);  // p = z + beta p
-        rz = rzn;
+        vec_dot(N, c->cr.ptr, c->cz.ptr, c->partial.ptr, sc + 3, s);  // rz_new
+        c0ip_cg_scalars<<<1, 1, 0, s>>>(sc, 1);                         // beta, rz = rz_new
+        c0ip_axpby_dev<<<vg, 256, 0, s>>>(N, sc + 7, c->cz.ptr, sc + 6, c->cp.ptr);  // p = z + beta p
+        TPSS_CUDA(cudaGetLastError());
       }
     }
     if(iterations) *iterations = converged ? it : max_iter;
