@@ -29,6 +29,9 @@ bool TPSS_FD_FN(int k, int ncp, const FdLaunch &l, cudaStream_t s)
   a.n_patches = l.n_patches;
   a.omega = l.omega;
   a.entry_stride = l.entry_stride;
+  a.fd_eo = l.fd_eo;
+  a.sym = l.sym;
+  a.eo_stride = l.eo_stride;
   const int sms = num_sms();
 #define TPSS_FD_CASE(NCP, K1) \
   if(ncp == NCP && k + 1 == K1) return fd::launch<FD_T, FD_DIM, NCP, K1>(a, s, sms);

@@ -91,6 +91,71 @@ struct Entry
   static constexpr int size = (2 * N + 1) * NPAD;
 };
 
+// Even/odd form of a mirror-symmetric entry (n = 2h): [Se^T h x HPAD][So^T][Se][So][lambda: NPAD,
+// even then odd], Se = S_even / sqrt(2) (the host builds it in precond.cu)
+template<typename T, int N>
+struct EoEntry
+{
+  static constexpr int H = N / 2;
+  static constexpr int HPAD = Pad<T, (H > 0 ? H : 1)>::value;
+  static constexpr int SOT = H * HPAD, SE = 2 * H * HPAD, SO = 3 * H * HPAD, LAM = 4 * H * HPAD;
+  static constexpr int size = LAM + Pad<T, N>::value;
+};
+
+// h x h matrix rows (stride HPAD) times a vector: o[k] = sum_i B[k][i] v[i]
+template<typename T, int H, int HPAD>
+__device__ __forceinline__ T eo_row(const T *__restrict__ row, const T (&v)[H])
+{
+  T acc = T(0);
+#pragma unroll
+  for(int i = 0; i < H; ++i) acc = fma(row[i], v[i], acc);
+  return acc;
+}
+
+// forward transform of one pencil: o = [Se^T (r_i + r_{n-1-i}) ; So^T (r_i - r_{n-1-i})]
+template<typename T, int N>
+__device__ __forceinline__ void eo_fwd(const T *__restrict__ E, const T (&r)[N], T (&o)[N])
+{
+  using X = EoEntry<T, N>;
+  constexpr int H = X::H;
+  T a[H], b[H];
+#pragma unroll
+  for(int i = 0; i < H; ++i)
+  {
+    a[i] = r[i] + r[N - 1 - i];
+    b[i] = r[i] - r[N - 1 - i];
+  }
+#pragma unroll
+  for(int k = 0; k < H; ++k)
+  {
+    o[k] = eo_row<T, H, X::HPAD>(E + k * X::HPAD, a);
+    o[H + k] = eo_row<T, H, X::HPAD>(E + X::SOT + k * X::HPAD, b);
+  }
+}
+
+// backward transform: u_i = (Se t_e)_i + (So t_o)_i, u_{n-1-i} = (Se t_e)_i - (So t_o)_i
+template<typename T, int N>
+__device__ __forceinline__ void eo_bwd(const T *__restrict__ E, const T (&t)[N], T (&u)[N])
+{
+  using X = EoEntry<T, N>;
+  constexpr int H = X::H;
+  T te[H], to[H];
+#pragma unroll
+  for(int k = 0; k < H; ++k)
+  {
+    te[k] = t[k];
+    to[k] = t[H + k];
+  }
+#pragma unroll
+  for(int i = 0; i < H; ++i)
+  {
+    const T e = eo_row<T, H, X::HPAD>(E + X::SE + i * X::HPAD, te);
+    const T o = eo_row<T, H, X::HPAD>(E + X::SO + i * X::HPAD, to);
+    u[i] = e + o;
+    u[N - 1 - i] = e - o;
+  }
+}
+
 template<typename T, int DIM, int NCP, int K1>
 struct Cfg
 {
@@ -99,7 +164,8 @@ struct Cfg
   static constexpr int NPENCIL = NLOC / N;
   static constexpr int NCELL = cpow(NCP, DIM);
   static constexpr int CELLDOFS = cpow(K1, DIM);
-  static constexpr int ESIZE = Entry<T, N>::size;
+  // a slot holds the dense entry or, for a mirror-symmetric direction, its even/odd form
+  static constexpr int ESIZE = Entry<T, N>::size > EoEntry<T, N>::size ? Entry<T, N>::size : EoEntry<T, N>::size;
   // patches per CTA: enough pencils for >= 128 threads, bounded by shared memory
   static constexpr int PPC_WANT = NPENCIL >= 128 ? 1 : (128 + NPENCIL - 1) / NPENCIL;
   static constexpr int SLOT_BYTES = NLOC * sizeof(T) + DIM * ESIZE * sizeof(T) + NCELL * 12;
@@ -111,7 +177,8 @@ struct Cfg
   static constexpr size_t OFF_FD = 0;
   static constexpr size_t OFF_FIRST = al16(OFF_FD + (size_t)PPC * DIM * ESIZE * sizeof(T));
   static constexpr size_t OFF_W = al16(OFF_FIRST + (size_t)PPC * NCELL * 8);
-  static constexpr size_t OFF_DATA = al16(OFF_W + (size_t)PPC * NCELL * 4);
+  static constexpr size_t OFF_SYM = al16(OFF_W + (size_t)PPC * NCELL * 4);   // PPC * DIM ints
+  static constexpr size_t OFF_DATA = al16(OFF_SYM + (size_t)PPC * DIM * 4);
   static constexpr size_t smem_bytes() { return al16(OFF_DATA + (size_t)PPC * NLOC * sizeof(T)); }
 };
 
@@ -142,8 +209,9 @@ __device__ __forceinline__ int pencil_base(int p)
   return (p % stride) + (p / stride) * stride * N;
 }
 
+// TRANSPOSED: S^T (forward), else S (backward); sym: the entry is in even/odd form
 template<typename T, int DIM, int N, int DIR, bool TRANSPOSED>
-__device__ __forceinline__ void pass(T *__restrict__ data, const T *__restrict__ entry, int p,
+__device__ __forceinline__ void pass(T *__restrict__ data, const T *__restrict__ entry, bool sym, int p,
                                      T scale)
 {
   constexpr int NPAD = Entry<T, N>::NPAD;
@@ -152,18 +220,31 @@ __device__ __forceinline__ void pass(T *__restrict__ data, const T *__restrict__
   T r[N], o[N];
 #pragma unroll
   for(int m = 0; m < N; ++m) r[m] = data[base + m * stride];
-  rowmat<T, N, NPAD>(entry + (TRANSPOSED ? Entry<T, N>::ST : Entry<T, N>::S), r, o);
+  if constexpr(N % 2 == 0)
+  {
+    if(sym)
+    {
+      if constexpr(TRANSPOSED)
+        eo_fwd<T, N>(entry, r, o);
+      else
+        eo_bwd<T, N>(entry, r, o);
+    }
+    else
+      rowmat<T, N, NPAD>(entry + (TRANSPOSED ? Entry<T, N>::ST : Entry<T, N>::S), r, o);
+  }
+  else
+    rowmat<T, N, NPAD>(entry + (TRANSPOSED ? Entry<T, N>::ST : Entry<T, N>::S), r, o);
 #pragma unroll
   for(int i = 0; i < N; ++i) data[base + i * stride] = o[i] * scale;
 }
 
 // last direction: S^T along DIM-1, divide by sum of eigenvalues, S along DIM-1
-template<typename T, int DIM, int N>
+// (the eigenvalues of an even/odd entry are in the transformed order its forward pass produces)
+template<typename T, int DIM, int N, int ES>
 __device__ __forceinline__ void pass_last(T *__restrict__ data, const T *__restrict__ entries,
-                                          int p)
+                                          const int *sym, int p)
 {
   constexpr int NPAD = Entry<T, N>::NPAD;
-  constexpr int ES = Entry<T, N>::size;
   constexpr int DIR = DIM - 1;
   constexpr int stride = cpow(N, DIR);
   const int base = pencil_base<DIM, N, DIR>(p);
@@ -171,7 +252,16 @@ __device__ __forceinline__ void pass_last(T *__restrict__ data, const T *__restr
 #pragma unroll
   for(int m = 0; m < N; ++m) r[m] = data[base + m * stride];
   const T *eL = entries + DIR * ES;
-  rowmat<T, N, NPAD>(eL + Entry<T, N>::ST, r, o);
+  const bool symL = N % 2 == 0 && sym[DIR];
+  if constexpr(N % 2 == 0)
+  {
+    if(symL)
+      eo_fwd<T, N>(eL, r, o);
+    else
+      rowmat<T, N, NPAD>(eL + Entry<T, N>::ST, r, o);
+  }
+  else
+    rowmat<T, N, NPAD>(eL + Entry<T, N>::ST, r, o);
   // eigenvalue sum of the other directions (p enumerates i_0 [+ N i_1])
   T lsum = T(0);
   {
@@ -179,13 +269,23 @@ __device__ __forceinline__ void pass_last(T *__restrict__ data, const T *__restr
 #pragma unroll
     for(int d = 0; d < DIM - 1; ++d)
     {
-      lsum += entries[d * ES + Entry<T, N>::LAM + rem % N];
+      const int lam = N % 2 == 0 && sym[d] ? EoEntry<T, N>::LAM : Entry<T, N>::LAM;
+      lsum += entries[d * ES + lam + rem % N];
       rem /= N;
     }
   }
+  const T *lamL = eL + (symL ? EoEntry<T, N>::LAM : Entry<T, N>::LAM);
 #pragma unroll
-  for(int i = 0; i < N; ++i) o[i] = o[i] / (lsum + eL[Entry<T, N>::LAM + i]);
-  rowmat<T, N, NPAD>(eL + Entry<T, N>::S, o, r);
+  for(int i = 0; i < N; ++i) o[i] = o[i] / (lsum + lamL[i]);
+  if constexpr(N % 2 == 0)
+  {
+    if(symL)
+      eo_bwd<T, N>(eL, o, r);
+    else
+      rowmat<T, N, NPAD>(eL + Entry<T, N>::S, o, r);
+  }
+  else
+    rowmat<T, N, NPAD>(eL + Entry<T, N>::S, o, r);
 #pragma unroll
   for(int i = 0; i < N; ++i) data[base + i * stride] = r[i];
 }
@@ -201,6 +301,9 @@ struct KernelArgs
   int64_t n_patches;
   double omega;
   int entry_stride;
+  const void *__restrict__ fd_eo;     // even/odd forms (nullptr: none)
+  const int32_t *__restrict__ sym;    // entry is mirror-symmetric (nullptr: none)
+  int eo_stride;                      // elements per even/odd entry
 };
 
 template<typename T, int DIM, int NCP, int K1>
@@ -215,8 +318,10 @@ __global__ void __launch_bounds__(Cfg<T, DIM, NCP, K1>::THREADS)
   int64_t *s_first = reinterpret_cast<int64_t *>(smem_raw + C::OFF_FIRST);  // PPC * NCELL
   float *s_w = reinterpret_cast<float *>(smem_raw + C::OFF_W);          // PPC * NCELL
   T *s_data = reinterpret_cast<T *>(smem_raw + C::OFF_DATA);           // PPC * NLOC
+  int *s_sym = reinterpret_cast<int *>(smem_raw + C::OFF_SYM);          // PPC * DIM
 
   const T *fd = reinterpret_cast<const T *>(a.fd);
+  const T *fd_eo = reinterpret_cast<const T *>(a.fd_eo);
   const int tid = threadIdx.x;
   const int slot = tid / C::NPENCIL, pencil = tid % C::NPENCIL;
   const T omega = T(a.omega);
@@ -237,11 +342,16 @@ __global__ void __launch_bounds__(Cfg<T, DIM, NCP, K1>::THREADS)
     }
     for(int i = tid; i < PPC * DIM * ES; i += C::THREADS)
     {
-      const int sd = i / ES, s = sd / DIM;
+      const int sd = i / ES, s = sd / DIM, o = i % ES;
       if(s < nvalid)
       {
         const int e = a.patch_fd[p0 * DIM + sd];
-        s_fd[i] = fd[(size_t)e * a.entry_stride + (i % ES)];
+        const bool sy = N % 2 == 0 && a.sym && a.sym[e];
+        if(sy)
+          s_fd[i] = o < EoEntry<T, N>::size ? fd_eo[(size_t)e * a.eo_stride + o] : T(0);
+        else
+          s_fd[i] = o < Entry<T, N>::size ? fd[(size_t)e * a.entry_stride + o] : T(0);
+        if(o == 0) s_sym[sd] = sy;
       }
     }
     __syncthreads();
@@ -258,24 +368,25 @@ __global__ void __launch_bounds__(Cfg<T, DIM, NCP, K1>::THREADS)
     const bool active = slot < nvalid;
     T *my = s_data + slot * NLOC;
     const T *ent = s_fd + slot * DIM * ES;
+    const int *sy = s_sym + slot * DIM;
     // --- forward S^T along directions 0..DIM-2
-    if(active) pass<T, DIM, N, 0, true>(my, ent + 0 * ES, pencil, T(1));
+    if(active) pass<T, DIM, N, 0, true>(my, ent + 0 * ES, sy[0], pencil, T(1));
     __syncthreads();
     if constexpr(DIM == 3)
     {
-      if(active) pass<T, DIM, N, 1, true>(my, ent + 1 * ES, pencil, T(1));
+      if(active) pass<T, DIM, N, 1, true>(my, ent + 1 * ES, sy[1], pencil, T(1));
       __syncthreads();
     }
     // --- last direction fused with the eigenvalue division
-    if(active) pass_last<T, DIM, N>(my, ent, pencil);
+    if(active) pass_last<T, DIM, N, ES>(my, ent, sy, pencil);
     __syncthreads();
     // --- backward S along directions DIM-2..0, damping folded into direction 0
     if constexpr(DIM == 3)
     {
-      if(active) pass<T, DIM, N, 1, false>(my, ent + 1 * ES, pencil, T(1));
+      if(active) pass<T, DIM, N, 1, false>(my, ent + 1 * ES, sy[1], pencil, T(1));
       __syncthreads();
     }
-    if(active) pass<T, DIM, N, 0, false>(my, ent + 0 * ES, pencil, omega);
+    if(active) pass<T, DIM, N, 0, false>(my, ent + 0 * ES, sy[0], pencil, omega);
     __syncthreads();
     // --- scatter-add: whole cells, coalesced read-modify-write
     for(int i = tid; i < PPC * NCELL * CELLDOFS; i += C::THREADS)

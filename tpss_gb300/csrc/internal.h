@@ -235,9 +235,11 @@ struct FdTables
   // Even/odd split of mirror-symmetric entries (vertex patches with equal cells and equal
   // boundary flags): per entry [Se^T h x hpad][So^T][Se][So][lambda: even then odd, npad],
   // Se = S_even / sqrt(2); sym[e] = 1 when entry e has this form.
-  int hpad32 = 0;
+  int hpad32 = 0, hpad64 = 0;
   DeviceBuffer<float> fd32_eo;
+  DeviceBuffer<double> fd64_eo;  // the same in FP64 (per-color kernel, FP64 smoother)
   DeviceBuffer<int32_t> sym;
+  bool has_eo = false;           // some entry has the even/odd form
   // per-patch entries (entry p * dim + d) instead of the layout's shared keys
   DeviceBuffer<int32_t> own_fd;
   // exact local inverses (local solver TPSS_LOCAL_EXACT): P x nloc x nloc, transposed
@@ -327,6 +329,9 @@ struct FdLaunch
   int64_t n_patches;
   double omega;
   int entry_stride;            // elements per table entry
+  const void *fd_eo = nullptr;     // even/odd forms of the mirror-symmetric entries (or nullptr)
+  const int32_t *sym = nullptr;    // entry has the even/odd form (or nullptr)
+  int eo_stride = 0;               // elements per even/odd entry
 };
 bool launch_fd_f32(int dim, int k, int ncp, const FdLaunch &a, cudaStream_t s);
 bool launch_fd_f64(int dim, int k, int ncp, const FdLaunch &a, cudaStream_t s);

@@ -46,12 +46,15 @@ void build_even_odd(const tpss_layout &L, FdTables &T, const std::vector<double>
     }
   const int h = n / 2;
   T.hpad32 = pad_to(h, 4);
+  T.hpad64 = pad_to(h, 2);
   const int npad = T.npad32, hp = T.hpad32;
   const int es = 4 * h * hp + npad;
+  const int hp64 = T.hpad64, es64 = 4 * h * hp64 + T.npad64;
   std::vector<int> ids;
   for(int e = 0; e < T.n_entries; ++e)
     if(sym[e]) ids.push_back(e);
   std::vector<float> tab((size_t)std::max<size_t>(1, (size_t)T.n_entries) * es, 0.f);
+  std::vector<double> tab64((size_t)std::max<size_t>(1, (size_t)T.n_entries) * es64, 0.0);
   if(!ids.empty())
   {
     const double r2 = 1.0 / std::sqrt(2.0);
@@ -82,6 +85,7 @@ void build_even_odd(const tpss_layout &L, FdTables &T, const std::vector<double>
     for(size_t u = 0; u < ids.size(); ++u)
     {
       float *E = &tab[(size_t)ids[u] * es];
+      double *E64 = &tab64[(size_t)ids[u] * es64];
       for(int par = 0; par < 2; ++par)
       {
         const double *S = &Sh[(2 * u + par) * hh];
@@ -90,12 +94,20 @@ void build_even_odd(const tpss_layout &L, FdTables &T, const std::vector<double>
           {
             E[(par * h + k) * hp + i] = float(S[i * h + k] * r2);          // Se^T / So^T rows
             E[(2 * h + par * h + i) * hp + k] = float(S[i * h + k] * r2);  // Se / So rows
+            E64[(par * h + k) * hp64 + i] = S[i * h + k] * r2;
+            E64[(2 * h + par * h + i) * hp64 + k] = S[i * h + k] * r2;
           }
-        for(int k = 0; k < h; ++k) E[4 * h * hp + par * h + k] = float(lamh[(2 * u + par) * h + k]);
+        for(int k = 0; k < h; ++k)
+        {
+          E[4 * h * hp + par * h + k] = float(lamh[(2 * u + par) * h + k]);
+          E64[4 * h * hp64 + par * h + k] = lamh[(2 * u + par) * h + k];
+        }
       }
     }
   }
   T.fd32_eo.upload(tab.data(), tab.size());
+  T.fd64_eo.upload(tab64.data(), tab64.size());
+  T.has_eo = !ids.empty();
   T.sym.upload(sym.data(), sym.size());
 }
 
@@ -416,16 +428,25 @@ void apply_color(tpss_precond *p, int color, double *dst, const double *src, cud
   a.n_patches = e - b;
   a.omega = p->desc.relaxation;
   bool ok;
+  // even/odd forms of the mirror-symmetric entries (shared keyed tables only; per-patch tables
+  // of the fitted and learned solvers have none)
+  const bool eo = p->tables->has_eo && !p->tables->own_fd.n;
+  const int h = L.n / 2;
+  a.sym = eo ? p->tables->sym.ptr : nullptr;
   if(p->desc.precision == TPSS_FP32)
   {
     a.fd = p->tables->fd32.ptr;
     a.entry_stride = (2 * L.n + 1) * p->tables->npad32;
+    a.fd_eo = eo ? (const void *)p->tables->fd32_eo.ptr : nullptr;
+    a.eo_stride = 4 * h * p->tables->hpad32 + p->tables->npad32;
     ok = launch_fd_f32(L.dim, L.k, L.ncp, a, s);
   }
   else
   {
     a.fd = p->tables->fd64.ptr;
     a.entry_stride = (2 * L.n + 1) * p->tables->npad64;
+    a.fd_eo = eo ? (const void *)p->tables->fd64_eo.ptr : nullptr;
+    a.eo_stride = 4 * h * p->tables->hpad64 + p->tables->npad64;
     ok = launch_fd_f64(L.dim, L.k, L.ncp, a, s);
   }
   if(!ok)
