@@ -57,6 +57,9 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--kernel", choices=["auto", "color", "stream"], default="auto")
+    ap.add_argument("--level-kernels", action="store_true",
+                    help="time only the level operator (FP64, FP32) and the transfers on the "
+                         "--cells level (also the command the operator profile captures)")
     return ap.parse_args()
 
 
@@ -641,11 +644,47 @@ def batch_section(tpss, args):
             "setup_seconds": setup}
 
 
+def level_kernels(args):
+    """Level operator (FP64 and FP32 arithmetic) and DG prolongation / restriction from the
+    half-size level, on random vectors of the --cells level: milliseconds per application
+    (CUDA events, warmed up), one JSON line."""
+    import torch
+    import tpss_gb300 as tpss
+    dim, k, n = args.dim, args.degree, args.cells
+    nd = (k + 1) ** dim
+    sh = tpss.SubdomainHandler(tpss.SubdomainHandler.AdditionalData(dim=dim, degree=k, n_cells=(n,) * dim,
+                                                                     patch_variant=1))
+    op = tpss.LaplaceOperator(sh, 1.0)
+    g = torch.Generator(device="cuda").manual_seed(args.seed)
+    x = torch.rand(sh.n_dofs(), dtype=torch.float64, device="cuda", generator=g) * 2 - 1
+    y = torch.empty_like(x)
+    ncc = (n // 2,) * dim
+    coarse = torch.rand((n // 2) ** dim * nd, dtype=torch.float64, device="cuda", generator=g) * 2 - 1
+    fns = {"operator_fp64": lambda: op.vmult(y, x), "operator_fp32": lambda: op.vmult_fp32(y, x),
+           "prolongate_add": lambda: tpss.prolongate_add(dim, k, ncc, x, coarse),
+           "restrict_add": lambda: tpss.restrict_add(dim, k, ncc, coarse, x)}
+    out = {"workload": f"{dim}D SIPG DGQ{k} {n}^{dim} cells, {sh.n_dofs()} DoFs; transfers from {n // 2}^{dim}"}
+    for name, fn in fns.items():
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        out[name + "_ms"] = e0.elapsed_time(e1) / args.steps
+    print(json.dumps(out))
+
+
 def main():
     args = parse()
     if args.steps < 1 or args.warmup < 3:
         raise SystemExit("need --steps >= 1 and --warmup >= 3")
-    if args.impl == "reference":
+    if args.level_kernels:
+        level_kernels(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)
