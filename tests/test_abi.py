@@ -145,6 +145,9 @@ def test_new_entry_points_reject_invalid_input_before_gpu_work(tpss):
     assert lib.tpss_batch_create(None, 0, 1, C.byref(h)) == 1
     assert lib.tpss_precond_vmult_host(None, None, None, None) == 1
     assert lib.tpss_c0ip_cg_solve(None, None, None, 1e-8, 1e-14, 10, None, None, None) == 1
+    assert lib.tpss_operator_vmult_fp32(None, None, None, None) == 1
+    with pytest.raises(tpss.TPSSInvalidArgument, match="vcycle_precision"):
+        tpss.MultigridSolver(2, 2, 2, 8, vcycle_precision=5)
 
 
 def test_ctypes_descriptors_match_the_c_structs(tpss):
