@@ -24,36 +24,6 @@ namespace
 {
 __host__ __device__ constexpr int cpow(int b, int e) { return e == 0 ? 1 : b * cpow(b, e - 1); }
 
-// in-place pencil contraction along DIR of one (NP)^DIM block: x <- (I x..x B x..x I) x,
-// B row-major NP x NP (TRANS: B^T)
-template<int DIM, int NP, int DIR, bool TRANS, typename T>
-__device__ __forceinline__ void pencil(T *x, const T *B, int p)
-{
-  constexpr int stride = cpow(NP, DIR);
-  const int base = (p % stride) + (p / stride) * stride * NP;
-  T r[NP], o[NP];
-#pragma unroll
-  for(int m = 0; m < NP; ++m) r[m] = x[base + m * stride];
-#pragma unroll
-  for(int i = 0; i < NP; ++i)
-  {
-    T acc = T(0);
-#pragma unroll
-    for(int m = 0; m < NP; ++m) acc = fma(TRANS ? B[m * NP + i] : B[i * NP + m], r[m], acc);
-    o[i] = acc;
-  }
-#pragma unroll
-  for(int i = 0; i < NP; ++i) x[base + i * stride] = o[i];
-}
-
-template<int DIM, int NP, bool TRANS, typename T>
-__device__ __forceinline__ void pencil_dir(int dir, T *x, const T *B, int p)
-{
-  if(dir == 0) pencil<DIM, NP, 0, TRANS>(x, B, p);
-  else if(dir == 1) pencil<DIM, NP, 1, TRANS>(x, B, p);
-  else if constexpr(DIM == 3) pencil<DIM, NP, 2, TRANS>(x, B, p);
-}
-
 // T: arithmetic, shared-memory and source type (double; float for the single-precision level
 // operator, whose source is a pre-converted FP32 copy). The result is stored in FP64.
 template<typename T>
