@@ -60,6 +60,15 @@ def parse():
     ap.add_argument("--level-kernels", action="store_true",
                     help="time only the level operator (FP64, FP32) and the transfers on the "
                          "--cells level (also the command the operator profile captures)")
+    ap.add_argument("--no-dgq3-2d", action="store_true",
+                    help="skip the 2D SIPG DGQ3 64^2 section (both penalty modes)")
+    ap.add_argument("--profile-case", choices=["bsr", "c0ip", "mlp", "host"],
+                    help="run one small workload of a secondary kernel three times and exit (the "
+                         "commands the ncu profiles capture): bsr = mapped SIPG operator on a "
+                         "distorted 3D DGQ3 24^3 level; c0ip = C0IP FE_Q(3) 512^2 operator and "
+                         "FP32 Bilaplacian-FD smoother; mlp = one training epoch of the "
+                         "87 -> 3 x 64 -> 108 network on 119,164 samples; host = the FP32 "
+                         "smoother between pinned host buffers on 3D DGQ4 64^3")
     return ap.parse_args()
 
 
@@ -356,6 +365,8 @@ def run_ours(args):
     if not args.no_solve:
         out["operator"] = operator_time(tpss, sh, src, W)
         out["solve"] = solve_times(tpss, args)
+    if not args.no_dgq3_2d:
+        out["dgq3_2d"] = dgq3_2d_section(tpss, args)
     if not args.no_distorted:
         out["distorted"] = distorted_section(tpss, args)
     if not args.no_c0ip:
@@ -483,6 +494,67 @@ def solve_times(tpss, args):
                        f"fp32: FP32 smoothers; fp32_vcycle: FP32 smoothers and FP32 level operators "
                        f"in the V-cycle (outer CG and coarse solve FP64); fp64: all FP64")
     return res
+
+
+def dgq3_2d_section(tpss, args):
+    """2D SIPG DGQ3 on 64^2 cells (65,536 DoFs), additive vertex patches of 8 x 8 DoFs, FP64 as
+    stated (damping 0.5, penalty 2(k+1)^2/h) and with the reference's penalty: smoother
+    milliseconds and DoF/s, lambda_max(P A) of the finest level, CG + V-cycle (2 root cells,
+    6 levels, dense coarse solve, graphs) to 1e-8 at damping 0.5 and at the reference's 0.25."""
+    import torch
+    dim, k, nrep, n = 2, 3, 2, 64
+    N = n ** dim * (k + 1) ** dim
+    f = torch.tensor(philox_src(N, args.seed), dtype=torch.float64, device="cuda")
+    sh = tpss.SubdomainHandler(tpss.SubdomainHandler.AdditionalData(dim=dim, degree=k, n_cells=(n, n),
+                                                                     patch_variant=1))
+    out = {"workload": "2D SIPG DGQ3 64^2 cells, 65536 DoFs, additive vertex patches (8x8 DoFs, 4 colors), "
+                       "f ~ U[-1,1]; CG + V-cycle (1 pre/1 post smoothing step) to 1e-8, 2 root cells, "
+                       "dense coarse solve"}
+    for pen_name, mode in (("kp1sq", tpss.Penalty.kp1sq), ("reference", tpss.Penalty.reference)):
+        r = {}
+        for prec_name, prec in (("fp64", tpss.Precision.fp64), ("fp32", tpss.Precision.fp32)):
+            p = tpss.SchwarzPreconditioner()
+            p.initialize(sh, None, tpss.SchwarzPreconditioner.AdditionalData(
+                relaxation=0.5, precision=prec, penalty_mode=mode))
+            d = torch.empty_like(f)
+            for _ in range(10):
+                p.vmult(d, f)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(200):
+                p.vmult(d, f)
+            e1.record()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / 200
+            r[f"smoother_{prec_name}_ms"] = ms
+            r[f"smoother_{prec_name}_dof_per_s"] = N / (ms * 1e-3)
+        probe = tpss.MultigridSolver(dim, k, nrep, n, relaxation=0.5, coarse_solver=1,
+                                     auto_relaxation=True, penalty_mode=mode)
+        r["lambda_max_PA_finest"] = probe.relaxation(probe.n_levels - 1)[1]
+        del probe
+        for om in (0.5, 0.25):
+            for prec_name, prec in (("fp64", tpss.Precision.fp64), ("fp32", tpss.Precision.fp32)):
+                mg = tpss.MultigridSolver(dim, k, nrep, n, relaxation=om, precision=prec, coarse_solver=1,
+                                          use_graph=True, penalty_mode=mode)
+                u = torch.zeros_like(f)
+                mg.vmult(u, f)  # graph capture
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                try:
+                    it, hist = mg.solve(u, f, rel_tol=1e-8, max_iter=100)
+                    torch.cuda.synchronize()
+                    res = {"seconds": time.perf_counter() - t0, "iterations": it,
+                           "final_rel_residual": float(hist[-1] / hist[0])}
+                except tpss.TPSSNotConverged:
+                    torch.cuda.synchronize()
+                    res = {"converged": False, "max_iter": 100,
+                           "why": "damping x lambda_max(P A) > 2: the smoother amplifies and the V-cycle "
+                                  "is indefinite (the oracle does not converge either)"}
+                r[f"solve_damping{om}_{prec_name}"] = res
+                del mg
+        out[pen_name] = r
+    return out
 
 
 def distorted_section(tpss, args):
@@ -678,11 +750,56 @@ def level_kernels(args):
     print(json.dumps(out))
 
 
+def profile_case(args):
+    """One small workload of a secondary kernel, run three times (--profile-case)."""
+    import torch
+    import tpss_gb300 as tpss
+    from tpss_gb300.mesh import distorted_cube
+
+    name = args.profile_case
+    if name == "bsr":
+        n, k = 24, 3
+        X = distorted_cube(3, [n] * 3, 7, 0.15)
+        sh = tpss.SubdomainHandler(tpss.SubdomainHandler.AdditionalData(
+            dim=3, degree=k, n_cells=(n,) * 3, vertex_coords=X))
+        op = tpss.LaplaceOperator(sh)
+        x = torch.rand(sh.n_dofs(), dtype=torch.float64, device="cuda")
+        y = torch.empty_like(x)
+        for _ in range(3):
+            op.vmult(y, x)
+    elif name == "c0ip":
+        P = tpss.C0IPBiharmonic(3, 2, 512, local_solver=tpss.LocalSolver.fd, precision=tpss.Precision.fp32)
+        x = torch.rand(P.n_dofs(), dtype=torch.float64, device="cuda")
+        y = torch.empty_like(x)
+        for _ in range(3):
+            P.vmult(y, x)
+            P.smooth(y, x)
+    elif name == "mlp":
+        m = tpss.MLP(87, 108, 64, 3, seed=1)
+        x = torch.rand(119164, 87, device="cuda")
+        t = torch.rand(119164, 108, device="cuda")
+        m.train(x, t, epochs=1, batch=256)
+    elif name == "host":
+        sh = tpss.SubdomainHandler(tpss.SubdomainHandler.AdditionalData(dim=3, degree=4, n_cells=(64,) * 3))
+        p = tpss.SchwarzPreconditioner()
+        p.initialize(sh, None, tpss.SchwarzPreconditioner.AdditionalData(relaxation=0.15,
+                                                                         precision=tpss.Precision.fp32))
+        N = sh.n_dofs()
+        h_src = torch.rand(N, dtype=torch.float64).pin_memory()
+        h_dst = torch.empty(N, dtype=torch.float64).pin_memory()
+        for _ in range(3):
+            p.vmult_host(h_dst, h_src)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_case": name, "done": True}))
+
+
 def main():
     args = parse()
     if args.steps < 1 or args.warmup < 3:
         raise SystemExit("need --steps >= 1 and --warmup >= 3")
-    if args.level_kernels:
+    if args.profile_case:
+        profile_case(args)
+    elif args.level_kernels:
         level_kernels(args)
     elif args.impl == "reference":
         run_reference(args)

@@ -62,6 +62,17 @@ extern "C" {
 #define TPSS_FP64 0
 #define TPSS_FP32 1
 
+/* SIPG penalty (tpss_precond_desc / tpss_mg_desc .penalty_mode, tpss_operator_create_penalty).
+ * The operator and the local solvers of one level must use the same mode. */
+#define TPSS_PENALTY_REFERENCE 0 /* the reference's: sigma = ip*gamma*(1/h_l+1/h_r)/2 on interior
+                                    faces, 2*ip*gamma/h on Dirichlet faces, gamma = k(k+1)
+                                    (apps/common_integrator.h:30-37,
+                                    apps/laplace_integrator.h:134-148, 649-654, 691-693) */
+#define TPSS_PENALTY_2KP1SQ 1    /* sigma = ip*2(k+1)^2*(1/h_l+1/h_r)/2 on interior faces and
+                                    ip*2(k+1)^2/h on Dirichlet faces: "2(k+1)^2/h" on every face
+                                    of a uniform mesh (no counterpart in the reference, whose
+                                    formula cannot give this on both face kinds with one ip) */
+
 typedef struct tpss_layout tpss_layout;
 typedef struct tpss_operator tpss_operator;
 typedef struct tpss_precond tpss_precond;
@@ -116,6 +127,9 @@ void tpss_layout_destroy(tpss_layout *layout);
  * penalty 2*ip*gamma/h, gamma = k(k+1) (apps/common_integrator.h:30-37).
  */
 int tpss_operator_create(const tpss_layout *layout, double ip_factor, tpss_operator **out);
+/* The same with a TPSS_PENALTY_* mode (tpss_operator_create uses TPSS_PENALTY_REFERENCE). */
+int tpss_operator_create_penalty(const tpss_layout *layout, double ip_factor, int penalty_mode,
+                                 tpss_operator **out);
 /* MF::Operator::vmult (apps/laplace_integrator.h:578-598), FP64. */
 int tpss_operator_vmult(tpss_operator *op, double *dst, const double *src, void *stream);
 /* The same product in FP32 arithmetic on FP64 vectors (src is converted once into a scratch
@@ -144,6 +158,7 @@ typedef struct tpss_precond_desc
                                   (0..5, see tpss_precond_autotune); 0 by default */
   int local_solver;            /* TPSS_LOCAL_*: how the patch inverses are formed */
   const tpss_mlp *model;       /* trained network for TPSS_LOCAL_LEARNED, else NULL */
+  int penalty_mode;            /* TPSS_PENALTY_* of the local SIPG matrices (0: the reference) */
 } tpss_precond_desc;
 
 #define TPSS_KERNEL_AUTO 0
@@ -195,6 +210,12 @@ int tpss_precond_Tvmult(tpss_precond *p, double *dst, const double *src, void *s
  * array and it keeps the last call's contents; every entry a call reads is written by the same
  * call first, so nothing needs clearing, but calls that overlap on the GPU (for example on two
  * streams at once) race on it.
+ *
+ * Differences from tpss_precond_vmult: the preconditioner must have been created with
+ * check_finite = 0 (the check's flag would need a buffer) and a kernel_variant other than
+ * TPSS_KERNEL_COLOR, else the call returns TPSS_ERR_INVALID_ARGUMENT; dense (TPSS_LOCAL_EXACT)
+ * and per-patch (fitted, learned) local solvers are rejected the same way; the call is not
+ * recorded in the preconditioner's timers (tpss_precond_time_info).
  */
 int tpss_precond_vmult_static_scratch(tpss_precond *p, double *dst, const double *src, void *stream);
 
@@ -279,6 +300,7 @@ typedef struct tpss_mg_desc
                                   compute in FP32 (tpss_operator_vmult_fp32); the outer CG
                                   operator and the coarse solve stay FP64 (no counterpart in the
                                   reference, whose multigrid runs in the vector precision) */
+  int penalty_mode;            /* TPSS_PENALTY_* of every level's operator and local solvers */
 } tpss_mg_desc;
 
 int tpss_mg_create(const tpss_mg_desc *desc, tpss_mg **out);

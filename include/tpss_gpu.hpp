@@ -131,10 +131,11 @@ private:
 class LaplaceOperator
 {
 public:
-  LaplaceOperator(std::shared_ptr<const SubdomainHandler> sh, double ip_factor = 1.)
+  LaplaceOperator(std::shared_ptr<const SubdomainHandler> sh, double ip_factor = 1.,
+                  int penalty_mode = TPSS_PENALTY_REFERENCE)
     : sh_(std::move(sh))
   {
-    check(tpss_operator_create(sh_->handle(), ip_factor, &handle_));
+    check(tpss_operator_create_penalty(sh_->handle(), ip_factor, penalty_mode, &handle_));
   }
   LaplaceOperator(const LaplaceOperator &) = delete;
   ~LaplaceOperator() { tpss_operator_destroy(handle_); }
@@ -182,6 +183,7 @@ public:
     int stream_variant = 0;
     int local_solver = TPSS_LOCAL_FD;  // TPSS_LOCAL_FD / EXACT / KSUM / LEARNED
     const tpss_mlp *model = nullptr;   // trained network for TPSS_LOCAL_LEARNED
+    int penalty_mode = TPSS_PENALTY_REFERENCE;  // must match the level operator's
   };
 
   SchwarzPreconditioner() = default;
@@ -275,6 +277,7 @@ private:
     d.stream_variant = ad.stream_variant;
     d.local_solver = ad.local_solver;
     d.model = ad.model;
+    d.penalty_mode = ad.penalty_mode;
     return d;
   }
 

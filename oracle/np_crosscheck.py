@@ -52,8 +52,12 @@ def _cell_dofs(dim, k, nc, c):
     return np.arange(lex * nd, (lex + 1) * nd)
 
 
-def sipg_matrix(dim, k, nc, ip=1.0, h=None):
-    """Dense global SIPG matrix on [0,1]^dim with nc cells per direction (DoFs cell-wise)."""
+def sipg_matrix(dim, k, nc, ip=1.0, h=None, penalty="reference"):
+    """Dense global SIPG matrix on [0,1]^dim with nc cells per direction (DoFs cell-wise).
+
+    penalty "reference": sigma = ip k(k+1) (1/h_l + 1/h_r)/2 inside, 2 ip k(k+1)/h on the
+    boundary; "kp1sq": sigma = ip 2(k+1)^2 (1/h_l + 1/h_r)/2 inside, ip 2(k+1)^2/h on the
+    boundary (2(k+1)^2/h on every face of a uniform mesh)."""
     nc = list(nc)
     if h is None:
         h = [np.full(nc[d], 1.0 / nc[d]) for d in range(dim)]
@@ -64,6 +68,20 @@ def sipg_matrix(dim, k, nc, ip=1.0, h=None):
     V, D = lagrange(nodes, qx)  # [i, q]
     F, FD = lagrange(nodes, np.array([0.0, 1.0]))  # [i, face]
     gamma = 1.0 if k == 0 else k * (k + 1.0)
+    if penalty == "reference":
+        def sig_bd(hb):
+            return ip * 2.0 * gamma / hb
+
+        def sig_in(hl, hr):
+            return ip * gamma * (1.0 / hl + 1.0 / hr) / 2.0
+    elif penalty == "kp1sq":
+        def sig_bd(hb):
+            return ip * 2.0 * (k + 1.0) ** 2 / hb
+
+        def sig_in(hl, hr):
+            return ip * 2.0 * (k + 1.0) ** 2 * (1.0 / hl + 1.0 / hr) / 2.0
+    else:
+        raise ValueError(penalty)
     ncell = int(np.prod(nc))
     N = ncell * npt ** dim
     A = np.zeros((N, N))
@@ -116,11 +134,11 @@ def sipg_matrix(dim, k, nc, ip=1.0, h=None):
             if c[d] == 0:
                 v, dn, w = face_vals(hc, d, 0)
                 dn = -dn  # outward normal -x_d
-                sig = ip * 2.0 * gamma / hc[d]
+                sig = sig_bd(hc[d])
                 A[np.ix_(dofs, dofs)] += (sig * v * w) @ v.T - (v * w) @ dn.T - (dn * w) @ v.T
             if c[d] == nc[d] - 1:
                 v, dn, w = face_vals(hc, d, 1)
-                sig = ip * 2.0 * gamma / hc[d]
+                sig = sig_bd(hc[d])
                 A[np.ix_(dofs, dofs)] += (sig * v * w) @ v.T - (v * w) @ dn.T - (dn * w) @ v.T
             if c[d] + 1 < nc[d]:
                 cr = list(c)
@@ -129,7 +147,7 @@ def sipg_matrix(dim, k, nc, ip=1.0, h=None):
                 dofs_r = _cell_dofs(dim, k, nc + [1] * (3 - dim), cr + [0] * (3 - dim))
                 vl, dl, w = face_vals(hc, d, 1)
                 vr, dr, _ = face_vals(hr, d, 0)
-                sig = ip * gamma * (1.0 / hc[d] + 1.0 / hr[d]) / 2.0
+                sig = sig_in(hc[d], hr[d])
                 # jump [w] = w_l - w_r ; average {dn w} = (dl + dr)/2, normal +x_d
                 J = np.vstack([vl, -vr])
                 Av = 0.5 * np.vstack([dl, dr])

@@ -70,8 +70,33 @@ def lib():
             L.or_schwarz_destroy.argtypes = [C.c_void_p]
             L.or_num_threads.restype = C.c_int
             L.or_set_num_threads.argtypes = [C.c_int]
+            L.or_set_penalty_mode.argtypes = [C.c_int]
             _lib = L
     return _lib
+
+
+PENALTY_MODES = {"reference": 0, "kp1sq": 1}
+
+
+class _penalty:
+    """Holds the oracle's SIPG penalty mode for one call: "reference" (ip k(k+1)(1/h_l+1/h_r)/2
+    inside, 2 ip k(k+1)/h on the boundary, apps/common_integrator.h:30-37) or "kp1sq"
+    (ip 2(k+1)^2 (1/h_l+1/h_r)/2 inside, ip 2(k+1)^2/h on the boundary)."""
+
+    _mutex = threading.RLock()
+
+    def __init__(self, mode):
+        if mode not in PENALTY_MODES:
+            raise ValueError(f"unknown penalty mode {mode!r}")
+        self.mode = PENALTY_MODES[mode]
+
+    def __enter__(self):
+        self._mutex.acquire()
+        lib().or_set_penalty_mode(self.mode)
+
+    def __exit__(self, *exc):
+        lib().or_set_penalty_mode(0)
+        self._mutex.release()
 
 
 def _d(a):
@@ -104,13 +129,14 @@ def shape_data(k):
                 fval=fval.reshape(2, np1), fgrad=fgrad.reshape(2, np1))
 
 
-def patch_matrices_1d(k, h, bdry_lo, bdry_hi, ip=1.0):
+def patch_matrices_1d(k, h, bdry_lo, bdry_hi, ip=1.0, penalty="reference"):
     """1-D mass M and SIPG Laplace A of a DG patch of len(h) (1 or 2) cells."""
     h = _c64(h)
     n = len(h) * (k + 1)
     M, A = np.zeros((n, n)), np.zeros((n, n))
-    rc = lib().or_patch_matrices_1d(k, len(h), _d(h), int(bdry_lo), int(bdry_hi), float(ip),
-                                    _d(M), _d(A))
+    with _penalty(penalty):
+        rc = lib().or_patch_matrices_1d(k, len(h), _d(h), int(bdry_lo), int(bdry_hi), float(ip),
+                                        _d(M), _d(A))
     assert rc == 0
     return M, A
 
@@ -168,7 +194,8 @@ def _h_arrays(dim, nc, h):
 
 
 def schwarz_vmult(dim, k, nc, src, patch_variant=1, smoother_variant=0, omega=1.0, ip=1.0,
-                  h=None, cell_start=None, reverse=False, symmetrized=False, use_ras=False):
+                  h=None, cell_start=None, reverse=False, symmetrized=False, use_ras=False,
+                  penalty="reference"):
     nc3 = _nc3(dim, nc)
     hs = _h_arrays(dim, nc, h)
     src = _c64(src)
@@ -176,23 +203,27 @@ def schwarz_vmult(dim, k, nc, src, patch_variant=1, smoother_variant=0, omega=1.
     cs = None
     if cell_start is not None:
         cs = np.ascontiguousarray(cell_start, dtype=np.int64)
-    rc = lib().or_schwarz_vmult(dim, k, nc3.ctypes.data_as(_ip), _d(hs[0]), _d(hs[1]), _d(hs[2]),
-                                float(ip), cs.ctypes.data_as(_i64p) if cs is not None else None,
-                                patch_variant, smoother_variant, float(omega), int(reverse),
-                                int(symmetrized), int(use_ras), _d(src), _d(dst))
+    with _penalty(penalty):
+        rc = lib().or_schwarz_vmult(dim, k, nc3.ctypes.data_as(_ip), _d(hs[0]), _d(hs[1]),
+                                    _d(hs[2]), float(ip),
+                                    cs.ctypes.data_as(_i64p) if cs is not None else None,
+                                    patch_variant, smoother_variant, float(omega), int(reverse),
+                                    int(symmetrized), int(use_ras), _d(src), _d(dst))
     assert rc == 0
     return dst
 
 
-def sipg_vmult(dim, k, nc, src, ip=1.0, h=None, cell_start=None):
+def sipg_vmult(dim, k, nc, src, ip=1.0, h=None, cell_start=None, penalty="reference"):
     nc3 = _nc3(dim, nc)
     hs = _h_arrays(dim, nc, h)
     src = _c64(src)
     dst = np.zeros_like(src)
     cs = None if cell_start is None else np.ascontiguousarray(cell_start, dtype=np.int64)
-    assert lib().or_sipg_vmult(dim, k, nc3.ctypes.data_as(_ip), _d(hs[0]), _d(hs[1]), _d(hs[2]),
-                               float(ip), cs.ctypes.data_as(_i64p) if cs is not None else None,
-                               _d(src), _d(dst)) == 0
+    with _penalty(penalty):
+        rc = lib().or_sipg_vmult(dim, k, nc3.ctypes.data_as(_ip), _d(hs[0]), _d(hs[1]), _d(hs[2]),
+                                 float(ip), cs.ctypes.data_as(_i64p) if cs is not None else None,
+                                 _d(src), _d(dst))
+    assert rc == 0
     return dst
 
 
@@ -211,16 +242,17 @@ def restrict_add(dim, k, nc_coarse, coarse, fine):
 
 
 def mg_cg_solve(dim, k, n_rep, nc_fine, f, ip=1.0, patch_variant=1, smoother_variant=0,
-                omega=None, rel_tol=1e-8, abs_tol=1e-14, max_iter=100):
+                omega=None, rel_tol=1e-8, abs_tol=1e-14, max_iter=100, penalty="reference"):
     """CG + one V-cycle per iteration; returns (iterations, u, residual history)."""
     if omega is None:
         omega = lookup_damping_factor(patch_variant, smoother_variant, dim)
     f = _c64(f)
     u = np.zeros_like(f)
     hist = np.zeros(max_iter + 1)
-    it = lib().or_mg_cg_solve(dim, k, n_rep, nc_fine, float(ip), patch_variant, smoother_variant,
-                              float(omega), float(rel_tol), float(abs_tol), max_iter, _d(f), _d(u),
-                              _d(hist))
+    with _penalty(penalty):
+        it = lib().or_mg_cg_solve(dim, k, n_rep, nc_fine, float(ip), patch_variant,
+                                  smoother_variant, float(omega), float(rel_tol), float(abs_tol),
+                                  max_iter, _d(f), _d(u), _d(hist))
     n = it if it >= 0 else max_iter
     return it, u, hist[: n + 1]
 

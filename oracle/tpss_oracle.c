@@ -59,6 +59,30 @@
 
 #define OR_MAXN 32 /* largest 1-D patch size handled (2(k+1) with k <= 15) */
 
+/* SIPG penalty mode.  0: the reference's sigma = ip*gamma*(1/h_l+1/h_r)/2 inside and
+ * 2*ip*gamma/h on Dirichlet faces, gamma = k(k+1) (apps/common_integrator.h:30-37).
+ * 1: sigma = ip*2(k+1)^2*(1/h_l+1/h_r)/2 inside and ip*2(k+1)^2/h on Dirichlet faces (the
+ * "2(k+1)^2/h" penalty of the 2D DGQ3 benchmark problem; no counterpart in the reference).
+ * Both are written with gamma = k(k+1) and per-face-kind ip factors. */
+static int g_penalty_mode = 0;
+
+void or_set_penalty_mode(int mode) { g_penalty_mode = mode; }
+
+static void penalty_factors(double ip, int k, double *ip_in, double *ip_bd)
+{
+  const double gamma = (k == 0) ? 1.0 : (double)k * (k + 1.0), kp = k + 1.0;
+  if(g_penalty_mode == 1)
+  {
+    *ip_in = ip * 2.0 * kp * kp / gamma;
+    *ip_bd = ip * kp * kp / gamma;
+  }
+  else
+  {
+    *ip_in = ip;
+    *ip_bd = ip;
+  }
+}
+
 /* ===================================================================================== */
 /*                               1-D quadrature and shape data                            */
 /* ===================================================================================== */
@@ -245,6 +269,8 @@ int or_patch_matrices_1d(int k, int ncp, const double *h, int bdry_lo, int bdry_
   shape1d_init(&s, k);
   const int np = k + 1, n = ncp * np;
   const double gamma = (k == 0) ? 1.0 : (double)k * (k + 1.0);
+  double ip_in, ip_bd;
+  penalty_factors(ip, k, &ip_in, &ip_bd);
   memset(M, 0, sizeof(double) * n * n);
   memset(A, 0, sizeof(double) * n * n);
   for(int c = 0; c < ncp; ++c)
@@ -272,7 +298,7 @@ int or_patch_matrices_1d(int k, int ncp, const double *h, int bdry_lo, int bdry_
       if(!interior_face)
         at_bdry = (f == 0) ? bdry_lo : bdry_hi;
       const double avg = at_bdry ? 1.0 : 0.5;
-      const double penalty = ip * avg * 2.0 * gamma * (0.5 / hc + 0.5 / hc);
+      const double penalty = (at_bdry ? ip_bd : ip_in) * avg * 2.0 * gamma * (0.5 / hc + 0.5 / hc);
       for(int i = 0; i < np; ++i)
       {
         const double v = s.fval[f][i], dv = s.fgrad[f][i] / hc;
@@ -291,7 +317,7 @@ int or_patch_matrices_1d(int k, int ncp, const double *h, int bdry_lo, int bdry_
     /* interface between cell 0 (face 1) and cell 1 (face 0) */
     const double n0 = 1.0, n1 = -1.0;
     const double h0 = h[0], h1 = h[1];
-    const double penalty = ip * 0.5 * 2.0 * gamma * (0.5 / h0 + 0.5 / h1);
+    const double penalty = ip_in * 0.5 * 2.0 * gamma * (0.5 / h0 + 0.5 / h1);
     for(int i = 0; i < np; ++i)
     {
       const double v0 = s.fval[1][i], dv0 = s.fgrad[1][i] / h0;
@@ -805,6 +831,8 @@ static void op1d_build(op1d_t *O, int k, int nc, const double *h, double ip)
   shape1d_init(&s, k);
   const int np = k + 1, q2 = np * np;
   const double gamma = (k == 0) ? 1.0 : (double)k * (k + 1.0);
+  double ip_in, ip_bd;
+  penalty_factors(ip, k, &ip_in, &ip_bd);
   O->k = k;
   O->np = np;
   O->nc = nc;
@@ -834,7 +862,7 @@ static void op1d_build(op1d_t *O, int k, int nc, const double *h, double ip)
         if(f == 0 && c != 0) continue;
         if(f == 1 && c != nc - 1) continue;
         const double nrm = f == 0 ? -1.0 : 1.0;
-        const double sigma = ip * 2.0 * gamma * (0.5 / hc + 0.5 / hc);
+        const double sigma = ip_bd * 2.0 * gamma * (0.5 / hc + 0.5 / hc);
         for(int i = 0; i < np; ++i)
           for(int j = 0; j < np; ++j)
           {
@@ -849,7 +877,7 @@ static void op1d_build(op1d_t *O, int k, int nc, const double *h, double ip)
   for(int c = 0; c + 1 < nc; ++c)
   {
     const double hl = h[c], hr = h[c + 1];
-    const double sigma = ip * 0.5 * 2.0 * gamma * (0.5 / hl + 0.5 / hr);
+    const double sigma = ip_in * 0.5 * 2.0 * gamma * (0.5 / hl + 0.5 / hr);
     double *LL = O->blk + ((size_t)c * 3 + 1) * q2;
     double *LR = O->blk + ((size_t)c * 3 + 2) * q2;
     double *RL = O->blk + ((size_t)(c + 1) * 3 + 0) * q2;

@@ -1,6 +1,7 @@
 """Regenerates the golden fixtures in tests/golden from the CPU oracle.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py            # small fixtures (seconds)
+    python tests/golden/make_golden.py --large    # benchmark-size CG+MG histories (minutes)
 
 The reference (jwitte08/TPSS) cannot be built here (it needs deal.II) and its tests draw
 unseeded rand() values, so it ships no numeric vectors for this path.  These fixtures are
@@ -100,9 +101,34 @@ def mg():
         json.dump(res, f, indent=1)
 
 
+def mg_large():
+    """CG + V-cycle iteration counts and residual histories of the two benchmark problems,
+    FP64, coarse CG to 1e-12 (the reference's coarse solver), right-hand side f ~ U[-1,1] per
+    DoF from numpy's Philox generator with seed 0:
+      3D SIPG DGQ4 on 64^3 cells (one root cell, 7 levels), damping 0.15 (TPSS.h:121-163);
+      2D SIPG DGQ3 on 64^2 cells (2 root cells, 6 levels), damping 0.25, both penalty modes.
+    The 3D case takes minutes on a few CPU cores: it is not run by pytest."""
+    res = []
+    for dim, k, nrep, ncf, om, pen in ((2, 3, 2, 64, 0.25, "reference"), (2, 3, 2, 64, 0.25, "kp1sq"),
+                                       (3, 4, 1, 64, 0.15, "reference")):
+        N = ncf ** dim * (k + 1) ** dim
+        f = rng(0).uniform(-1.0, 1.0, N)
+        it, u, hist = O.mg_cg_solve(dim, k, nrep, ncf, f, omega=om, rel_tol=1e-8, penalty=pen)
+        assert it > 0, (dim, k, ncf, pen)
+        res.append(dict(dim=dim, k=k, n_rep=nrep, n_cells_fine=ncf, patch_variant=1,
+                        smoother_variant=0, omega=om, penalty=pen, rhs="random", rhs_seed=0,
+                        rel_tol=1e-8, iterations=it, residual_history=[float(r) for r in hist]))
+        print(dim, k, ncf, pen, it, flush=True)
+    with open(os.path.join(HERE, "mg_large.json"), "w") as f:
+        json.dump(res, f, indent=1)
+
+
 if __name__ == "__main__":
     O.build()
-    fd1d()
-    vmult()
-    mg()
+    if "--large" in sys.argv:
+        mg_large()
+    else:
+        fd1d()
+        vmult()
+        mg()
     print("golden fixtures written to", HERE)

@@ -87,6 +87,34 @@ def test_local_matrix_is_level_submatrix(oracle, xcheck, dim, k, nc, pv):
         assert np.abs(K - Kj).max() <= 1e-12 * np.abs(Kj).max()
 
 
+@pytest.mark.parametrize("dim,k,nc", [(2, 3, [4, 4]), (2, 2, [3, 4]), (3, 2, [3, 2, 3])])
+def test_kp1sq_penalty_matches_quadrature(oracle, xcheck, dim, k, nc):
+    """The opt-in penalty 2(k+1)^2/h (interior faces 2(k+1)^2 (1/h_l+1/h_r)/2, Dirichlet faces
+    2(k+1)^2/h): the oracle's operator equals the independent quadrature assembly, and every
+    vertex-patch FD matrix equals the level submatrix, as in CheckLocalSolvers
+    (tests/apps_laplace_integrator.cc:55-115)."""
+    A = xcheck.sipg_matrix(dim, k, nc, penalty="kp1sq")
+    Aref = xcheck.sipg_matrix(dim, k, nc)
+    assert np.abs(A - Aref).max() > 1e-3 * np.abs(Aref).max()  # the mode changes the matrix
+    v = np.random.default_rng(11).uniform(-1, 1, A.shape[0])
+    got = oracle.sipg_vmult(dim, k, nc, v, penalty="kp1sq")
+    assert np.abs(got - A @ v).max() <= 1e-12 * np.abs(A @ v).max()
+    lowers, _, _ = oracle.patches(dim, nc, 1, 0)
+    for lo in lowers:
+        idx = xcheck.patch_dofs(dim, k, nc, lo, 2)
+        Ms, As = [], []
+        for d in range(dim):
+            M1, A1 = oracle.patch_matrices_1d(k, [1.0 / nc[d]] * 2, lo[d] == 0, lo[d] + 1 == nc[d] - 1,
+                                              penalty="kp1sq")
+            Ms.append(M1)
+            As.append(A1)
+        Kj = A[np.ix_(idx, idx)]
+        assert np.abs(kron_sum(Ms, As) - Kj).max() <= 1e-12 * np.abs(Kj).max()
+    # the mode is reset after each call
+    np.testing.assert_allclose(oracle.sipg_vmult(dim, k, nc, v), Aref @ v, rtol=0,
+                               atol=1e-12 * np.abs(Aref @ v).max())
+
+
 @pytest.mark.parametrize("dim,n", [(2, 4), (2, 8), (3, 4), (3, 6)])
 def test_fd_inverse_matches_explicit(oracle, dim, n):
     """Kronecker-sum apply_inverse against the explicit matrix (tensor_product_matrix.cc)."""

@@ -29,7 +29,7 @@ from ._lib import (TPSS_ADDITIVE, TPSS_FP32, TPSS_FP64, TPSS_MULTIPLICATIVE, TPS
                    TPSSNotImplemented, check, load)
 
 __all__ = ["SubdomainHandler", "LaplaceOperator", "SchwarzPreconditioner", "SchwarzSmoother",
-           "MultigridSolver", "PatchVariant", "SmootherVariant", "Precision", "TimeInfo",
+           "MultigridSolver", "PatchVariant", "SmootherVariant", "Precision", "Penalty", "TimeInfo",
            "lookup_damping_factor", "prolongate_add", "restrict_add", "TPSSError",
            "TPSSNotImplemented", "TPSSInvalidArgument", "TPSSNotConverged", "load"]
 
@@ -49,6 +49,12 @@ class SmootherVariant:
 class Precision:
     fp64 = TPSS_FP64
     fp32 = TPSS_FP32
+
+
+class Penalty:
+    """SIPG penalty of the operator and the local solvers (tpss_*_desc.penalty_mode)."""
+    reference = _lib.TPSS_PENALTY_REFERENCE  # ip k(k+1) (1/h_l+1/h_r)/2 inside, 2 ip k(k+1)/h on the boundary
+    kp1sq = _lib.TPSS_PENALTY_2KP1SQ          # ip 2(k+1)^2 (1/h_l+1/h_r)/2 inside, ip 2(k+1)^2/h on the boundary
 
 
 def lookup_damping_factor(patch_variant: int, smoother_variant: int, dim: int) -> float:
@@ -203,12 +209,15 @@ class SubdomainHandler:
 class LaplaceOperator:
     """Matrix-free SIPG operator of one level (MF::Operator, FP64)."""
 
-    def __init__(self, subdomain_handler: SubdomainHandler, ip_factor: float = 1.0):
+    def __init__(self, subdomain_handler: SubdomainHandler, ip_factor: float = 1.0,
+                 penalty_mode: int = Penalty.reference):
         self.subdomain_handler = subdomain_handler
         h = C.c_void_p()
-        check(load().tpss_operator_create(subdomain_handler.handle, float(ip_factor), C.byref(h)))
+        check(load().tpss_operator_create_penalty(subdomain_handler.handle, float(ip_factor),
+                                                  int(penalty_mode), C.byref(h)))
         self._h = h
         self.ip_factor = ip_factor
+        self.penalty_mode = penalty_mode
 
     def m(self):
         return self.subdomain_handler.n_dofs()
@@ -258,6 +267,7 @@ class SchwarzPreconditioner:
         stream_variant: int = 0  # work decomposition of the column-streamed kernel (0..3)
         local_solver: int = 0    # LocalSolver.fd / exact / ksum / learned
         model: "MLP" = None      # trained network for LocalSolver.learned
+        penalty_mode: int = Penalty.reference  # must match the level operator's
 
     def __init__(self):
         self._h = None
@@ -278,6 +288,7 @@ class SchwarzPreconditioner:
         d.stream_variant = int(ad.stream_variant)
         d.local_solver = int(ad.local_solver)
         d.model = ad.model.handle if ad.model is not None else None
+        d.penalty_mode = int(ad.penalty_mode)
         return d
 
     def initialize(self, subdomain_handler, linear_operator=None, additional_data=None):
@@ -630,7 +641,8 @@ class MultigridSolver:
                  smoother_variant=SmootherVariant.additive, relaxation=None, ip_factor=1.0,
                  precision=Precision.fp64, coarse_tol=1e-12, coarse_solver=0, use_graph=True,
                  vertex_coords=None, surrogate_n_q=5, local_solver=0, model=None,
-                 auto_relaxation=False, vcycle_precision=Precision.fp64):
+                 auto_relaxation=False, vcycle_precision=Precision.fp64,
+                 penalty_mode=Penalty.reference):
         if relaxation is None:
             relaxation = lookup_damping_factor(patch_variant, smoother_variant, dim)
         d = _lib.MgDesc()
@@ -643,6 +655,7 @@ class MultigridSolver:
         d.model = model.handle if model is not None else None
         d.auto_relaxation = int(auto_relaxation)
         d.vcycle_precision = int(vcycle_precision)
+        d.penalty_mode = int(penalty_mode)
         self._model = model
         d.dim, d.degree, d.n_rep, d.n_cells_fine = dim, degree, n_rep, n_cells_fine
         d.ip_factor, d.patch_variant, d.smoother_variant = float(ip_factor), patch_variant, smoother_variant

@@ -33,6 +33,8 @@ TPSS_FP32 = 1
 TPSS_KERNEL_AUTO = 0
 TPSS_KERNEL_COLOR = 1
 TPSS_KERNEL_STREAM = 2
+TPSS_PENALTY_REFERENCE = 0
+TPSS_PENALTY_2KP1SQ = 1
 
 
 class TPSSError(RuntimeError):
@@ -66,7 +68,7 @@ class PrecondDesc(C.Structure):
                 ("use_ras_weights", C.c_int), ("use_ras_boolean_weights", C.c_int),
                 ("precision", C.c_int), ("ip_factor", C.c_double), ("check_finite", C.c_int),
                 ("kernel_variant", C.c_int), ("stream_variant", C.c_int),
-                ("local_solver", C.c_int), ("model", C.c_void_p)]
+                ("local_solver", C.c_int), ("model", C.c_void_p), ("penalty_mode", C.c_int)]
 
 
 class C0ipDesc(C.Structure):
@@ -92,7 +94,7 @@ class MgDesc(C.Structure):
                 ("coarse_solver", C.c_int), ("use_graph", C.c_int),
                 ("vertex_coords", C.POINTER(C.c_double)), ("surrogate_n_q", C.c_int),
                 ("local_solver", C.c_int), ("model", C.c_void_p), ("auto_relaxation", C.c_int),
-                ("vcycle_precision", C.c_int)]
+                ("vcycle_precision", C.c_int), ("penalty_mode", C.c_int)]
 
 
 _vp = C.c_void_p
@@ -106,6 +108,7 @@ SIGNATURES = {
     "tpss_layout_patches": (C.c_int, [_vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "tpss_layout_destroy": (None, [_vp]),
     "tpss_operator_create": (C.c_int, [_vp, C.c_double, C.POINTER(_vp)]),
+    "tpss_operator_create_penalty": (C.c_int, [_vp, C.c_double, C.c_int, C.POINTER(_vp)]),
     "tpss_operator_vmult": (C.c_int, [_vp, _vp, _vp, _vp]),
     "tpss_operator_vmult_fp32": (C.c_int, [_vp, _vp, _vp, _vp]),
     "tpss_operator_destroy": (None, [_vp]),

@@ -139,14 +139,27 @@ struct Shape1D
   std::vector<double> fval[2], fgrad[2];  // at x=0 and x=1
 };
 Shape1D make_shape_1d(int k);
+// Effective ip factors of the SIPG faces: interior faces sigma = in * gamma * (1/h_l + 1/h_r)/2,
+// Dirichlet faces sigma = 2 * bd * gamma / h, gamma = k(k+1). A plain ip converts to in = bd = ip
+// (the reference's penalty).
+struct Penalty
+{
+  double in = 1.0, bd = 1.0;
+  Penalty() = default;
+  Penalty(double ip) : in(ip), bd(ip) {}
+  Penalty(double i, double b) : in(i), bd(b) {}
+};
+// TPSS_PENALTY_REFERENCE: in = bd = ip; TPSS_PENALTY_2KP1SQ: sigma = ip 2(k+1)^2 (1/h_l+1/h_r)/2
+// inside and ip 2(k+1)^2 / h on the boundary
+Penalty make_penalty(double ip, int mode, int k);
 // 1-D DG patch matrices of the FD local solver (ncp = 1 or 2 cells)
 void patch_matrices_1d(const Shape1D &s, int ncp, const double *h, bool bdry_lo, bool bdry_hi,
-                       double ip, double *M, double *A);
+                       Penalty ip, double *M, double *A);
 // global 1-D SIPG blocks of one direction: mass[c][np^2], blk[c][3][np^2]
-void operator_blocks_1d(const Shape1D &s, int nc, const double *h, double ip,
+void operator_blocks_1d(const Shape1D &s, int nc, const double *h, Penalty ip,
                         std::vector<double> &mass, std::vector<double> &blk);
 // per-cell 1-D factors of the operator: mass, own block, rank-2 neighbour couplings
-std::vector<double> operator_factors_1d(const Shape1D &s, int nc, const double *h, double ip);
+std::vector<double> operator_factors_1d(const Shape1D &s, int nc, const double *h, Penalty ip);
 // child embedding E[s][i*np+j] = phi_j((z_i+s)/2)
 std::vector<double> embedding_1d(const Shape1D &s);
 
@@ -210,6 +223,7 @@ struct tpss_operator
 {
   const tpss_layout *layout = nullptr;
   double ip = 1.0;
+  int penalty_mode = TPSS_PENALTY_REFERENCE;
   tpss::DeviceBuffer<double> d_mass[3], d_blk[3];
   tpss::DeviceBuffer<double> d_fac[3];  // operator_factors_1d per direction
   tpss::DeviceBuffer<float> d_fac32[3];  // the same in FP32 (single-precision level operator)
@@ -338,7 +352,7 @@ bool launch_fd_f64(int dim, int k, int ncp, const FdLaunch &a, cudaStream_t s);
 
 // mapped (distorted) levels (mapped.cu)
 size_t mapped_smem_bytes(int dim, int np);
-void mapped_build(tpss_operator &op, const tpss_layout &L, double ip);
+void mapped_build(tpss_operator &op, const tpss_layout &L, Penalty ip);
 void mapped_apply(const tpss_operator &op, double *dst, const double *src, cudaStream_t s,
                   const double *rhs = nullptr);
 // FP32 blocks and source, FP64 result (the level operator of a single-precision V-cycle)
@@ -349,7 +363,7 @@ std::vector<double> mapped_dense(const tpss_operator &op);
 void gen_eig_batched(int n, int n_problems, const std::vector<double> &Ms,
                      const std::vector<double> &As, std::vector<double> &S,
                      std::vector<double> &lam);
-void key_matrices(const tpss_layout &L, double ip, std::vector<double> &Ms, std::vector<double> &As);
+void key_matrices(const tpss_layout &L, Penalty ip, std::vector<double> &Ms, std::vector<double> &As);
 std::vector<double> per_patch(const tpss_layout &L, const std::vector<double> &keyed);
 int64_t keep_definite(const tpss_layout &L, const std::vector<double> &Mp, std::vector<double> &Ap,
                       const std::vector<double> &Asur);
@@ -426,4 +440,6 @@ void layout_to_device(const tpss_layout &L);
 
 // preconditioner internals (precond.cu)
 void precond_vmult(tpss_precond *p, double *dst, const double *src, cudaStream_t s);
+// the column-streamed FP32 smoother can serve this preconditioner (layout, precision, tables)
+bool stream_eligible(const tpss_precond *p);
 }  // namespace tpss

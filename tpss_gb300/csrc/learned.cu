@@ -78,7 +78,7 @@ std::vector<float> features(const tpss_layout &L)
 }
 
 // surrogate 1-D problems of every patch direction (entry p * dim + d)
-void surrogate_problems(const tpss_layout &L, double ip, std::vector<double> &Mp, std::vector<double> &Ap)
+void surrogate_problems(const tpss_layout &L, Penalty ip, std::vector<double> &Mp, std::vector<double> &Ap)
 {
   std::vector<double> Mk, Ak;
   key_matrices(L, ip, Mk, Ak);
@@ -105,7 +105,7 @@ std::shared_ptr<FdTables> build_learned_tables(const tpss_layout &L, const tpss_
     TPSS_CUDA(cudaMemcpy(Y.data(), dy.ptr, sizeof(float) * Y.size(), cudaMemcpyDeviceToHost));
   }
   std::vector<double> Mp, Ap;
-  surrogate_problems(L, d.ip_factor, Mp, Ap);
+  surrogate_problems(L, make_penalty(d.ip_factor, d.penalty_mode, L.k), Mp, Ap);
   const std::vector<double> Asur = Ap;
   std::vector<double> H(nn), W(nn);
   int64_t fallbacks = 0;

@@ -38,7 +38,7 @@ struct AsmArgs
   const double *coords;  // lexicographic vertices, dim coordinates each
   int nc[3];
   int np, nd, nb;
-  double ip, gamma;
+  double ip, ip_bd, gamma;  // interior / boundary ip factors
   double *vals;
   int32_t *col;
 };
@@ -330,7 +330,7 @@ __global__ void __launch_bounds__(256) assemble_kernel(const AsmArgs a, const Ma
         }
       }
       __syncthreads();
-      const double sigma = boundary ? a.ip * 2.0 * a.gamma / hh[0]
+      const double sigma = boundary ? a.ip_bd * 2.0 * a.gamma / hh[0]
                                     : a.ip * a.gamma * (1.0 / hh[0] + 1.0 / hh[1]) * 0.5;
       const double beta = boundary ? 1.0 : 0.5;
       for(int e = threadIdx.x; e < nd * nd; e += blockDim.x)
@@ -434,7 +434,7 @@ size_t mapped_smem_bytes(int dim, int np)
   return sizeof(double) * (48 + (size_t)nq * ns + nfq + 2 * (size_t)nfq * dim + 2 + 4 * (size_t)nfq * nd);
 }
 
-void mapped_build(tpss_operator &op, const tpss_layout &L, double ip)
+void mapped_build(tpss_operator &op, const tpss_layout &L, Penalty ip)
 {
   TPSS_REQUIRE(L.k + 1 <= kMaxNp, "mapped operator: degree must be at most 7");
   const size_t smem = mapped_smem_bytes(L.dim, L.np);
@@ -452,7 +452,8 @@ void mapped_build(tpss_operator &op, const tpss_layout &L, double ip)
   a.np = L.np;
   a.nd = M->nd;
   a.nb = M->nb;
-  a.ip = ip;
+  a.ip = ip.in;
+  a.ip_bd = ip.bd;
   a.gamma = L.k == 0 ? 1.0 : L.k * (L.k + 1.0);
   a.vals = M->vals.ptr;
   a.col = M->col.ptr;

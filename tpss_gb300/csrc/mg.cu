@@ -65,7 +65,7 @@ int grid_for(int64_t n)
 
 // Dense SIPG matrix of a small Cartesian level (Kronecker sum of the global 1-D operators),
 // FP64 on the host.
-std::vector<double> dense_matrix(const tpss_layout &L, double ip)
+std::vector<double> dense_matrix(const tpss_layout &L, Penalty ip)
 {
   const Shape1D s = make_shape_1d(L.k);
   const int np = L.np, dim = L.dim;
@@ -483,7 +483,7 @@ extern "C" int tpss_mg_create(const tpss_mg_desc *d, tpss_mg **out)
       for(int dd = 0; dd < 3; ++dd) ld.n_cells[dd] = dd < d->dim ? (d->n_rep << l) : 1;
       int rc = tpss_layout_create(&ld, &lv.L);
       if(rc) fail(rc, tpss_last_error());
-      rc = tpss_operator_create(lv.L, d->ip_factor, &lv.op);
+      rc = tpss_operator_create_penalty(lv.L, d->ip_factor, d->penalty_mode, &lv.op);
       if(rc) fail(rc, tpss_last_error());
       if(l > 0)
       {
@@ -491,6 +491,7 @@ extern "C" int tpss_mg_create(const tpss_mg_desc *d, tpss_mg **out)
         pd.relaxation = d->relaxation;
         pd.precision = d->precision;
         pd.ip_factor = d->ip_factor;
+        pd.penalty_mode = d->penalty_mode;
         pd.local_solver = d->local_solver;
         pd.model = d->model;
         rc = tpss_precond_create(lv.L, lv.op, &pd, &lv.P);
@@ -508,7 +509,9 @@ extern "C" int tpss_mg_create(const tpss_mg_desc *d, tpss_mg **out)
       TPSS_REQUIRE(n0 <= 4096, "dense coarse solver limited to 4096 coarse DoFs");
       const tpss_operator &cop = *mg->lv[0].op;
       std::vector<double> inv = cholesky_inverse(
-        cop.mapped ? mapped_dense(cop) : dense_matrix(*mg->lv[0].L, d->ip_factor), n0);
+        cop.mapped ? mapped_dense(cop)
+                   : dense_matrix(*mg->lv[0].L, make_penalty(d->ip_factor, d->penalty_mode, d->degree)),
+        n0);
       mg->coarse_inv.upload(inv.data(), inv.size());
     }
     mg->cp.resize(n0);

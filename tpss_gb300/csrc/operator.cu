@@ -707,18 +707,26 @@ using namespace tpss;
 
 extern "C" int tpss_operator_create(const tpss_layout *layout, double ip_factor, tpss_operator **out)
 {
+  return tpss_operator_create_penalty(layout, ip_factor, TPSS_PENALTY_REFERENCE, out);
+}
+
+extern "C" int tpss_operator_create_penalty(const tpss_layout *layout, double ip_factor, int penalty_mode,
+                                            tpss_operator **out)
+{
   return guarded([&] {
     TPSS_REQUIRE(layout && out, "null argument");
     TPSS_REQUIRE(ip_factor > 0.0, "ip_factor must be positive");
     *out = nullptr;
+    const Penalty pen = make_penalty(ip_factor, penalty_mode, layout->k);
     layout_to_device(*layout);
     auto op = std::make_unique<tpss_operator>();
     op->layout = layout;
     op->ip = ip_factor;
+    op->penalty_mode = penalty_mode;
     if(!layout->coords.empty())
     {
       // distorted level: block-sparse matrix assembled by quadrature on the mapped cells
-      mapped_build(*op, *layout, ip_factor);
+      mapped_build(*op, *layout, pen);
       *out = op.release();
       return;
     }
@@ -726,7 +734,7 @@ extern "C" int tpss_operator_create(const tpss_layout *layout, double ip_factor,
     op->sparse_faces = true;
     for(int d = 0; d < layout->dim; ++d)
     {
-      const std::vector<double> fac0 = operator_factors_1d(s, layout->nc[d], layout->h[d].data(), ip_factor);
+      const std::vector<double> fac0 = operator_factors_1d(s, layout->nc[d], layout->h[d].data(), pen);
       // per cell: the factors, then the even/odd form of the cell mass (mass_pass)
       const int np = layout->np, q2 = np * np, fs0 = 2 * q2 + 8 * np, hh = np / 2;
       const int fs = fs0 + 2 * hh * hh + 2 * hh + 1;

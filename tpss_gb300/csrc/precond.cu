@@ -114,7 +114,7 @@ void build_even_odd(const tpss_layout &L, FdTables &T, const std::vector<double>
 }  // namespace
 
 // 1-D patch matrices (mass, SIPG Laplace) of every FD key of the layout
-void key_matrices(const tpss_layout &L, double ip, std::vector<double> &Ms, std::vector<double> &As)
+void key_matrices(const tpss_layout &L, Penalty ip, std::vector<double> &Ms, std::vector<double> &As)
 {
   const int n = L.n, nn = n * n, ne = (int)L.fd_keys.size();
   const Shape1D shape = make_shape_1d(L.k);
@@ -181,7 +181,7 @@ namespace
 {
 // FD tables of the layout's keys, or (patchM, patchA given) of one 1-D problem per patch and
 // direction
-std::shared_ptr<FdTables> build_tables(const tpss_layout &L, double ip, bool ras,
+std::shared_ptr<FdTables> build_tables(const tpss_layout &L, Penalty ip, bool ras,
                                        const std::vector<double> *patchM = nullptr,
                                        const std::vector<double> *patchA = nullptr)
 {
@@ -258,6 +258,7 @@ std::shared_ptr<FdTables> build_local_solvers(const tpss_layout &L, const tpss_o
                                               const tpss_precond_desc &d)
 {
   const bool ras = d.use_ras_weights != 0;
+  const Penalty pen = make_penalty(d.ip_factor, d.penalty_mode, L.k);
   switch(d.local_solver)
   {
   case TPSS_LOCAL_EXACT:
@@ -277,21 +278,21 @@ std::shared_ptr<FdTables> build_local_solvers(const tpss_layout &L, const tpss_o
     check_exact_local(L, op);
     auto t0 = std::chrono::steady_clock::now();
     std::vector<double> Mk, Ak;
-    key_matrices(L, d.ip_factor, Mk, Ak);
+    key_matrices(L, pen, Mk, Ak);
     const std::vector<double> Mp = per_patch(L, Mk);
     std::vector<double> Ap = ksum_fit(L, *op, Mp);
     const int64_t kept = keep_definite(L, Mp, Ap, per_patch(L, Ak));
-    auto T = build_tables(L, d.ip_factor, ras, &Mp, &Ap);
+    auto T = build_tables(L, pen, ras, &Mp, &Ap);
     T->learned_fallbacks = kept;
     T->setup_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     return T;
   }
   case TPSS_LOCAL_LEARNED:
     return build_learned_tables(L, d, [&](const std::vector<double> *Mp, const std::vector<double> *Ap) {
-      return build_tables(L, d.ip_factor, ras, Mp, Ap);
+      return build_tables(L, pen, ras, Mp, Ap);
     });
   default:
-    return build_tables(L, d.ip_factor, ras);
+    return build_tables(L, pen, ras);
   }
 }
 
@@ -302,6 +303,8 @@ void validate_desc(const tpss_precond_desc &d)
   TPSS_REQUIRE(d.stream_variant >= 0 && d.stream_variant <= 5, "stream_variant must be in 0..5");
   TPSS_REQUIRE(d.relaxation > 0.0, "Invalid relaxation factor.");
   TPSS_REQUIRE(d.precision == TPSS_FP64 || d.precision == TPSS_FP32, "invalid precision");
+  TPSS_REQUIRE(d.penalty_mode == TPSS_PENALTY_REFERENCE || d.penalty_mode == TPSS_PENALTY_2KP1SQ,
+               "invalid penalty_mode");
   TPSS_REQUIRE(d.local_solver >= TPSS_LOCAL_FD && d.local_solver <= TPSS_LOCAL_LEARNED,
                "invalid local solver");
   if(d.local_solver == TPSS_LOCAL_EXACT && d.use_ras_weights)
@@ -472,12 +475,19 @@ bool launch_fd_f64(int dim, int k, int ncp, const FdLaunch &a, cudaStream_t s)
   return dim == 2 ? launch_fd_double_2(k, ncp, a, s) : launch_fd_double_3(k, ncp, a, s);
 }
 
-bool use_stream(const tpss_precond *p)
+// the column-streamed FP32 smoother applies to this preconditioner: additive 3D vertex patches
+// on a Cartesian level with k <= 4, keyed FD tables (not dense inverses, not per-patch entries)
+bool stream_eligible(const tpss_precond *p)
 {
   const tpss_layout &L = *p->tables->layout;
+  return L.smoother_variant == TPSS_ADDITIVE && p->desc.precision == TPSS_FP32 &&
+         stream_supported(L) && !p->tables->dense && p->tables->own_fd.n == 0;
+}
+
+bool use_stream(const tpss_precond *p)
+{
   if(p->desc.kernel_variant == TPSS_KERNEL_COLOR) return false;
-  const bool ok = L.smoother_variant == TPSS_ADDITIVE && p->desc.precision == TPSS_FP32 &&
-                  stream_supported(L) && !p->tables->dense && p->tables->own_fd.n == 0;
+  const bool ok = stream_eligible(p);
   if(p->desc.kernel_variant == TPSS_KERNEL_STREAM && !ok)
     fail(TPSS_ERR_INVALID_ARGUMENT, "the streamed kernel needs additive 3D vertex patches, FP32, k <= 4");
   return ok;
@@ -607,6 +617,8 @@ extern "C" int tpss_precond_create_shallow(const tpss_precond *other, const tpss
     validate_desc(*desc);
     TPSS_REQUIRE(desc->ip_factor == other->desc.ip_factor,
                  "shallow copies share the local solvers: ip_factor must match");
+    TPSS_REQUIRE(desc->penalty_mode == other->desc.penalty_mode,
+                 "shallow copies share the local solvers: penalty_mode must match");
     TPSS_REQUIRE(desc->local_solver == other->desc.local_solver && desc->model == other->desc.model,
                  "shallow copies share the local solvers: local_solver must match");
     if(other->tables->dense)

@@ -132,8 +132,17 @@ Shape1D make_shape_1d(int k)
   return s;
 }
 
+Penalty make_penalty(double ip, int mode, int k)
+{
+  if(mode == TPSS_PENALTY_REFERENCE) return Penalty(ip);
+  TPSS_REQUIRE(mode == TPSS_PENALTY_2KP1SQ, "unknown penalty_mode");
+  // interior: in * gamma = 2 (k+1)^2; boundary: 2 bd gamma = 2 (k+1)^2
+  const double gamma = k == 0 ? 1.0 : double(k) * (k + 1), kp = k + 1.0;
+  return Penalty(ip * 2.0 * kp * kp / gamma, ip * kp * kp / gamma);
+}
+
 void patch_matrices_1d(const Shape1D &s, int ncp, const double *h, bool bdry_lo, bool bdry_hi,
-                       double ip, double *M, double *A)
+                       Penalty ip, double *M, double *A)
 {
   const int np = s.np, n = ncp * np;
   const double gamma = s.k == 0 ? 1.0 : double(s.k) * (s.k + 1);
@@ -163,7 +172,7 @@ void patch_matrices_1d(const Shape1D &s, int ncp, const double *h, bool bdry_lo,
       const bool interface = ncp == 2 && ((c == 0 && f == 1) || (c == 1 && f == 0));
       const bool physical = !interface && (f == 0 ? bdry_lo : bdry_hi);
       const double avg = physical ? 1.0 : 0.5;
-      const double penalty = ip * avg * 2.0 * gamma / hc;
+      const double penalty = (physical ? ip.bd : ip.in) * avg * 2.0 * gamma / hc;
       for(int i = 0; i < np; ++i)
         for(int j = 0; j < np; ++j)
         {
@@ -176,7 +185,7 @@ void patch_matrices_1d(const Shape1D &s, int ncp, const double *h, bool bdry_lo,
   if(ncp == 2)
   {
     const double h0 = h[0], h1 = h[1];
-    const double penalty = ip * gamma * (0.5 / h0 + 0.5 / h1);  // ip * 0.5 * 2 gamma (...)
+    const double penalty = ip.in * gamma * (0.5 / h0 + 0.5 / h1);  // ip * 0.5 * 2 gamma (...)
     for(int i = 0; i < np; ++i)
       for(int j = 0; j < np; ++j)
       {
@@ -191,7 +200,7 @@ void patch_matrices_1d(const Shape1D &s, int ncp, const double *h, bool bdry_lo,
   }
 }
 
-void operator_blocks_1d(const Shape1D &s, int nc, const double *h, double ip,
+void operator_blocks_1d(const Shape1D &s, int nc, const double *h, Penalty ip,
                         std::vector<double> &mass, std::vector<double> &blk)
 {
   const int np = s.np, q2 = np * np;
@@ -218,7 +227,7 @@ void operator_blocks_1d(const Shape1D &s, int nc, const double *h, double ip,
     for(int f = 0; f < 2; ++f)
     {
       if((f == 0 && c != 0) || (f == 1 && c != nc - 1)) continue;
-      const double nu = f == 0 ? -1.0 : 1.0, sigma = ip * 2.0 * gamma / hc;
+      const double nu = f == 0 ? -1.0 : 1.0, sigma = ip.bd * 2.0 * gamma / hc;
       for(int i = 0; i < np; ++i)
         for(int j = 0; j < np; ++j)
         {
@@ -231,7 +240,7 @@ void operator_blocks_1d(const Shape1D &s, int nc, const double *h, double ip,
   for(int c = 0; c + 1 < nc; ++c)
   {
     const double hl = h[c], hr = h[c + 1];
-    const double sigma = ip * 0.5 * gamma * (1.0 / hl + 1.0 / hr);
+    const double sigma = ip.in * 0.5 * gamma * (1.0 / hl + 1.0 / hr);
     double *LL = &blk[((size_t)c * 3 + 1) * q2], *LR = &blk[((size_t)c * 3 + 2) * q2];
     double *RL = &blk[((size_t)(c + 1) * 3 + 0) * q2], *RR = &blk[((size_t)(c + 1) * 3 + 1) * q2];
     for(int i = 0; i < np; ++i)
@@ -273,7 +282,7 @@ namespace tpss
 //   block(c, c+1) = aR_0 bR_0^T + aR_1 bR_1^T,  block(c, c-1) = aL_0 bL_0^T + aL_1 bL_1^T
 // (zero at the physical boundary), from the interior-face terms
 // sigma [u][v] - {u'}[v] - [u]{v'} with sigma = ip gamma (1/h_l + 1/h_r)/2.
-std::vector<double> operator_factors_1d(const Shape1D &s, int nc, const double *h, double ip)
+std::vector<double> operator_factors_1d(const Shape1D &s, int nc, const double *h, Penalty ip)
 {
   const int np = s.np, q2 = np * np, stride = 2 * q2 + 8 * np;
   const double gamma = s.k == 0 ? 1.0 : double(s.k) * (s.k + 1);
@@ -292,7 +301,7 @@ std::vector<double> operator_factors_1d(const Shape1D &s, int nc, const double *
     if(c > 0)
     {
       const double hl = h[c - 1], hc = h[c];
-      const double sigma = ip * 0.5 * gamma * (1.0 / hl + 1.0 / hc);
+      const double sigma = ip.in * 0.5 * gamma * (1.0 / hl + 1.0 / hc);
       for(int i = 0; i < np; ++i)
       {
         aL[i] = s.fval[0][i];                // test value at the cell's left face
@@ -304,7 +313,7 @@ std::vector<double> operator_factors_1d(const Shape1D &s, int nc, const double *
     if(c + 1 < nc)
     {
       const double hc = h[c], hr = h[c + 1];
-      const double sigma = ip * 0.5 * gamma * (1.0 / hc + 1.0 / hr);
+      const double sigma = ip.in * 0.5 * gamma * (1.0 / hc + 1.0 / hr);
       for(int i = 0; i < np; ++i)
       {
         aR[i] = s.fval[1][i];

@@ -423,10 +423,17 @@ extern "C" int tpss_precond_vmult_static_scratch(tpss_precond *p, double *dst, c
     TPSS_REQUIRE(p && dst && src, "null argument");
     TPSS_REQUIRE(dst != src, "dst and src must not alias");
     const tpss_layout &L = *p->tables->layout;
-    if(!(L.smoother_variant == TPSS_ADDITIVE && p->desc.precision == TPSS_FP32 && tpss::stream_supported(L)))
+    if(!tpss::stream_eligible(p))
       tpss::fail(TPSS_ERR_INVALID_ARGUMENT,
                  "the allocation-free smoother needs additive 3D vertex patches on a Cartesian level, "
-                 "FP32 arithmetic and degree <= 4");
+                 "FP32 arithmetic, degree <= 4 and fast-diagonalization local solvers");
+    // options that would need memory or a second kernel path are refused rather than ignored
+    TPSS_REQUIRE(!p->desc.check_finite,
+                 "the allocation-free smoother has no finiteness check (its flag would need a buffer); "
+                 "create the preconditioner with check_finite = 0");
+    TPSS_REQUIRE(p->desc.kernel_variant != TPSS_KERNEL_COLOR,
+                 "the allocation-free smoother is the column-streamed kernel; kernel_variant asks for "
+                 "the per-color kernel");
     cudaStream_t s = tpss::as_stream(stream);
     switch(L.k)
     {
