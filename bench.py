@@ -89,6 +89,14 @@ def workload(args):
                 flops=P * flops_per_patch, bytes=N * 16)
 
 
+def workload_name(args, W):
+    """config.workload of both arms (the same string, so that their lines compare)."""
+    n, k = args.cells, args.degree
+    prec = "FP32" if args.precision == "fp32" else "FP64"
+    return (f"additive vertex-patch Schwarz vmult, 3D SIPG DGQ{k}, {n}^3 cells, {W['N']} DoFs, "
+            f"{W['P']} patches of {W['n1d']}^3, {prec} smoother / FP64 vectors")
+
+
 def philox_src(N, seed):
     import numpy as np
     return np.random.Generator(np.random.Philox(seed)).uniform(-1.0, 1.0, N)
@@ -177,14 +185,16 @@ def ncu_traffic(dim, k):
 
 
 def cpu_baseline(args, W):
-    """Oracle port (plain C, OpenMP over patches of a color, FP64) on all host threads: a
-    full vmult of the same workload, repeated, ~a few seconds."""
+    """The reference's CPU path restated with SIMD macro patches (oracle/simd_baseline.c: 8 FP64
+    lanes per macro patch, lane-wise eigenvectors, FMA, OpenMP over the macro patches of a
+    color), FP64: full vmults of the same workload on all host threads (a few seconds), and a
+    bounded sample (1/16 of the patches, all colors) on one thread."""
     from oracle import oracle as O
     O.build()
     import numpy as np
-    threads = O.num_threads()
+    threads = O.simd_num_threads()
     n = args.cells
-    h = O.SchwarzHandle(args.dim, args.degree, (n,) * args.dim, patch_variant=1, omega=args.omega)
+    h = O.SimdSchwarzHandle(args.dim, args.degree, (n,) * args.dim, patch_variant=1, omega=args.omega)
     src = philox_src(W["N"], args.seed)
     dst = np.zeros_like(src)
     h.apply(dst, src)  # warm-up (page-in)
@@ -195,11 +205,22 @@ def cpu_baseline(args, W):
         el = time.perf_counter() - t0
         if el > 8.0 or reps >= 5:
             break
-    h.close()
     per = el / reps
+    P = h.n_patches
+    part = max(1, P // 16)
+    O.simd_set_num_threads(1)
+    t0 = time.perf_counter()
+    h.apply_range(0, part, dst, src)
+    one = (time.perf_counter() - t0) * P / part
+    O.simd_set_num_threads(threads)
+    h.close()
     return {"value": W["N"] / per, "unit": "DoF/s", "cores": threads, "kind": "port",
             "sample": f"{reps} full FP64 vmults of the same 3D DGQ{args.degree} {n}^3 workload, "
-                      f"{per:.3f} s each, {threads} OpenMP threads"}
+                      f"{per:.3f} s each, {threads} OpenMP threads; SIMD restatement of the "
+                      f"reference's CPU path (macro patches of 8 FP64 lanes, FMA)",
+            "single_core": {"value": W["N"] / one, "unit": "DoF/s", "cores": 1,
+                            "sample": f"patches 0..{part} of {P} on one thread, scaled to a vmult "
+                                      f"({one:.2f} s)"}}
 
 
 def run_reference(args):
@@ -211,7 +232,7 @@ def run_reference(args):
     O.build()
     import numpy as np
     n = args.cells
-    h = O.SchwarzHandle(args.dim, args.degree, (n,) * args.dim, patch_variant=1, omega=args.omega)
+    h = O.SimdSchwarzHandle(args.dim, args.degree, (n,) * args.dim, patch_variant=1, omega=args.omega)
     src = philox_src(W["N"], args.seed)
     dst = np.zeros_like(src)
     # one step = a bounded sample: 1/8 of the patches (about one color's worth) per step
@@ -230,17 +251,16 @@ def run_reference(args):
     el = time.perf_counter() - t0
     h.close()
     value = W["N"] * (done / P) / el
-    threads = O.num_threads()
+    threads = O.simd_num_threads()
     line = {"metric": METRIC, "value": value, "unit": "DoF/s", "n_gpus": args.gpus, "steps": steps,
             "warmup": warm, "ms_per_step": 1e3 * el / steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "impl": "reference",
-            "config": {"workload": f"additive vertex-patch Schwarz vmult, 3D SIPG DGQ{args.degree}, "
-                                   f"{n}^3 cells, {W['N']} DoFs",
-                       "sample_per_step": f"{chunk} of {P} patches"},
+            "config": {"workload": workload_name(args, W), "sample_per_step": f"{chunk} of {P} patches"},
             "cpu_baseline": {"value": value, "unit": "DoF/s", "cores": threads, "kind": "port",
                              "sample": f"{steps} steps of {chunk} patches (1/8 of a vmult) each, "
-                                       f"CPU oracle port, {threads} OpenMP threads"},
+                                       f"SIMD restatement of the reference's CPU path (macro "
+                                       f"patches of 8 FP64 lanes, FMA), {threads} OpenMP threads"},
             "e2e": {"value": value, "unit": "DoF/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -350,8 +370,7 @@ def run_ours(args):
            "warmup": args.warmup, "ms_per_step": t_max, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32" if prec == tpss.Precision.fp32 else "f64",
            "data": "synthetic (f ~ U[-1,1] per DoF, numpy Philox seed %d)" % args.seed,
-           "config": {"workload": f"additive vertex-patch Schwarz vmult, 3D SIPG DGQ{k}, {n}^3 cells, "
-                                  f"{W['N']} DoFs, {P} patches of {W['n1d']}^3, FP32 smoother / FP64 vectors",
+           "config": {"workload": workload_name(args, W),
                       "dim": dim, "degree": k, "cells_per_direction": n, "n_dofs": W["N"],
                       "n_patches": P, "n_colors": n_colors, "relaxation": args.omega,
                       "l2": "inputs larger than L2 (src and dst 262 MB each)",

@@ -147,7 +147,10 @@ typedef struct tpss_precond_desc
   int reverse;                 /* reverse color sequence (multiplicative) */
   int symmetrized;             /* forward + backward color sweep (multiplicative) */
   int use_ras_weights;         /* divide local solutions by patch multiplicity (additive) */
-  int use_ras_boolean_weights; /* not implemented: returns TPSS_ERR_NOT_IMPLEMENTED */
+  int use_ras_boolean_weights; /* restricted prolongation (rscatter_add): every DoF is added by
+                                  one patch only, the one where it lies closest to the patch
+                                  centre (dof_info.templates.h:194-313); additive vertex patches,
+                                  FD local solvers (cell patches: TPSS_ERR_NOT_IMPLEMENTED) */
   int precision;               /* TPSS_FP64 or TPSS_FP32 smoother arithmetic */
   double ip_factor;            /* EquationData::ip_factor of the local SIPG matrices */
   int check_finite;            /* 1: vmult checks that dst is finite (one extra reduction) */

@@ -27,10 +27,16 @@ _i64p = C.POINTER(C.c_int64)
 _i32p = C.POINTER(C.c_int32)
 
 
+_SIMD_PATH = os.path.join(_HERE, "_build", "liboracle_simd.so")
+
+
 def build(force: bool = False) -> str:
-    """Compile the oracle with its Makefile (gcc) and return the library path."""
-    src = os.path.join(_HERE, "tpss_oracle.c")
-    if force or not os.path.exists(_LIB_PATH) or os.path.getmtime(_LIB_PATH) < os.path.getmtime(src):
+    """Compile the oracle and the SIMD CPU baseline with their Makefile (gcc) and return the
+    oracle library path."""
+    srcs = [os.path.join(_HERE, f) for f in ("tpss_oracle.c", "simd_baseline.c")]
+    newest = max(os.path.getmtime(s) for s in srcs)
+    stale = any(not os.path.exists(p) or os.path.getmtime(p) < newest for p in (_LIB_PATH, _SIMD_PATH))
+    if force or stale:
         subprocess.run(["make", "-s", "-C", _HERE], check=True)
     return _LIB_PATH
 
@@ -208,7 +214,8 @@ def schwarz_vmult(dim, k, nc, src, patch_variant=1, smoother_variant=0, omega=1.
                                     _d(hs[2]), float(ip),
                                     cs.ctypes.data_as(_i64p) if cs is not None else None,
                                     patch_variant, smoother_variant, float(omega), int(reverse),
-                                    int(symmetrized), int(use_ras), _d(src), _d(dst))
+                                    int(symmetrized), 2 if use_ras == "boolean" else int(bool(use_ras)),
+                                    _d(src), _d(dst))
     assert rc == 0
     return dst
 
@@ -304,6 +311,68 @@ class SchwarzHandle:
             self.close()
         except Exception:
             pass
+
+
+_simd = None
+
+
+def simd_lib():
+    """The timed CPU baseline (oracle/simd_baseline.c: SIMD macro patches of 8 FP64 lanes)."""
+    global _simd
+    with _lock:
+        if _simd is None:
+            build()
+            L = C.CDLL(_SIMD_PATH)
+            L.or_simd_create.argtypes = [C.c_int, C.c_int, _ip, C.c_int, C.c_double]
+            L.or_simd_create.restype = C.c_void_p
+            L.or_simd_apply.argtypes = [C.c_void_p, _dp, _dp]
+            L.or_simd_apply_range.argtypes = [C.c_void_p, C.c_int64, C.c_int64, _dp, _dp]
+            L.or_simd_n_patches.argtypes = [C.c_void_p]
+            L.or_simd_n_patches.restype = C.c_int64
+            L.or_simd_destroy.argtypes = [C.c_void_p]
+            L.or_num_threads.restype = C.c_int
+            L.or_set_num_threads.argtypes = [C.c_int]
+            _simd = L
+    return _simd
+
+
+class SimdSchwarzHandle:
+    """Additive Schwarz smoother of the reference's CPU path with SIMD macro patches (8 FP64
+    lanes, FMA), the timed CPU baseline; same interface as SchwarzHandle."""
+
+    def __init__(self, dim, k, nc, patch_variant=1, omega=1.0):
+        self.nc3 = _nc3(dim, nc)
+        self.h = simd_lib().or_simd_create(dim, k, self.nc3.ctypes.data_as(_ip), patch_variant, float(omega))
+        assert self.h, "SIMD baseline setup failed"
+
+    @property
+    def n_patches(self):
+        return simd_lib().or_simd_n_patches(self.h)
+
+    def apply(self, dst, src):
+        simd_lib().or_simd_apply(self.h, _d(dst), _d(src))
+
+    def apply_range(self, p0, p1, dst, src):
+        simd_lib().or_simd_apply_range(self.h, int(p0), int(p1), _d(dst), _d(src))
+
+    def close(self):
+        if self.h:
+            simd_lib().or_simd_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def simd_set_num_threads(n):
+    simd_lib().or_set_num_threads(int(n))
+
+
+def simd_num_threads():
+    return simd_lib().or_num_threads()
 
 
 def num_threads():

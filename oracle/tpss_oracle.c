@@ -765,9 +765,11 @@ static void scatter_add_patch(const level_t *L, const patches_t *T, int64_t p, i
   }
 }
 
-/* dst += omega * sum_{p in color} R_p^T A_p^-1 R_p src (weights: optional RAS weights). */
+/* dst += omega * sum_{p in color} R_p^T A_p^-1 R_p src (weights: optional RAS weights; keep:
+ * optional RAS boolean flags, P * nloc). */
 static void apply_color(const level_t *L, const patches_t *T, int color, int ncp, double omega,
-                        const double *weights, const double *src, double *dst)
+                        const double *weights, const unsigned char *keep, const double *src,
+                        double *dst)
 {
   const int64_t b = T->color_start[color], e = T->color_start[color + 1];
   const int dim = L->dim, n = T->n;
@@ -795,12 +797,61 @@ static void apply_color(const level_t *L, const patches_t *T, int color, int ncp
         gather_patch(L, T, p, ncp, weights, w);
         for(int i = 0; i < T->nloc; ++i) u[i] /= w[i];
       }
+      if(keep)
+        for(int i = 0; i < T->nloc; ++i)
+          if(!keep[p * T->nloc + i]) u[i] = 0.0; /* rscatter_add: restricted DoFs are skipped */
       scatter_add_patch(L, T, p, ncp, u, dst);
     }
     free(r);
     free(u);
     free(w);
   }
+}
+
+/* RAS boolean flags (DoFInfo::compute_restricted_dofs_impl, TPSS/dof_info.templates.h:194-313):
+ * of all occurrences (patch p, patch-local index i) of a global DoF only the one with the
+ * smallest (distance to the patch centre, i, p) scatters.  DGQ distance: max over directions of
+ * trunc(|n/2 - 1/2 - m_d|), m_d the patch-local 1-D index.  keep[p * nloc + i] = 1 for the
+ * winners.  Vertex patches of an additive smoother only. */
+static unsigned char *ras_boolean_flags(const level_t *L, const patches_t *T, int ncp)
+{
+  const int dim = L->dim, n = T->n, nloc = T->nloc;
+  int64_t *best_p = (int64_t *)malloc(sizeof(int64_t) * L->n_dofs);
+  int *best_i = (int *)malloc(sizeof(int) * L->n_dofs);
+  int *best_d = (int *)malloc(sizeof(int) * L->n_dofs);
+  for(int64_t g = 0; g < L->n_dofs; ++g) best_p[g] = -1;
+  for(int64_t p = 0; p < T->P; ++p)
+    for(int cn = 0; cn < T->npc; ++cn)
+    {
+      const int64_t f = T->cell_first[p * T->npc + cn];
+      for(int e = 0; e < L->ncell_dofs; ++e)
+      {
+        const int i = patch_index(dim, L->np, ncp, n, cn, e);
+        int dist = 0, rem = i;
+        for(int d = 0; d < dim; ++d, rem /= n)
+        {
+          const double diff = fabs(0.5 * n - 0.5 - (double)(rem % n));
+          const int t = (int)diff;
+          if(t > dist) dist = t;
+        }
+        const int64_t g = f + e;
+        const int better = best_p[g] < 0 || dist < best_d[g] || (dist == best_d[g] && i < best_i[g]) ||
+                           (dist == best_d[g] && i == best_i[g] && p < best_p[g]);
+        if(better)
+        {
+          best_p[g] = p;
+          best_i[g] = i;
+          best_d[g] = dist;
+        }
+      }
+    }
+  unsigned char *keep = (unsigned char *)calloc((size_t)T->P * nloc, 1);
+  for(int64_t g = 0; g < L->n_dofs; ++g)
+    if(best_p[g] >= 0) keep[best_p[g] * nloc + best_i[g]] = 1;
+  free(best_p);
+  free(best_i);
+  free(best_d);
+  return keep;
 }
 
 static void ras_weights(const level_t *L, const patches_t *T, int ncp, double *wgt)
@@ -968,8 +1019,9 @@ typedef struct
   op1d_t O[3];
   int patch_variant, smoother_variant, ncp;
   double omega;
-  int reverse, symmetrized, use_ras;
+  int reverse, symmetrized, use_ras; /* use_ras: 1 RAS weights, 2 RAS boolean weights */
   double *wgt;
+  unsigned char *keep;
 } schwarz_t;
 
 static int schwarz_init(schwarz_t *S, int dim, int k, const int *nc, const double *hx,
@@ -986,10 +1038,15 @@ static int schwarz_init(schwarz_t *S, int dim, int k, const int *nc, const doubl
   S->omega = omega;
   S->reverse = reverse;
   S->symmetrized = symmetrized;
-  S->use_ras = use_ras && smoother_variant == 0;
+  S->use_ras = smoother_variant == 0 ? use_ras : 0;
   if(smoother_variant == 1)
     for(int d = 0; d < dim; ++d) op1d_build(&S->O[d], k, S->L.nc[d], S->L.h[d], ip);
-  if(S->use_ras)
+  if(S->use_ras == 2)
+  {
+    if(patch_variant != 1) return -1; /* the reference: vertex patches only */
+    S->keep = ras_boolean_flags(&S->L, &S->T, S->ncp);
+  }
+  else if(S->use_ras)
   {
     S->wgt = (double *)malloc(sizeof(double) * S->L.n_dofs);
     ras_weights(&S->L, &S->T, S->ncp, S->wgt);
@@ -1003,6 +1060,7 @@ static void schwarz_free(schwarz_t *S)
   if(S->smoother_variant == 1)
     for(int d = 0; d < S->L.dim; ++d) op1d_free(&S->O[d]);
   free(S->wgt);
+  free(S->keep);
 }
 
 /* Color sequence as SchwarzPreconditioner::get_color_sequence (schwarz_preconditioner.h:532-567). */
@@ -1022,18 +1080,18 @@ static void schwarz_vmult(const schwarz_t *S, double *dst, const double *src)
   if(S->smoother_variant == 0)
   {
     for(int c = 0; c < S->T.ncol; ++c)
-      apply_color(&S->L, &S->T, c, S->ncp, S->omega, S->wgt, src, dst);
+      apply_color(&S->L, &S->T, c, S->ncp, S->omega, S->wgt, S->keep, src, dst);
     return;
   }
   int seq[64];
   const int ns = color_sequence(S->T.ncol, S->reverse, S->symmetrized, seq);
   double *res = (double *)malloc(sizeof(double) * N);
-  apply_color(&S->L, &S->T, seq[0], S->ncp, S->omega, NULL, src, dst);
+  apply_color(&S->L, &S->T, seq[0], S->ncp, S->omega, NULL, NULL, src, dst);
   for(int i = 1; i < ns; ++i)
   {
     sipg_apply(&S->L, S->O, dst, res);
     for(int64_t j = 0; j < N; ++j) res[j] = src[j] - res[j];
-    apply_color(&S->L, &S->T, seq[i], S->ncp, S->omega, NULL, res, dst);
+    apply_color(&S->L, &S->T, seq[i], S->ncp, S->omega, NULL, NULL, res, dst);
   }
   free(res);
 }
@@ -1090,7 +1148,7 @@ void or_schwarz_apply_range(void *h, int64_t p_begin, int64_t p_end, double *dst
     int64_t cs[2] = {b, e};
     sub.color_start = cs;
     sub.ncol = 1;
-    apply_color(&S->L, &sub, 0, S->ncp, S->omega, NULL, src, dst);
+    apply_color(&S->L, &sub, 0, S->ncp, S->omega, NULL, NULL, src, dst);
   }
 }
 
@@ -1653,7 +1711,7 @@ int or_schwarz_vmult_surrogate(int dim, int k, const int *nc_in, const double *h
     }
   }
   memset(dst, 0, sizeof(double) * L.n_dofs);
-  for(int c = 0; c < T.ncol; ++c) apply_color(&L, &T, c, 2, omega, NULL, src, dst);
+  for(int c = 0; c < T.ncol; ++c) apply_color(&L, &T, c, 2, omega, NULL, NULL, src, dst);
   patches_free(&T);
   free(hx);
   free(hy);

@@ -89,16 +89,24 @@ def test_cell_dof_start_must_be_a_permutation(tpss):
 
 
 def test_precond_option_errors_before_gpu_work(tpss):
-    """Both RAS options together and RAS boolean weights are rejected as in
-    schwarz_preconditioner.templates.h:599-600 -- before any device memory is touched."""
+    """Both RAS options together are rejected as in schwarz_preconditioner.templates.h:599-600,
+    RAS boolean weights on cell patches ("TODO") and on a multiplicative smoother ("Additive
+    scheme is only supported.") as in dof_info.templates.h:208-212 -- before any device memory
+    is touched."""
     ad = tpss.SubdomainHandler.AdditionalData(dim=2, degree=1, n_cells=(3, 3), patch_variant=1)
     sh = tpss.SubdomainHandler(ad)
     p = tpss.SchwarzPreconditioner()
     with pytest.raises(tpss.TPSSInvalidArgument, match="more than one RAS"):
         p.initialize(sh, None, tpss.SchwarzPreconditioner.AdditionalData(
             use_ras_weights=True, use_ras_boolean_weights=True))
+    shc = tpss.SubdomainHandler(tpss.SubdomainHandler.AdditionalData(dim=2, degree=1, n_cells=(3, 3),
+                                                                      patch_variant=0))
     with pytest.raises(tpss.TPSSNotImplemented):
-        p.initialize(sh, None, tpss.SchwarzPreconditioner.AdditionalData(use_ras_boolean_weights=True))
+        p.initialize(shc, None, tpss.SchwarzPreconditioner.AdditionalData(use_ras_boolean_weights=True))
+    shm = tpss.SubdomainHandler(tpss.SubdomainHandler.AdditionalData(dim=2, degree=1, n_cells=(3, 3),
+                                                                      patch_variant=1, smoother_variant=1))
+    with pytest.raises(tpss.TPSSInvalidArgument, match="Additive"):
+        p.initialize(shm, None, tpss.SchwarzPreconditioner.AdditionalData(use_ras_boolean_weights=True))
     with pytest.raises(tpss.TPSSInvalidArgument, match="relaxation"):
         p.initialize(sh, None, tpss.SchwarzPreconditioner.AdditionalData(relaxation=0.0))
 

@@ -35,8 +35,8 @@ def gpu_vmult(tpss, cuda, dim, k, nc, src, pv=1, sv=0, omega=1.0, ip=1.0, precis
     op = tpss.LaplaceOperator(sh, ip) if sv == 1 else None
     p = tpss.SchwarzPreconditioner()
     p.initialize(sh, op, tpss.SchwarzPreconditioner.AdditionalData(
-        relaxation=omega, precision=precision, ip_factor=ip, use_ras_weights=ras,
-        reverse=reverse, symmetrized=symmetrized))
+        relaxation=omega, precision=precision, ip_factor=ip, use_ras_weights=ras is True,
+        use_ras_boolean_weights=ras == "boolean", reverse=reverse, symmetrized=symmetrized))
     s = torch.tensor(src, dtype=torch.float64, device=cuda)
     d = torch.full_like(s, 123.0)  # vmult must overwrite dst
     p.vmult(d, s)
@@ -90,12 +90,27 @@ def test_nonuniform_h_permuted_cells_ras(tpss, oracle, cuda):
     nd = (k + 1) ** dim
     cell_start = g.permutation(ncell) * nd
     src = philox(7, ncell * nd)
-    for ras in (False, True):
+    for ras in (False, True, "boolean"):
         got, _ = gpu_vmult(tpss, cuda, dim, k, nc, src, pv=1, omega=0.8, h=h, cell_start=cell_start,
                            ras=ras)
         ref = oracle.schwarz_vmult(dim, k, nc, src, patch_variant=1, omega=0.8, h=h,
                                    cell_start=cell_start, use_ras=ras)
         assert rel_err(got, ref) <= 1e-12, ras
+
+
+@pytest.mark.parametrize("dim,k,nc", [(2, 1, (4, 4)), (2, 3, (6, 5)), (2, 5, (2, 3)), (3, 1, (3, 3, 3)),
+                                      (3, 2, (4, 3, 5)), (3, 4, (4, 4, 4)), (3, 6, (2, 3, 2))])
+def test_ras_boolean_weights_parity(tpss, oracle, cuda, dim, k, nc):
+    """Restricted prolongation (rscatter_add): FP64 <= 1e-12, FP32 <= 2e-5 against the oracle;
+    the streamed kernel is not used for it (the per-color kernel skips the restricted DoFs)."""
+    N = int(np.prod(nc)) * (k + 1) ** dim
+    src = philox(300 + k, N)
+    ref = oracle.schwarz_vmult(dim, k, nc, src, patch_variant=1, omega=0.45, use_ras="boolean")
+    plain = oracle.schwarz_vmult(dim, k, nc, src, patch_variant=1, omega=0.45)
+    assert rel_err(plain, ref) > 1e-3  # the restriction changes the result
+    for precision, tol in ((0, 1e-12), (1, 2e-5)):
+        got, _ = gpu_vmult(tpss, cuda, dim, k, nc, src, pv=1, omega=0.45, precision=precision, ras="boolean")
+        assert rel_err(got, ref) <= tol, precision
 
 
 @pytest.mark.parametrize("dim,k,nc,pv,rev,sym", [(2, 3, (5, 4), 1, False, False),

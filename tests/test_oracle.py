@@ -115,6 +115,44 @@ def test_kp1sq_penalty_matches_quadrature(oracle, xcheck, dim, k, nc):
                                atol=1e-12 * np.abs(Aref @ v).max())
 
 
+@pytest.mark.parametrize("dim,k,nc", [(2, 2, [5, 4]), (2, 3, [3, 3]), (3, 1, [3, 4, 3]), (3, 2, [3, 3, 3])])
+def test_ras_boolean_weights_vs_dense_restricted_patch_solves(oracle, xcheck, dim, k, nc):
+    """RAS boolean weights (rscatter_add, compute_restricted_dofs_impl in
+    TPSS/dof_info.templates.h:194-313), restated here with numpy as the reference states it:
+    collect for every global DoF all (distance to the patch centre, patch-local index, patch)
+    occurrences, sort, and let only the first scatter. The restricted prolongations form a
+    partition of unity (every DoF is scattered exactly once)."""
+    A = xcheck.sipg_matrix(dim, k, nc)
+    N = A.shape[0]
+    lowers, _, _ = oracle.patches(dim, nc, 1, 0)
+    n = 2 * (k + 1)
+    occ = {}
+    idxs = []
+    for p, lo in enumerate(lowers):
+        idx = xcheck.patch_dofs(dim, k, nc, lo, 2)
+        idxs.append(idx)
+        for i, g in enumerate(idx):
+            m = [(i // n ** d) % n for d in range(dim)]
+            dist = max(int(abs(n / 2.0 - 0.5 - md)) for md in m)
+            occ.setdefault(int(g), []).append((dist, i, p))
+    keep = [np.zeros(len(ix), dtype=bool) for ix in idxs]
+    for g, lst in occ.items():
+        _, i, p = sorted(lst)[0]
+        keep[p][i] = True
+    count = np.zeros(N)
+    for p, ix in enumerate(idxs):
+        np.add.at(count, ix[keep[p]], 1.0)
+    assert np.all(count == 1.0)
+    src = np.random.default_rng(21).uniform(-1, 1, N)
+    om = 0.6
+    ref = np.zeros(N)
+    for p, ix in enumerate(idxs):
+        u = om * np.linalg.solve(A[np.ix_(ix, ix)], src[ix])
+        ref[ix[keep[p]]] += u[keep[p]]
+    got = oracle.schwarz_vmult(dim, k, nc, src, patch_variant=1, omega=om, use_ras="boolean")
+    assert np.abs(got - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
 @pytest.mark.parametrize("dim,n", [(2, 4), (2, 8), (3, 4), (3, 6)])
 def test_fd_inverse_matches_explicit(oracle, dim, n):
     """Kronecker-sum apply_inverse against the explicit matrix (tensor_product_matrix.cc)."""
@@ -298,3 +336,22 @@ def test_golden_mg_iterations(oracle, xcheck):
                                       patch_variant=c["patch_variant"],
                                       smoother_variant=c["smoother_variant"], rel_tol=c["rel_tol"])
         assert it == c["iterations"]
+
+
+@pytest.mark.parametrize("dim,k,nc,pv", [(2, 3, (6, 5), 1), (2, 2, (5, 3), 0), (3, 2, (4, 3, 5), 1),
+                                         (3, 4, (4, 4, 4), 1), (3, 3, (3, 2, 4), 0), (3, 7, (2, 3, 2), 1)])
+def test_simd_cpu_baseline_matches_oracle(oracle, dim, k, nc, pv):
+    """The timed CPU baseline (oracle/simd_baseline.c: 8-lane macro patches, FMA allowed) is the
+    same smoother as the strict oracle: relative max-norm error <= 1e-12, full vmult and a
+    patch range."""
+    N = int(np.prod(nc)) * (k + 1) ** dim
+    src = np.random.default_rng(17).uniform(-1, 1, N)
+    ref = oracle.schwarz_vmult(dim, k, nc, src, patch_variant=pv, omega=0.41)
+    h = oracle.SimdSchwarzHandle(dim, k, nc, patch_variant=pv, omega=0.41)
+    got = np.full(N, np.nan)
+    h.apply(got, src)
+    assert np.abs(got - ref).max() <= 1e-12 * np.abs(ref).max()
+    part = np.zeros(N)
+    h.apply_range(0, h.n_patches, part, src)
+    assert np.abs(part - ref).max() <= 1e-12 * np.abs(ref).max()
+    h.close()

@@ -32,6 +32,10 @@ bool TPSS_FD_FN(int k, int ncp, const FdLaunch &l, cudaStream_t s)
   a.fd_eo = l.fd_eo;
   a.sym = l.sym;
   a.eo_stride = l.eo_stride;
+  a.rcp = l.rcp;
+  a.rcp_E = l.rcp_E;
+  a.keep_mask = l.keep_mask;
+  a.keep_class = l.keep_class;
   const int sms = num_sms();
 #define TPSS_FD_CASE(NCP, K1) \
   if(ncp == NCP && k + 1 == K1) return fd::launch<FD_T, FD_DIM, NCP, K1>(a, s, sms);

@@ -178,7 +178,9 @@ struct Cfg
   static constexpr size_t OFF_FIRST = al16(OFF_FD + (size_t)PPC * DIM * ESIZE * sizeof(T));
   static constexpr size_t OFF_W = al16(OFF_FIRST + (size_t)PPC * NCELL * 8);
   static constexpr size_t OFF_SYM = al16(OFF_W + (size_t)PPC * NCELL * 4);   // PPC * DIM ints
-  static constexpr size_t OFF_DATA = al16(OFF_SYM + (size_t)PPC * DIM * 4);
+  static constexpr size_t OFF_COMBO = al16(OFF_SYM + (size_t)PPC * DIM * 4);  // PPC ints
+  static constexpr size_t OFF_CLS = al16(OFF_COMBO + (size_t)PPC * 4);   // PPC ints
+  static constexpr size_t OFF_DATA = al16(OFF_CLS + (size_t)PPC * 4);
   static constexpr size_t smem_bytes() { return al16(OFF_DATA + (size_t)PPC * NLOC * sizeof(T)); }
 };
 
@@ -239,10 +241,12 @@ __device__ __forceinline__ void pass(T *__restrict__ data, const T *__restrict__
 }
 
 // last direction: S^T along DIM-1, divide by sum of eigenvalues, S along DIM-1
-// (the eigenvalues of an even/odd entry are in the transformed order its forward pass produces)
+// (the eigenvalues of an even/odd entry are in the transformed order its forward pass produces).
+// rcp (or nullptr): the patch's table of reciprocal eigenvalue sums, n^DIM values with direction
+// 0 fastest; the division becomes a multiplication.
 template<typename T, int DIM, int N, int ES>
 __device__ __forceinline__ void pass_last(T *__restrict__ data, const T *__restrict__ entries,
-                                          const int *sym, int p)
+                                          const int *sym, int p, const T *__restrict__ rcp)
 {
   constexpr int NPAD = Entry<T, N>::NPAD;
   constexpr int DIR = DIM - 1;
@@ -262,9 +266,16 @@ __device__ __forceinline__ void pass_last(T *__restrict__ data, const T *__restr
   }
   else
     rowmat<T, N, NPAD>(eL + Entry<T, N>::ST, r, o);
-  // eigenvalue sum of the other directions (p enumerates i_0 [+ N i_1])
-  T lsum = T(0);
+  if(rcp)
   {
+    // p enumerates i_0 [+ N i_1]; i runs along the last direction
+#pragma unroll
+    for(int i = 0; i < N; ++i) o[i] *= __ldg(rcp + p + i * stride);
+  }
+  else
+  {
+    // eigenvalue sum of the other directions (p enumerates i_0 [+ N i_1])
+    T lsum = T(0);
     int rem = p;
 #pragma unroll
     for(int d = 0; d < DIM - 1; ++d)
@@ -273,10 +284,10 @@ __device__ __forceinline__ void pass_last(T *__restrict__ data, const T *__restr
       lsum += entries[d * ES + lam + rem % N];
       rem /= N;
     }
-  }
-  const T *lamL = eL + (symL ? EoEntry<T, N>::LAM : Entry<T, N>::LAM);
+    const T *lamL = eL + (symL ? EoEntry<T, N>::LAM : Entry<T, N>::LAM);
 #pragma unroll
-  for(int i = 0; i < N; ++i) o[i] = o[i] / (lsum + lamL[i]);
+    for(int i = 0; i < N; ++i) o[i] = o[i] / (lsum + lamL[i]);
+  }
   if constexpr(N % 2 == 0)
   {
     if(symL)
@@ -304,6 +315,10 @@ struct KernelArgs
   const void *__restrict__ fd_eo;     // even/odd forms (nullptr: none)
   const int32_t *__restrict__ sym;    // entry is mirror-symmetric (nullptr: none)
   int eo_stride;                      // elements per even/odd entry
+  const void *__restrict__ rcp;       // reciprocal eigenvalue sums per entry combination (or nullptr)
+  int rcp_E;                          // entries per direction of the combinations
+  const unsigned char *__restrict__ keep_mask;  // RAS boolean: [class][NLOC] 1 = scatter (or nullptr)
+  const int32_t *__restrict__ keep_class;       // RAS boolean: class of each patch of the range
 };
 
 template<typename T, int DIM, int NCP, int K1>
@@ -319,6 +334,9 @@ __global__ void __launch_bounds__(Cfg<T, DIM, NCP, K1>::THREADS)
   float *s_w = reinterpret_cast<float *>(smem_raw + C::OFF_W);          // PPC * NCELL
   T *s_data = reinterpret_cast<T *>(smem_raw + C::OFF_DATA);           // PPC * NLOC
   int *s_sym = reinterpret_cast<int *>(smem_raw + C::OFF_SYM);          // PPC * DIM
+  int *s_combo = reinterpret_cast<int *>(smem_raw + C::OFF_COMBO);      // PPC
+  int *s_cls = reinterpret_cast<int *>(smem_raw + C::OFF_CLS);          // PPC
+  const T *rcp = reinterpret_cast<const T *>(a.rcp);
 
   const T *fd = reinterpret_cast<const T *>(a.fd);
   const T *fd_eo = reinterpret_cast<const T *>(a.fd_eo);
@@ -354,6 +372,14 @@ __global__ void __launch_bounds__(Cfg<T, DIM, NCP, K1>::THREADS)
         if(o == 0) s_sym[sd] = sy;
       }
     }
+    if(rcp && tid < nvalid)
+    {
+      int c = 0;
+#pragma unroll
+      for(int d = DIM - 1; d >= 0; --d) c = c * a.rcp_E + a.patch_fd[(p0 + tid) * DIM + d];
+      s_combo[tid] = c;
+    }
+    if(a.keep_mask && tid < nvalid) s_cls[tid] = a.keep_class[p0 + tid];
     __syncthreads();
     // --- gather: whole cells, coalesced
     for(int i = tid; i < PPC * NCELL * CELLDOFS; i += C::THREADS)
@@ -378,7 +404,8 @@ __global__ void __launch_bounds__(Cfg<T, DIM, NCP, K1>::THREADS)
       __syncthreads();
     }
     // --- last direction fused with the eigenvalue division
-    if(active) pass_last<T, DIM, N, ES>(my, ent, sy, pencil);
+    if(active)
+      pass_last<T, DIM, N, ES>(my, ent, sy, pencil, rcp ? rcp + (size_t)s_combo[slot] * NLOC : nullptr);
     __syncthreads();
     // --- backward S along directions DIM-2..0, damping folded into direction 0
     if constexpr(DIM == 3)
@@ -397,7 +424,10 @@ __global__ void __launch_bounds__(Cfg<T, DIM, NCP, K1>::THREADS)
       if(s < nvalid)
       {
         const int64_t g = s_first[s * NCELL + cn] + e;
-        const double v = double(s_data[s * NLOC + patch_index<DIM, NCP, K1>(cn, e)]);
+        const int pidx = patch_index<DIM, NCP, K1>(cn, e);
+        // RAS boolean weights (rscatter_add): only the patch that owns the DoF adds it
+        if(a.keep_mask && !a.keep_mask[s_cls[s] * NLOC + pidx]) continue;
+        const double v = double(s_data[s * NLOC + pidx]);
         a.dst[g] += a.ras_w ? v * double(s_w[s * NCELL + cn]) : v;
       }
     }

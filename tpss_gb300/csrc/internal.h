@@ -254,6 +254,20 @@ struct FdTables
   DeviceBuffer<double> fd64_eo;  // the same in FP64 (per-color kernel, FP64 smoother)
   DeviceBuffer<int32_t> sym;
   bool has_eo = false;           // some entry has the even/odd form
+  // eigenvalues of every entry in the order the kernels read them (the even/odd order for
+  // mirror-symmetric entries), n_entries x n, host
+  std::vector<double> lam_kernel;
+  // reciprocal eigenvalue sums of keyed entries: for the entry combination c = sum_d e_d E^d
+  // (e_d the entry of direction d, E = n_entries) the n^dim values 1 / (lambda_0 + .. +
+  // lambda_{dim-1}) in the kernels' eigenvalue order; empty when E^dim n^dim > 4 Mi (many
+  // distinct 1-D problems) or for per-patch entries, which keep the division
+  DeviceBuffer<double> rcp64;
+  DeviceBuffer<float> rcp32;
+  int rcp_E = 0;
+  // RAS boolean weights (restricted prolongation, rscatter_add): per patch its boundary class
+  // sum_d (lo_d + 2 hi_d) 4^d, and per class and patch-local DoF 1 when the patch scatters it
+  DeviceBuffer<int32_t> keep_class;
+  DeviceBuffer<unsigned char> keep_mask;
   // per-patch entries (entry p * dim + d) instead of the layout's shared keys
   DeviceBuffer<int32_t> own_fd;
   // exact local inverses (local solver TPSS_LOCAL_EXACT): P x nloc x nloc, transposed
@@ -346,6 +360,10 @@ struct FdLaunch
   const void *fd_eo = nullptr;     // even/odd forms of the mirror-symmetric entries (or nullptr)
   const int32_t *sym = nullptr;    // entry has the even/odd form (or nullptr)
   int eo_stride = 0;               // elements per even/odd entry
+  const void *rcp = nullptr;       // reciprocal eigenvalue sums (FdTables::rcp*) or nullptr
+  int rcp_E = 0;                   // entries per direction of the rcp combinations
+  const unsigned char *keep_mask = nullptr;  // RAS boolean weights (FdTables::keep_mask) or nullptr
+  const int32_t *keep_class = nullptr;       // first patch of the range
 };
 bool launch_fd_f32(int dim, int k, int ncp, const FdLaunch &a, cudaStream_t s);
 bool launch_fd_f64(int dim, int k, int ncp, const FdLaunch &a, cudaStream_t s);

@@ -37,6 +37,7 @@ void build_even_odd(const tpss_layout &L, FdTables &T, const std::vector<double>
                     const std::vector<double> &As, bool keyed)
 {
   const int n = L.n, nn = n * n;
+  T.lam_kernel = T.lam_host;  // mirror-symmetric entries are overwritten below
   std::vector<int32_t> sym(T.n_entries, 0);
   if(keyed && L.ncp == 2 && n % 2 == 0)
     for(int e = 0; e < T.n_entries; ++e)
@@ -101,6 +102,7 @@ void build_even_odd(const tpss_layout &L, FdTables &T, const std::vector<double>
         {
           E[4 * h * hp + par * h + k] = float(lamh[(2 * u + par) * h + k]);
           E64[4 * h * hp64 + par * h + k] = lamh[(2 * u + par) * h + k];
+          T.lam_kernel[(size_t)ids[u] * n + par * h + k] = lamh[(2 * u + par) * h + k];
         }
       }
     }
@@ -109,6 +111,36 @@ void build_even_odd(const tpss_layout &L, FdTables &T, const std::vector<double>
   T.fd64_eo.upload(tab64.data(), tab64.size());
   T.has_eo = !ids.empty();
   T.sym.upload(sym.data(), sym.size());
+}
+
+// 1 / (lambda_0 + .. + lambda_{dim-1}) for every combination of keyed entries, in the order the
+// kernels read the eigenvalues (T.lam_kernel), summed as the kernels sum them (directions
+// 0..dim-2 first, then the last)
+void build_reciprocals(const tpss_layout &L, FdTables &T)
+{
+  const int n = L.n, dim = L.dim, E = T.n_entries;
+  const int64_t nloc = ipow(n, dim), combos = ipow(E, dim);
+  if(E == 0 || combos * nloc > (int64_t(1) << 22)) return;
+  std::vector<double> r64((size_t)(combos * nloc));
+  std::vector<float> r32(r64.size());
+  for(int64_t c = 0; c < combos; ++c)
+  {
+    int e[3] = {0, 0, 0};
+    for(int d = 0, rem = (int)c; d < dim; ++d, rem /= E) e[d] = rem % E;
+    for(int64_t i = 0; i < nloc; ++i)
+    {
+      int id[3] = {0, 0, 0};
+      for(int d = 0, rem = (int)i; d < dim; ++d, rem /= n) id[d] = rem % n;
+      double lsum = 0.0;
+      for(int d = 0; d < dim - 1; ++d) lsum += T.lam_kernel[(size_t)e[d] * n + id[d]];
+      const double sum = lsum + T.lam_kernel[(size_t)e[dim - 1] * n + id[dim - 1]];
+      r64[(size_t)(c * nloc + i)] = 1.0 / sum;
+      r32[(size_t)(c * nloc + i)] = float(1.0 / sum);
+    }
+  }
+  T.rcp64.upload(r64.data(), r64.size());
+  T.rcp32.upload(r32.data(), r32.size());
+  T.rcp_E = E;
 }
 
 }  // namespace
@@ -235,6 +267,7 @@ std::shared_ptr<FdTables> build_tables(const tpss_layout &L, Penalty ip, bool ra
   T->fd64.upload(t64.data(), t64.size());
   T->fd32.upload(t32.data(), t32.size());
   build_even_odd(L, *T, Ms, As, keyed);
+  if(keyed) build_reciprocals(L, *T);
   if(ras)
   {
     // RAS weights: 1 / (number of patches sharing the cell), the gathered "appearances" of
@@ -313,8 +346,78 @@ void validate_desc(const tpss_precond_desc &d)
     TPSS_REQUIRE(d.model != nullptr, "the learned local solver needs a trained model");
   if(d.use_ras_weights && d.use_ras_boolean_weights)
     fail(TPSS_ERR_INVALID_ARGUMENT, "It isn't possible to use more than one RAS option.");
-  if(d.use_ras_boolean_weights)
-    fail(TPSS_ERR_NOT_IMPLEMENTED, "RAS boolean weights (rscatter_add) are not implemented");
+  if(d.local_solver == TPSS_LOCAL_EXACT && d.use_ras_boolean_weights)
+    fail(TPSS_ERR_NOT_IMPLEMENTED, "RAS boolean weights are implemented for the FD local solvers");
+}
+
+// RAS boolean weights need additive vertex patches (DoFInfo::compute_restricted_dofs_impl,
+// TPSS/dof_info.templates.h:194-216)
+void validate_ras_boolean(const tpss_layout &L, const tpss_precond_desc &d)
+{
+  if(!d.use_ras_boolean_weights) return;
+  if(L.patch_variant != TPSS_PATCH_VERTEX)
+    fail(TPSS_ERR_NOT_IMPLEMENTED, "RAS boolean weights: only vertex patches are supported (TODO in the reference)");
+  TPSS_REQUIRE(L.smoother_variant == TPSS_ADDITIVE, "RAS boolean weights: Additive scheme is only supported.");
+}
+
+// Restricted prolongation of the RAS boolean weights. Of the (up to 2^dim) vertex patches that
+// hold a DoF, only the one where the DoF has the smallest (distance to the patch centre,
+// patch-local index) scatters it; the distance is max_d trunc(|n/2 - 1/2 - m_d|) for the
+// patch-local 1-D indices m_d (dof_info.templates.h:233-313). Two patches never give the same
+// (distance, index) pair, so the reference's last tie-break (patch id) never applies, and the
+// choice depends only on which neighbouring patches exist: per patch the class
+// sum_d (lo_d + 2 hi_d) 4^d of its boundary flags (lo_d: no patch below in direction d, hi_d:
+// none above).
+void build_keep_tables(const tpss_layout &L, FdTables &T)
+{
+  if(T.keep_mask.n) return;
+  const int dim = L.dim, n = L.n, K1 = L.np, nloc = L.nloc, ncls = ipow(4, dim);
+  auto dist_of = [&](const int *m) {
+    int dist = 0;
+    for(int d = 0; d < dim; ++d) dist = std::max(dist, (int)std::fabs(0.5 * n - 0.5 - m[d]));
+    return dist;
+  };
+  std::vector<unsigned char> mask((size_t)ncls * nloc, 0);
+  for(int c = 0; c < ncls; ++c)
+    for(int i = 0; i < nloc; ++i)
+    {
+      int m[3] = {0, 0, 0};
+      for(int d = 0, rem = i; d < dim; ++d, rem /= n) m[d] = rem % n;
+      const int own = dist_of(m);
+      bool keep = true;
+      for(int f = 1; f < (1 << dim) && keep; ++f)
+      {
+        int m2[3] = {m[0], m[1], m[2]};
+        bool exists = true;
+        for(int d = 0; d < dim; ++d)
+          if(f >> d & 1)
+          {
+            const bool lower_cell = m[d] < K1;  // the DoF's cell is this patch's lower cell
+            const int flag = (c >> (2 * d + (lower_cell ? 0 : 1))) & 1;
+            exists = exists && !flag;
+            m2[d] = lower_cell ? m[d] + K1 : m[d] - K1;
+          }
+        if(!exists) continue;
+        int i2 = 0;
+        for(int d = dim - 1; d >= 0; --d) i2 = i2 * n + m2[d];
+        const int other = dist_of(m2);
+        if(other < own || (other == own && i2 < i)) keep = false;
+      }
+      mask[(size_t)c * nloc + i] = keep;
+    }
+  std::vector<int32_t> cls(L.P);
+  for(int64_t p = 0; p < L.P; ++p)
+  {
+    int c = 0;
+    for(int d = dim - 1; d >= 0; --d)
+    {
+      const int lo = L.lower[p * 3 + d] == 0, hi = L.lower[p * 3 + d] + 2 == L.nc[d];
+      c = c * 4 + lo + 2 * hi;
+    }
+    cls[p] = c;
+  }
+  T.keep_class.upload(cls.data(), cls.size());
+  T.keep_mask.upload(mask.data(), mask.size());
 }
 
 cudaEvent_t get_event(tpss_precond *p)
@@ -428,6 +531,11 @@ void apply_color(tpss_precond *p, int color, double *dst, const double *src, cud
   a.patch_fd = (p->tables->own_fd.n ? p->tables->own_fd.ptr : L.d_patch_fd.ptr) + b * L.dim;
   const bool ras = p->desc.use_ras_weights && L.smoother_variant == TPSS_ADDITIVE;
   a.ras_w = ras ? p->tables->ras_w.ptr + b * L.npc : nullptr;
+  if(p->desc.use_ras_boolean_weights)
+  {
+    a.keep_mask = p->tables->keep_mask.ptr;
+    a.keep_class = p->tables->keep_class.ptr + b;
+  }
   a.n_patches = e - b;
   a.omega = p->desc.relaxation;
   bool ok;
@@ -436,8 +544,12 @@ void apply_color(tpss_precond *p, int color, double *dst, const double *src, cud
   const bool eo = p->tables->has_eo && !p->tables->own_fd.n;
   const int h = L.n / 2;
   a.sym = eo ? p->tables->sym.ptr : nullptr;
+  // reciprocal eigenvalue sums (keyed tables of few distinct 1-D problems)
+  const bool rcp = p->tables->rcp_E > 0 && !p->tables->own_fd.n;
+  a.rcp_E = p->tables->rcp_E;
   if(p->desc.precision == TPSS_FP32)
   {
+    a.rcp = rcp ? (const void *)p->tables->rcp32.ptr : nullptr;
     a.fd = p->tables->fd32.ptr;
     a.entry_stride = (2 * L.n + 1) * p->tables->npad32;
     a.fd_eo = eo ? (const void *)p->tables->fd32_eo.ptr : nullptr;
@@ -446,6 +558,7 @@ void apply_color(tpss_precond *p, int color, double *dst, const double *src, cud
   }
   else
   {
+    a.rcp = rcp ? (const void *)p->tables->rcp64.ptr : nullptr;
     a.fd = p->tables->fd64.ptr;
     a.entry_stride = (2 * L.n + 1) * p->tables->npad64;
     a.fd_eo = eo ? (const void *)p->tables->fd64_eo.ptr : nullptr;
@@ -481,7 +594,8 @@ bool stream_eligible(const tpss_precond *p)
 {
   const tpss_layout &L = *p->tables->layout;
   return L.smoother_variant == TPSS_ADDITIVE && p->desc.precision == TPSS_FP32 &&
-         stream_supported(L) && !p->tables->dense && p->tables->own_fd.n == 0;
+         stream_supported(L) && !p->tables->dense && p->tables->own_fd.n == 0 &&
+         !p->desc.use_ras_boolean_weights;
 }
 
 bool use_stream(const tpss_precond *p)
@@ -589,6 +703,7 @@ extern "C" int tpss_precond_create(const tpss_layout *layout, tpss_operator *op,
     TPSS_REQUIRE(layout && desc && out, "null argument");
     *out = nullptr;
     validate_desc(*desc);
+    validate_ras_boolean(*layout, *desc);
     if(layout->smoother_variant == TPSS_MULTIPLICATIVE)
     {
       TPSS_REQUIRE(op, "the multiplicative smoother needs the level operator");
@@ -600,6 +715,7 @@ extern "C" int tpss_precond_create(const tpss_layout *layout, tpss_operator *op,
     p->op = op;
     p->stream_variant = desc->stream_variant;
     p->tables = build_local_solvers(*layout, op, *desc);
+    if(desc->use_ras_boolean_weights) build_keep_tables(*layout, *p->tables);
     p->timers.resize(5);
     for(int i = 0; i < 5; ++i) p->timers[i].name = kTimerNames[i];
     p->timers[2].time = p->tables->setup_seconds;
@@ -630,6 +746,8 @@ extern "C" int tpss_precond_create_shallow(const tpss_precond *other, const tpss
     p->tables = other->tables;
     if(desc->use_ras_weights && p->tables->ras_w.n == 0)
       fail(TPSS_ERR_INVALID_ARGUMENT, "shallow copy cannot add RAS weights");
+    validate_ras_boolean(*p->tables->layout, *desc);
+    if(desc->use_ras_boolean_weights) build_keep_tables(*p->tables->layout, *p->tables);
     p->timers = other->timers;
     *out = p.release();
   });
