@@ -381,6 +381,8 @@ def run_ours(args):
 
     if not args.no_e2e:
         out["e2e"] = e2e(tpss, p, src_h, args, W, world, dist)
+    if prec == tpss.Precision.fp32:
+        out["fp64"] = fp64_arm(tpss, sh, src, src_h, args, W, world, dist)
     if not args.no_solve:
         out["operator"] = operator_time(tpss, sh, src, W)
         out["solve"] = solve_times(tpss, args)
@@ -440,6 +442,55 @@ def e2e(tpss, p, src_h, args, W, world, dist):
         ms = float(t.item())
     return {"value": world * N / (ms * 1e-3), "unit": "DoF/s", "h2d_bytes_per_step": N * 8,
             "d2h_bytes_per_step": N * 8, "ms_per_step": ms, "steps": steps}
+
+
+def executed_fd_flops(n, k, dim):
+    """Floating-point operations the FD kernels execute per vmult on the Cartesian n^dim level:
+    per patch and direction a forward and a backward pass over n1^(dim-1) pencils, 2 h^2
+    multiply-adds plus n1 additions per pencil where the 1-D problem is mirror-symmetric (the
+    even/odd split, h = n1/2: interior vertices), n1^2 multiply-adds elsewhere; one
+    reciprocal multiplication per patch DoF and one damping multiplication."""
+    n1, h = 2 * (k + 1), k + 1
+    pencils = n1 ** (dim - 1)
+    sym_frac = max(0, n - 3) / max(1, n - 1)  # vertex positions 2..n-2 of 1..n-1 per direction
+    per_dir = 2 * pencils * (sym_frac * (2 * 2 * h * h + n1) + (1 - sym_frac) * 2 * n1 * n1)
+    return (n - 1) ** dim * (dim * per_dir + 2 * n1 ** dim)
+
+
+def fp64_arm(tpss, sh, src, src_h, args, W, world, dist):
+    """The FP64 smoother on the same level (the precision of the reference's arithmetic): device
+    DoF/s, e2e through tpss_precond_vmult_host (copy in, vmult, copy out), and the roofline of the
+    FP64 pipe that binds it (executed operations / measured FP64 FMA peak)."""
+    import torch
+    p = tpss.SchwarzPreconditioner()
+    p.initialize(sh, None, tpss.SchwarzPreconditioner.AdditionalData(relaxation=args.omega,
+                                                                     precision=tpss.Precision.fp64))
+    dst = torch.empty_like(src)
+    chosen, tuned_ms = p.autotune(dst, src, reps=2)
+    for _ in range(3):
+        p.vmult(dst, src)
+    torch.cuda.synchronize()
+    steps = 10
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        p.vmult(dst, src)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    ex = executed_fd_flops(args.cells, args.degree, args.dim)
+    peak = tpss_fma_peak(tpss, tpss.Precision.fp64)
+    ee = e2e(tpss, p, src_h, argparse.Namespace(steps=5), W, world, dist)
+    return {"value": world * W["N"] / (ms * 1e-3), "unit": "DoF/s", "ms_per_step": ms, "steps": steps,
+            "kernel": f"schwarz_color_kernel<double,3,2,{args.degree + 1}> x {sh.n_colors()} colors",
+            "autotuned_variant": chosen, "autotune_ms_per_variant": tuned_ms,
+            "e2e": ee,
+            "roofline": {"bound": "fp64 pipe", "achieved": ex / (ms * 1e-3) / 1e12, "peak": peak / 1e12,
+                         "unit": "TFLOP/s", "frac": ex / (ms * 1e-3) / peak,
+                         "peak_source": "measured in this run (tpss_diag_fma_peak, FP64)",
+                         "executed_flops_per_vmult": ex,
+                         "algorithmic_dense_flops_per_vmult": W["flops"],
+                         "hbm_frac": W["bytes"] / (ms * 1e-3) / 1e9 / measured_peaks()[0]}}
 
 
 def operator_time(tpss, sh, src, W):
@@ -685,18 +736,16 @@ def c0ip_section(tpss, args):
 
 def batch_section(tpss, args):
     """Many independent Poisson SIPG problems (dimension 2/3, degree 2..7 and mesh 8^d..64^d drawn
-    from the seed; one root cell, dense coarse solve, V-cycles in CUDA graphs, FP32 smoothers, FP64
-    CG) solved in lockstep, against solving them one after the other."""
+    from the seed; a draw beyond the per-problem or the total DoF cap is rejected and drawn again;
+    one root cell, dense coarse solve, V-cycles in CUDA graphs, kernel decompositions chosen by the
+    autotuner per level shape, FP32 smoothers, FP64 CG) solved in lockstep, against solving them
+    one after the other."""
     import numpy as np
     import torch
-    rng = np.random.Generator(np.random.Philox(args.seed + 4))
-    problems = []
-    for _ in range(args.batch_problems):
-        dim = int(rng.integers(2, 4))
-        k = int(rng.integers(2, 8))
-        cells = [8, 16, 32, 64] if dim == 2 else ([8, 16] if k <= 4 else [8])
-        n = int(rng.choice(cells))
-        problems.append(dict(dim=dim, degree=k, n_rep=1, n_cells_fine=n, precision=tpss.Precision.fp32))
+    cap_total, cap_problem = 96_000_000, 8_000_000
+    problems, rejected = tpss.draw_batch_problems(args.batch_problems, args.seed + 4, cap_total, cap_problem)
+    for pr in problems:
+        pr["precision"] = tpss.Precision.fp32
     t0 = time.perf_counter()
     b = tpss.BatchSolver(problems, n_streams=16)
     fs = [torch.tensor(philox_src(n, args.seed + i), dtype=torch.float64, device="cuda")
@@ -726,9 +775,13 @@ def batch_section(tpss, args):
     torch.cuda.synchronize()
     t_seq = time.perf_counter() - t0
     total = int(sum(b.n_dofs))
+    shapes = sorted({(p["dim"], p["degree"], p["n_cells_fine"]) for p in problems})
     return {"workload": f"{len(problems)} independent 2D/3D SIPG Poisson problems, DGQ2..7, 8^d..64^d cells, "
                         f"{total} DoFs in total, CG + V-cycle to 1e-8 each, FP32 smoothers",
             "problems": len(problems), "total_dofs": total,
+            "draw": {"seed": args.seed + 4, "max_dofs_total": cap_total, "max_dofs_problem": cap_problem,
+                     "rejected_draws": rejected, "distinct_shapes": len(shapes),
+                     "largest": max(shapes, key=lambda s: (s[2] * (s[1] + 1)) ** s[0])},
             "lockstep_seconds": t_batch, "sequential_seconds": t_seq,
             "dofs_solved_per_s": total / t_batch, "lockstep_speedup": t_seq / t_batch,
             "iterations_mean": float(np.mean(its)), "iterations_max": int(np.max(its)),

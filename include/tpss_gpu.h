@@ -157,8 +157,10 @@ typedef struct tpss_precond_desc
   int kernel_variant;          /* additive smoother kernel: TPSS_KERNEL_AUTO, TPSS_KERNEL_COLOR
                                   (one fused launch per color) or TPSS_KERNEL_STREAM (3D vertex
                                   patches, FP32, k <= 4: column-streamed, one pass) */
-  int stream_variant;          /* initial work decomposition of the column-streamed kernel
-                                  (0..5, see tpss_precond_autotune); 0 by default */
+  int stream_variant;          /* initial work decomposition of the smoother kernel (see
+                                  tpss_precond_autotune): 0..5 for the column-streamed kernel,
+                                  0..2 (patches per CTA x1, x2, x4) for the per-color kernel, which
+                                  uses 0 where the level offers fewer; 0 by default */
   int local_solver;            /* TPSS_LOCAL_*: how the patch inverses are formed */
   const tpss_mlp *model;       /* trained network for TPSS_LOCAL_LEARNED, else NULL */
   int penalty_mode;            /* TPSS_PENALTY_* of the local SIPG matrices (0: the reference) */
@@ -224,8 +226,10 @@ int tpss_precond_vmult_static_scratch(tpss_precond *p, double *dst, const double
 
 /* Autotuner (no counterpart in the reference): times every work decomposition of the smoother
  * kernel for this level (for the column-streamed kernel: pencils per thread and vertex layers per
- * work item) on the caller's vectors, `reps` applications each, and keeps the fastest for later
- * vmult calls.  On return dst = P src, *chosen is the selected variant, ms_per_variant (optional,
+ * work item; for the per-color kernel, which serves 2D, cell patches, FP64, k > 4 and the
+ * multiplicative smoother: 1, 2 or 4 times its base number of patches per CTA, as far as 512
+ * threads and 200 KB of shared memory allow) on the caller's vectors, `reps` applications each,
+ * and keeps the fastest for later vmult calls.  On return dst = P src, *chosen is the selected variant, ms_per_variant (optional,
  * >= 6 entries) the measured milliseconds per application and *n_variants their count (1 when the
  * level has a single kernel). */
 /* vmult with dst and src in HOST memory (the reference's vmult on host vectors; a device-vector
@@ -304,6 +308,10 @@ typedef struct tpss_mg_desc
                                   operator and the coarse solve stay FP64 (no counterpart in the
                                   reference, whose multigrid runs in the vector precision) */
   int penalty_mode;            /* TPSS_PENALTY_* of every level's operator and local solvers */
+  int autotune;                /* 1: every level's smoother kernel decomposition is chosen by the
+                                  autotuner (tpss_precond_autotune) at setup; levels of a shape
+                                  tuned before in this process (e.g. in another problem of a
+                                  batch) reuse that choice (no counterpart in the reference) */
 } tpss_mg_desc;
 
 int tpss_mg_create(const tpss_mg_desc *desc, tpss_mg **out);

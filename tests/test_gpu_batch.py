@@ -1,4 +1,5 @@
-"""Batched lockstep solves give each problem's own CG + GMG result (same kernels, same order)."""
+"""Batched lockstep solves: each problem gets its own CG + GMG result (same kernels, same order),
+and a seeded sample of the benchmark family matches the CPU oracle's iteration counts."""
 import numpy as np
 import pytest
 
@@ -27,3 +28,34 @@ def test_batch_equals_individual_solves(tpss, cuda):
         it1, _ = mg.solve(v, f)
         assert it == it1
         assert torch.equal(u, v)
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_batch_sample_matches_oracle_iterations(tpss, oracle, cuda, precision):
+    """A seeded sample of the batched problem family (drawn by tpss.draw_batch_problems, the
+    rule of the 512-problem benchmark, with caps the CPU oracle finishes in seconds), solved in
+    lockstep with autotuned kernels and the dense coarse solve the batch needs: FP64 smoothers
+    give the oracle's CG + GMG iteration count (the oracle's coarse solver is CG to 1e-12, so
+    one iteration more or less is accepted where the oracle's residual at the smaller count lies
+    within 25 % of the tolerance); FP32 smoothers stay within one iteration of it."""
+    import torch
+    problems, _ = tpss.draw_batch_problems(10, 2024, 600_000, 80_000)
+    for pr in problems:
+        pr["precision"] = precision
+        pr["autotune"] = 1
+    b = tpss.BatchSolver(problems, n_streams=4)
+    fs_h = [philox(100 + i, n) for i, n in enumerate(b.n_dofs)]
+    fs = [torch.tensor(f, dtype=torch.float64, device=cuda) for f in fs_h]
+    us = [torch.empty_like(f) for f in fs]
+    its = b.solve(us, fs)
+    for pr, f, it in zip(problems, fs_h, its):
+        it_ref, _, hist = oracle.mg_cg_solve(pr["dim"], pr["degree"], 1, pr["n_cells_fine"], f, rel_tol=1e-8)
+        assert it_ref > 0
+        assert abs(it - it_ref) <= 1, (pr, it, it_ref)
+        if precision == 0 and it != it_ref:
+            assert hist[min(it, it_ref)] / hist[0] <= 1.25e-8, (pr, it, it_ref)
+
+
+def test_batch_rejects_coarse_cg(tpss, cuda):
+    with pytest.raises(tpss.TPSSInvalidArgument, match="dense coarse"):
+        tpss.BatchSolver([dict(dim=2, degree=2, n_rep=1, n_cells_fine=8, coarse_solver=0)])

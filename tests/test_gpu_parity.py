@@ -515,6 +515,41 @@ def test_streamed_variants_and_autotune(tpss, oracle, cuda, k, nc):
     assert rel_err(d2.cpu().numpy(), ref) <= 2e-5
 
 
+@pytest.mark.parametrize("dim,k,nc,pv,sv,precision", [
+    (2, 3, (9, 7), 1, 0, 0), (2, 1, (8, 9), 1, 0, 1), (2, 6, (4, 5), 0, 0, 0), (3, 4, (5, 4, 6), 1, 0, 0),
+    (3, 2, (5, 5, 4), 0, 0, 1), (3, 6, (3, 3, 2), 1, 0, 1), (2, 4, (5, 4), 1, 1, 0), (3, 1, (3, 4, 3), 0, 1, 0)])
+def test_color_kernel_variants_and_autotune(tpss, oracle, cuda, dim, k, nc, pv, sv, precision):
+    """Every patches-per-CTA decomposition of the per-color kernel (2D, cell patches, FP64,
+    k > 4, multiplicative) gives the oracle's result (FP64 1e-12, FP32 2e-5); the autotuner times
+    them, keeps one and leaves dst = P src."""
+    import torch
+    N = int(np.prod(nc)) * (k + 1) ** dim
+    src = philox(500 + k, N)
+    om = 0.3 if sv == 0 else 1.0
+    ref = oracle.schwarz_vmult(dim, k, nc, src, patch_variant=pv, smoother_variant=sv, omega=om)
+    tol = 1e-12 if precision == 0 else 2e-5
+    ad = tpss.SubdomainHandler.AdditionalData(dim=dim, degree=k, n_cells=nc, patch_variant=pv,
+                                              smoother_variant=sv)
+    sh = tpss.SubdomainHandler(ad)
+    op = tpss.LaplaceOperator(sh) if sv == 1 else None
+    s = torch.tensor(src, dtype=torch.float64, device=cuda)
+    for v in range(3):
+        p = tpss.SchwarzPreconditioner()
+        p.initialize(sh, op, tpss.SchwarzPreconditioner.AdditionalData(
+            relaxation=om, precision=precision, kernel_variant=1, stream_variant=v))
+        d = torch.full_like(s, float("nan"))
+        p.vmult(d, s)
+        assert rel_err(d.cpu().numpy(), ref) <= tol, v
+    d = torch.full_like(s, float("nan"))
+    chosen, ms = p.autotune(d, s, reps=2)
+    assert 1 <= len(ms) <= 3 and 0 <= chosen < len(ms)
+    if len(ms) > 1:
+        assert all(t > 0 for t in ms)
+    assert rel_err(d.cpu().numpy(), ref) <= tol
+    if dim == 2 or k <= 4:
+        assert len(ms) >= 2, "small patches offer at least two decompositions"
+
+
 @pytest.mark.parametrize("k,nc,variant", [(4, (9, 6, 19), 0), (3, (7, 5, 33), 2), (2, (6, 6, 17), 3), (1, (5, 9, 40), 1),
                                          (4, (10, 7, 21), 4), (3, (6, 9, 18), 5)])
 def test_vmult_host_buffers_pipelined(tpss, oracle, cuda, k, nc, variant):

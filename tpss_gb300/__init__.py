@@ -499,6 +499,8 @@ class BatchSolver:
             d.coarse_tol = float(pr.get("coarse_tol", 1e-12))
             d.coarse_solver = int(pr.get("coarse_solver", 1))
             d.use_graph = int(pr.get("use_graph", 1))
+            d.autotune = int(pr.get("autotune", 1))  # kernel decompositions chosen per level shape
+            d.penalty_mode = int(pr.get("penalty_mode", Penalty.reference))
         h = C.c_void_p()
         check(load().tpss_batch_create(arr, len(problems), int(n_streams), C.byref(h)))
         self._h = h
@@ -523,6 +525,31 @@ class BatchSolver:
                 self._h = None
         except Exception:
             pass
+
+
+def draw_batch_problems(count, seed, max_dofs_total, max_dofs_problem, dims=(2, 3), degrees=(2, 7),
+                        cells=(8, 16, 32, 64)):
+    """Seeded draw of independent Poisson problems for BatchSolver: dimension, degree k in
+    [degrees[0], degrees[1]] and cells per direction uniformly from `cells` (one root cell).
+    A draw is rejected and drawn again when its DoFs exceed max_dofs_problem, or when it would
+    leave less of the budget max_dofs_total than the smallest problem needs for every problem
+    still to be drawn. Returns (problems, rejected draws)."""
+    rng = np.random.Generator(np.random.Philox(seed))
+    n_min = min((n * (k + 1)) ** d for d in dims for k in range(degrees[0], degrees[1] + 1) for n in cells)
+    if count * n_min > max_dofs_total:
+        raise ValueError("max_dofs_total is below count times the smallest problem")
+    problems, rejected, total = [], 0, 0
+    while len(problems) < count:
+        dim = int(rng.choice(dims))
+        k = int(rng.integers(degrees[0], degrees[1] + 1))
+        n = int(rng.choice(cells))
+        N = (n * (k + 1)) ** dim
+        if N > max_dofs_problem or total + N + (count - len(problems) - 1) * n_min > max_dofs_total:
+            rejected += 1
+            continue
+        total += N
+        problems.append(dict(dim=dim, degree=k, n_rep=1, n_cells_fine=n))
+    return problems, rejected
 
 
 class LocalSolver:
@@ -642,7 +669,7 @@ class MultigridSolver:
                  precision=Precision.fp64, coarse_tol=1e-12, coarse_solver=0, use_graph=True,
                  vertex_coords=None, surrogate_n_q=5, local_solver=0, model=None,
                  auto_relaxation=False, vcycle_precision=Precision.fp64,
-                 penalty_mode=Penalty.reference):
+                 penalty_mode=Penalty.reference, autotune=False):
         if relaxation is None:
             relaxation = lookup_damping_factor(patch_variant, smoother_variant, dim)
         d = _lib.MgDesc()
@@ -656,6 +683,7 @@ class MultigridSolver:
         d.auto_relaxation = int(auto_relaxation)
         d.vcycle_precision = int(vcycle_precision)
         d.penalty_mode = int(penalty_mode)
+        d.autotune = int(autotune)
         self._model = model
         d.dim, d.degree, d.n_rep, d.n_cells_fine = dim, degree, n_rep, n_cells_fine
         d.ip_factor, d.patch_variant, d.smoother_variant = float(ip_factor), patch_variant, smoother_variant

@@ -38,12 +38,25 @@ bool TPSS_FD_FN(int k, int ncp, const FdLaunch &l, cudaStream_t s)
   a.keep_class = l.keep_class;
   const int sms = num_sms();
 #define TPSS_FD_CASE(NCP, K1) \
-  if(ncp == NCP && k + 1 == K1) return fd::launch<FD_T, FD_DIM, NCP, K1>(a, s, sms);
+  if(ncp == NCP && k + 1 == K1) return fd::launch<FD_T, FD_DIM, NCP, K1>(a, s, sms, l.variant);
   TPSS_FD_CASE(1, 2) TPSS_FD_CASE(1, 3) TPSS_FD_CASE(1, 4) TPSS_FD_CASE(1, 5)
   TPSS_FD_CASE(1, 6) TPSS_FD_CASE(1, 7) TPSS_FD_CASE(1, 8)
   TPSS_FD_CASE(2, 2) TPSS_FD_CASE(2, 3) TPSS_FD_CASE(2, 4) TPSS_FD_CASE(2, 5)
   TPSS_FD_CASE(2, 6) TPSS_FD_CASE(2, 7) TPSS_FD_CASE(2, 8)
 #undef TPSS_FD_CASE
   return false;
+}
+
+// work decompositions (patches per CTA) the kernel of (k, ncp) offers to the autotuner
+int TPSS_CAT(TPSS_CAT(fd_variants_, FD_T), TPSS_CAT(_, FD_DIM))(int k, int ncp)
+{
+#define TPSS_FD_CASE(NCP, K1) \
+  if(ncp == NCP && k + 1 == K1) return fd::Cfg<FD_T, FD_DIM, NCP, K1>::n_variants();
+  TPSS_FD_CASE(1, 2) TPSS_FD_CASE(1, 3) TPSS_FD_CASE(1, 4) TPSS_FD_CASE(1, 5)
+  TPSS_FD_CASE(1, 6) TPSS_FD_CASE(1, 7) TPSS_FD_CASE(1, 8)
+  TPSS_FD_CASE(2, 2) TPSS_FD_CASE(2, 3) TPSS_FD_CASE(2, 4) TPSS_FD_CASE(2, 5)
+  TPSS_FD_CASE(2, 6) TPSS_FD_CASE(2, 7) TPSS_FD_CASE(2, 8)
+#undef TPSS_FD_CASE
+  return 1;
 }
 }  // namespace tpss

@@ -171,17 +171,36 @@ struct Cfg
   static constexpr int SLOT_BYTES = NLOC * sizeof(T) + DIM * ESIZE * sizeof(T) + NCELL * 12;
   static constexpr int PPC_MEM = (96 * 1024) / SLOT_BYTES > 0 ? (96 * 1024) / SLOT_BYTES : 1;
   static constexpr int PPC = PPC_WANT < PPC_MEM ? PPC_WANT : PPC_MEM;
-  static constexpr int THREADS = ((PPC * NPENCIL + 31) / 32) * 32 < 64 ? 64 : ((PPC * NPENCIL + 31) / 32) * 32;
-  // shared memory carve-up (byte offsets, each 16-byte aligned)
+  // Work decompositions for the autotuner: variant v holds ppc(v) = PPC << v patches per CTA
+  // (more patches per CTA: fewer, larger blocks and more pencils per barrier); a variant is
+  // offered when it fits MAX_THREADS threads and MAX_SMEM bytes of shared memory.
+  static constexpr int MAX_THREADS = 512, MAX_SMEM = 200 * 1024, MAX_VARIANTS = 3;
+  static constexpr int ppc(int v) { return PPC << v; }
+  static constexpr int threads(int ppc_) { return ((ppc_ * NPENCIL + 31) / 32) * 32 < 64 ? 64 : ((ppc_ * NPENCIL + 31) / 32) * 32; }
+  // shared memory carve-up for ppc_ patches per CTA (byte offsets, each 16-byte aligned)
   static constexpr size_t al16(size_t x) { return (x + 15) / 16 * 16; }
-  static constexpr size_t OFF_FD = 0;
-  static constexpr size_t OFF_FIRST = al16(OFF_FD + (size_t)PPC * DIM * ESIZE * sizeof(T));
-  static constexpr size_t OFF_W = al16(OFF_FIRST + (size_t)PPC * NCELL * 8);
-  static constexpr size_t OFF_SYM = al16(OFF_W + (size_t)PPC * NCELL * 4);   // PPC * DIM ints
-  static constexpr size_t OFF_COMBO = al16(OFF_SYM + (size_t)PPC * DIM * 4);  // PPC ints
-  static constexpr size_t OFF_CLS = al16(OFF_COMBO + (size_t)PPC * 4);   // PPC ints
-  static constexpr size_t OFF_DATA = al16(OFF_CLS + (size_t)PPC * 4);
-  static constexpr size_t smem_bytes() { return al16(OFF_DATA + (size_t)PPC * NLOC * sizeof(T)); }
+  struct Lay
+  {
+    size_t fd, first, w, sym, combo, cls, data, bytes;
+  };
+  static constexpr Lay lay(int ppc_)
+  {
+    Lay l{};
+    l.fd = 0;
+    l.first = al16(l.fd + (size_t)ppc_ * DIM * ESIZE * sizeof(T));
+    l.w = al16(l.first + (size_t)ppc_ * NCELL * 8);
+    l.sym = al16(l.w + (size_t)ppc_ * NCELL * 4);      // ppc * DIM ints
+    l.combo = al16(l.sym + (size_t)ppc_ * DIM * 4);     // ppc ints
+    l.cls = al16(l.combo + (size_t)ppc_ * 4);           // ppc ints
+    l.data = al16(l.cls + (size_t)ppc_ * 4);
+    l.bytes = al16(l.data + (size_t)ppc_ * NLOC * sizeof(T));
+    return l;
+  }
+  static constexpr bool variant_ok(int v)
+  {
+    return v >= 0 && v < MAX_VARIANTS && threads(ppc(v)) <= MAX_THREADS && lay(ppc(v)).bytes <= (size_t)MAX_SMEM;
+  }
+  static constexpr int n_variants() { return variant_ok(2) ? 3 : variant_ok(1) ? 2 : 1; }
 };
 
 // patch-local index of DoF e of patch cell cn
@@ -319,23 +338,26 @@ struct KernelArgs
   int rcp_E;                          // entries per direction of the combinations
   const unsigned char *__restrict__ keep_mask;  // RAS boolean: [class][NLOC] 1 = scatter (or nullptr)
   const int32_t *__restrict__ keep_class;       // RAS boolean: class of each patch of the range
+  int ppc;                                      // patches per CTA (Cfg::ppc of the variant)
 };
 
 template<typename T, int DIM, int NCP, int K1>
-__global__ void __launch_bounds__(Cfg<T, DIM, NCP, K1>::THREADS)
+__global__ void __launch_bounds__(Cfg<T, DIM, NCP, K1>::MAX_THREADS)
   schwarz_color_kernel(KernelArgs a)
 {
   using C = Cfg<T, DIM, NCP, K1>;
-  constexpr int N = C::N, NLOC = C::NLOC, PPC = C::PPC, NCELL = C::NCELL;
+  constexpr int N = C::N, NLOC = C::NLOC, NCELL = C::NCELL;
   constexpr int CELLDOFS = C::CELLDOFS, ES = C::ESIZE;
+  const int PPC = a.ppc, NTHR = blockDim.x;
+  const typename C::Lay lay = C::lay(PPC);
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  T *s_fd = reinterpret_cast<T *>(smem_raw + C::OFF_FD);             // PPC * DIM * ES
-  int64_t *s_first = reinterpret_cast<int64_t *>(smem_raw + C::OFF_FIRST);  // PPC * NCELL
-  float *s_w = reinterpret_cast<float *>(smem_raw + C::OFF_W);          // PPC * NCELL
-  T *s_data = reinterpret_cast<T *>(smem_raw + C::OFF_DATA);           // PPC * NLOC
-  int *s_sym = reinterpret_cast<int *>(smem_raw + C::OFF_SYM);          // PPC * DIM
-  int *s_combo = reinterpret_cast<int *>(smem_raw + C::OFF_COMBO);      // PPC
-  int *s_cls = reinterpret_cast<int *>(smem_raw + C::OFF_CLS);          // PPC
+  T *s_fd = reinterpret_cast<T *>(smem_raw + lay.fd);                 // PPC * DIM * ES
+  int64_t *s_first = reinterpret_cast<int64_t *>(smem_raw + lay.first);  // PPC * NCELL
+  float *s_w = reinterpret_cast<float *>(smem_raw + lay.w);             // PPC * NCELL
+  T *s_data = reinterpret_cast<T *>(smem_raw + lay.data);              // PPC * NLOC
+  int *s_sym = reinterpret_cast<int *>(smem_raw + lay.sym);             // PPC * DIM
+  int *s_combo = reinterpret_cast<int *>(smem_raw + lay.combo);         // PPC
+  int *s_cls = reinterpret_cast<int *>(smem_raw + lay.cls);             // PPC
   const T *rcp = reinterpret_cast<const T *>(a.rcp);
 
   const T *fd = reinterpret_cast<const T *>(a.fd);
@@ -349,7 +371,7 @@ __global__ void __launch_bounds__(Cfg<T, DIM, NCP, K1>::THREADS)
     const int64_t left = a.n_patches - p0;
     const int nvalid = left < PPC ? (int)left : PPC;
     // --- patch metadata and the 1-D eigenbases
-    for(int i = tid; i < PPC * NCELL; i += C::THREADS)
+    for(int i = tid; i < PPC * NCELL; i += NTHR)
     {
       const int s = i / NCELL;
       if(s < nvalid)
@@ -358,7 +380,7 @@ __global__ void __launch_bounds__(Cfg<T, DIM, NCP, K1>::THREADS)
         s_w[i] = a.ras_w ? a.ras_w[p0 * NCELL + i] : 1.0f;
       }
     }
-    for(int i = tid; i < PPC * DIM * ES; i += C::THREADS)
+    for(int i = tid; i < PPC * DIM * ES; i += NTHR)
     {
       const int sd = i / ES, s = sd / DIM, o = i % ES;
       if(s < nvalid)
@@ -382,7 +404,7 @@ __global__ void __launch_bounds__(Cfg<T, DIM, NCP, K1>::THREADS)
     if(a.keep_mask && tid < nvalid) s_cls[tid] = a.keep_class[p0 + tid];
     __syncthreads();
     // --- gather: whole cells, coalesced
-    for(int i = tid; i < PPC * NCELL * CELLDOFS; i += C::THREADS)
+    for(int i = tid; i < PPC * NCELL * CELLDOFS; i += NTHR)
     {
       const int s = i / (NCELL * CELLDOFS);
       const int rem = i % (NCELL * CELLDOFS);
@@ -416,7 +438,7 @@ __global__ void __launch_bounds__(Cfg<T, DIM, NCP, K1>::THREADS)
     if(active) pass<T, DIM, N, 0, false>(my, ent + 0 * ES, sy[0], pencil, omega);
     __syncthreads();
     // --- scatter-add: whole cells, coalesced read-modify-write
-    for(int i = tid; i < PPC * NCELL * CELLDOFS; i += C::THREADS)
+    for(int i = tid; i < PPC * NCELL * CELLDOFS; i += NTHR)
     {
       const int s = i / (NCELL * CELLDOFS);
       const int rem = i % (NCELL * CELLDOFS);
@@ -436,26 +458,29 @@ __global__ void __launch_bounds__(Cfg<T, DIM, NCP, K1>::THREADS)
 }
 
 template<typename T, int DIM, int NCP, int K1>
-bool launch(const KernelArgs &a, cudaStream_t s, int n_sms)
+bool launch(KernelArgs a, cudaStream_t s, int n_sms, int variant)
 {
   using C = Cfg<T, DIM, NCP, K1>;
-  const size_t smem = C::smem_bytes();
-  static int per_sm = 0;  // occupancy, queried once per instantiation
-  if(per_sm == 0)
+  if(!C::variant_ok(variant)) variant = 0;
+  a.ppc = C::ppc(variant);
+  const int threads = C::threads(a.ppc);
+  const size_t smem = C::lay(a.ppc).bytes;
+  static int per_sm[C::MAX_VARIANTS] = {};  // occupancy per variant, queried once
+  if(per_sm[variant] == 0)
   {
+    const size_t smem_max = C::lay(C::ppc(C::n_variants() - 1)).bytes;
     if(cudaFuncSetAttribute(schwarz_color_kernel<T, DIM, NCP, K1>,
-                            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+                            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max) != cudaSuccess)
       return false;
     int occ = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, schwarz_color_kernel<T, DIM, NCP, K1>,
-                                                  C::THREADS, smem);
-    per_sm = occ < 1 ? 1 : occ;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, schwarz_color_kernel<T, DIM, NCP, K1>, threads, smem);
+    per_sm[variant] = occ < 1 ? 1 : occ;
   }
   if(a.n_patches <= 0) return true;
-  const int64_t batches = (a.n_patches + C::PPC - 1) / C::PPC;
-  const int64_t cap = (int64_t)n_sms * per_sm * 8;
+  const int64_t batches = (a.n_patches + a.ppc - 1) / a.ppc;
+  const int64_t cap = (int64_t)n_sms * per_sm[variant] * 8;
   const int grid = (int)(batches < cap ? batches : cap);
-  schwarz_color_kernel<T, DIM, NCP, K1><<<grid, C::THREADS, smem, s>>>(a);
+  schwarz_color_kernel<T, DIM, NCP, K1><<<grid, threads, smem, s>>>(a);
   return cudaGetLastError() == cudaSuccess;
 }
 

@@ -338,6 +338,7 @@ struct tpss_precond
   std::vector<int64_t> fix_layer[6];
   tpss::HostPipe pipe;                  // host-buffer entry point
   int stream_variant = 0;               // streamed kernel variant (autotuner)
+  int color_variant = 0;                // per-color kernel variant: patches per CTA (autotuner)
   std::vector<tpss::TimerSlot> timers;
   std::vector<tpss::PendingEvent> pending;
   std::vector<cudaEvent_t> event_pool;
@@ -364,9 +365,12 @@ struct FdLaunch
   int rcp_E = 0;                   // entries per direction of the rcp combinations
   const unsigned char *keep_mask = nullptr;  // RAS boolean weights (FdTables::keep_mask) or nullptr
   const int32_t *keep_class = nullptr;       // first patch of the range
+  int variant = 0;                           // work decomposition (patches per CTA) of the autotuner
 };
 bool launch_fd_f32(int dim, int k, int ncp, const FdLaunch &a, cudaStream_t s);
 bool launch_fd_f64(int dim, int k, int ncp, const FdLaunch &a, cudaStream_t s);
+// work decompositions the per-color kernel offers for (dim, k, ncp) in FP32 / FP64
+int fd_variants(bool fp32, int dim, int k, int ncp);
 
 // mapped (distorted) levels (mapped.cu)
 size_t mapped_smem_bytes(int dim, int np);

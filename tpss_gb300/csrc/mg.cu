@@ -16,6 +16,8 @@
 // the host-driven coarse iteration.
 #include <cmath>
 #include <cstring>
+#include <map>
+#include <mutex>
 
 #include "internal.h"
 
@@ -434,6 +436,35 @@ void scale_relaxation(tpss_mg &mg, MgLevel &lv)
   lv.P->desc.relaxation = w;
   lv.lambda_max = lambda;
 }
+
+// Autotuned smoother kernels of the levels: the first level of a shape (device, dim, degree,
+// cells per direction, patch/smoother variant, precision, local solver) times its kernel's work
+// decompositions (tpss_precond_autotune, zero vectors, 3 applications each); later levels of the
+// same shape -- e.g. the same level in many problems of a batch -- reuse the choice.
+std::mutex g_tune_mutex;
+std::map<std::vector<int>, std::pair<int, int>> g_tuned;  // shape -> (stream, color) variant
+
+void autotune_level(MgLevel &lv, const tpss_mg_desc &d)
+{
+  int dev = 0;
+  TPSS_CUDA(cudaGetDevice(&dev));
+  const tpss_layout &L = *lv.L;
+  const std::vector<int> key = {dev, L.dim, L.k, L.nc[0], L.nc[1], L.nc[2], d.patch_variant,
+                                d.smoother_variant, d.precision, d.local_solver, d.vertex_coords != nullptr};
+  std::lock_guard<std::mutex> lock(g_tune_mutex);
+  auto it = g_tuned.find(key);
+  if(it == g_tuned.end())
+  {
+    TPSS_CUDA(cudaMemset(lv.b.ptr, 0, sizeof(double) * L.n_dofs));
+    int chosen = 0;
+    const int rc = tpss_precond_autotune(lv.P, lv.x.ptr, lv.b.ptr, 3, &chosen, nullptr, nullptr, nullptr);
+    if(rc) fail(rc, tpss_last_error());
+    TPSS_CUDA(cudaDeviceSynchronize());
+    it = g_tuned.emplace(key, std::make_pair(lv.P->stream_variant, lv.P->color_variant)).first;
+  }
+  lv.P->stream_variant = it->second.first;
+  lv.P->color_variant = it->second.second;
+}
 }  // namespace
 
 extern "C" int tpss_mg_create(const tpss_mg_desc *d, tpss_mg **out)
@@ -529,6 +560,8 @@ extern "C" int tpss_mg_create(const tpss_mg_desc *d, tpss_mg **out)
     mg->E = embedding_table(d->degree);
     if(d->auto_relaxation)
       for(int l = 1; l < nl; ++l) scale_relaxation(*mg, mg->lv[l]);
+    if(d->autotune)
+      for(int l = 1; l < nl; ++l) autotune_level(mg->lv[l], *d);
     *out = mg.release();
   });
 }
@@ -733,6 +766,10 @@ extern "C" int tpss_batch_create(const tpss_mg_desc *descs, int n_problems, int 
     TPSS_REQUIRE(descs && out && n_problems >= 1 && n_streams >= 1 && n_streams <= 64, "invalid argument");
     *out = nullptr;
     auto b = std::make_unique<tpss_batch>();
+    for(int i = 0; i < n_problems; ++i)
+      TPSS_REQUIRE(descs[i].coarse_solver == 1,
+                   "batched solves run every CG iteration as one CUDA graph: they need the dense coarse "
+                   "solver (coarse_solver = 1); the coarse CG waits for the host");
     for(int i = 0; i < n_problems; ++i)
     {
       tpss_mg *m = nullptr;

@@ -119,8 +119,11 @@ void build_even_odd(const tpss_layout &L, FdTables &T, const std::vector<double>
 void build_reciprocals(const tpss_layout &L, FdTables &T)
 {
   const int n = L.n, dim = L.dim, E = T.n_entries;
-  const int64_t nloc = ipow(n, dim), combos = ipow(E, dim);
-  if(E == 0 || combos * nloc > (int64_t(1) << 22)) return;
+  const int64_t nloc = ipow(n, dim);
+  // E^dim n^dim values, at most 4 Mi (checked in floating point: E can be large on distorted
+  // levels, whose surrogate patches have many distinct 1-D problems)
+  if(E == 0 || std::pow(double(E), dim) * double(nloc) > double(int64_t(1) << 22)) return;
+  const int64_t combos = ipow(E, dim);
   std::vector<double> r64((size_t)(combos * nloc));
   std::vector<float> r32(r64.size());
   for(int64_t c = 0; c < combos; ++c)
@@ -538,6 +541,7 @@ void apply_color(tpss_precond *p, int color, double *dst, const double *src, cud
   }
   a.n_patches = e - b;
   a.omega = p->desc.relaxation;
+  a.variant = p->color_variant;
   bool ok;
   // even/odd forms of the mirror-symmetric entries (shared keyed tables only; per-patch tables
   // of the fitted and learned solvers have none)
@@ -586,6 +590,17 @@ bool launch_fd_f32(int dim, int k, int ncp, const FdLaunch &a, cudaStream_t s)
 bool launch_fd_f64(int dim, int k, int ncp, const FdLaunch &a, cudaStream_t s)
 {
   return dim == 2 ? launch_fd_double_2(k, ncp, a, s) : launch_fd_double_3(k, ncp, a, s);
+}
+
+int fd_variants_float_2(int k, int ncp);
+int fd_variants_float_3(int k, int ncp);
+int fd_variants_double_2(int k, int ncp);
+int fd_variants_double_3(int k, int ncp);
+
+int fd_variants(bool fp32, int dim, int k, int ncp)
+{
+  if(fp32) return dim == 2 ? fd_variants_float_2(k, ncp) : fd_variants_float_3(k, ncp);
+  return dim == 2 ? fd_variants_double_2(k, ncp) : fd_variants_double_3(k, ncp);
 }
 
 // the column-streamed FP32 smoother applies to this preconditioner: additive 3D vertex patches
@@ -714,6 +729,7 @@ extern "C" int tpss_precond_create(const tpss_layout *layout, tpss_operator *op,
     p->desc = *desc;
     p->op = op;
     p->stream_variant = desc->stream_variant;
+    p->color_variant = desc->stream_variant;  // variants the kernel does not offer fall back to 0
     p->tables = build_local_solvers(*layout, op, *desc);
     if(desc->use_ras_boolean_weights) build_keep_tables(*layout, *p->tables);
     p->timers.resize(5);
@@ -886,7 +902,13 @@ extern "C" int tpss_precond_autotune(tpss_precond *p, double *dst, const double 
     TPSS_REQUIRE(p && dst && src && reps >= 1, "invalid argument");
     cudaStream_t s = as_stream(stream);
     const tpss_layout &L = *p->tables->layout;
-    const int nv = use_stream(p) ? stream_variant_count(L) : 1;
+    // the streamed kernel's work decompositions, or the per-color kernel's patches per CTA
+    // (dense local inverses have a single kernel)
+    const bool streamed = use_stream(p);
+    const int nv = streamed ? stream_variant_count(L)
+                   : p->tables->dense ? 1
+                                      : fd_variants(p->desc.precision == TPSS_FP32, L.dim, L.k, L.ncp);
+    int &variant = streamed ? p->stream_variant : p->color_variant;
     if(n_variants) *n_variants = nv;
     if(nv <= 1)
     {
@@ -911,7 +933,7 @@ extern "C" int tpss_precond_autotune(tpss_precond *p, double *dst, const double 
     float best_ms = 0.f;
     for(int v = 0; v < nv; ++v)
     {
-      p->stream_variant = v;
+      variant = v;
       precond_vmult(p, dst, src, s);  // warm-up (scratch sizing, attributes)
       TPSS_CUDA(cudaEventRecord(e0, s));
       for(int r = 0; r < reps; ++r) precond_vmult(p, dst, src, s);
@@ -927,7 +949,7 @@ extern "C" int tpss_precond_autotune(tpss_precond *p, double *dst, const double 
         best_ms = ms;
       }
     }
-    p->stream_variant = best;
+    variant = best;
     if(chosen) *chosen = best;
     precond_vmult(p, dst, src, s);  // dst holds the chosen variant's result
   });
