@@ -631,7 +631,9 @@ def distorted_section(tpss, args):
     """Distorted 3D DGQ3 32^3 level (interior vertices moved by `distortion` x the shortest
     edge in random directions, as the reference's distort_random): train the learned local
     solver's network on the patches of four other meshes, then solve CG + V-cycle to 1e-8 with
-    surrogate (FP64, FP32), Kronecker-sum-fitted (FP32) and learned (FP32) local solvers."""
+    surrogate (FP64, FP32), Kronecker-sum-fitted, rank-2 Kronecker (KSVD), learned and exact
+    (FP32) local solvers; measured local inverse errors of the separable solvers."""
+    import numpy as np
     import torch
     from tpss_gb300.mesh import distorted_cube
     dim, k, n, fac = 3, 3, 32, args.distortion
@@ -664,11 +666,32 @@ def distorted_section(tpss, args):
     N = n ** dim * (k + 1) ** dim
     f = torch.tensor(philox_src(N, args.seed), dtype=torch.float64, device="cuda")
     fp64, fp32 = tpss.Precision.fp64, tpss.Precision.fp32
+    # measured local inverse error ||A_j^-1 - B_j||_F / ||A_j^-1||_F of every local solver on
+    # a sample of 512 patches spread over the finest level (exact FP64 inverses on the GPU)
+    sh = tpss.SubdomainHandler(tpss.SubdomainHandler.AdditionalData(
+        dim=dim, degree=k, n_cells=(n,) * dim, patch_variant=tpss.PatchVariant.vertex, vertex_coords=X))
+    op = tpss.LaplaceOperator(sh)
+    P = sh.n_subdomains()
+    first = P // 3
+    errs = {}
+    for name, ls, model in (("surrogate", tpss.LocalSolver.fd, None), ("ksum", tpss.LocalSolver.ksum, None),
+                            ("ksvd", tpss.LocalSolver.ksvd, None), ("learned", tpss.LocalSolver.learned, m)):
+        p = tpss.SchwarzPreconditioner()
+        p.initialize(sh, op, tpss.SchwarzPreconditioner.AdditionalData(relaxation=0.15, local_solver=ls,
+                                                                       model=model))
+        e = tpss.local_inverse_error(p, op, first, 512)
+        errs[name] = {"mean": float(e.mean()), "median": float(np.median(e)), "max": float(e.max())}
+        del p
+    out["local_inverse_error"] = dict(errs, sample=f"patches {first}..{first + 511} of {P}",
+                                      measure="||A_j^-1 - B_j||_F / ||A_j^-1||_F, A_j exact (FP64 inverse)")
+    del op, sh
     runs = (("surrogate_fp64", tpss.LocalSolver.fd, fp64, None, fp64),
             ("surrogate_fp32", tpss.LocalSolver.fd, fp32, None, fp64),
             ("ksum_fp32", tpss.LocalSolver.ksum, fp32, None, fp64),
+            ("ksvd_fp32", tpss.LocalSolver.ksvd, fp32, None, fp64),
             ("learned_fp32", tpss.LocalSolver.learned, fp32, m, fp64),
-            ("learned_fp32_vcycle", tpss.LocalSolver.learned, fp32, m, fp32))
+            ("learned_fp32_vcycle", tpss.LocalSolver.learned, fp32, m, fp32),
+            ("exact_fp32", tpss.LocalSolver.exact, fp32, None, fp64))
     for name, ls, prec, model, vprec in runs:
         ts = time.perf_counter()
         mg = tpss.MultigridSolver(dim, k, 2, n, relaxation=0.15, precision=prec, coarse_solver=1,

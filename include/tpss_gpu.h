@@ -58,6 +58,12 @@ extern "C" {
                                 the mapped level operator */
 #define TPSS_LOCAL_LEARNED 3 /* surrogate 1-D problems corrected by a trained network
                                 (tpss_mlp) from the patch's vertex geometry */
+#define TPSS_LOCAL_KSVD 4    /* rank-2 Kronecker approximation of the exact patch matrix
+                                (CP/ALS, compute_kcp / compute_ksvd, kroneckersvd.h:306-585),
+                                inverted by simultaneous diagonalization of its two terms
+                                (fast diagonalization with eigenvalue combinations
+                                1 + prod_d mu_d); patches whose fit is not safely positive
+                                definite keep the surrogate; needs the mapped level operator */
 
 #define TPSS_FP64 0
 #define TPSS_FP32 1
@@ -368,6 +374,14 @@ int tpss_transfer_restrict_add(int dim, int degree, const int *n_cells_coarse, d
  * term, LocalSolverVariant::Bilaplacian).
  * ------------------------------------------------------------------------------------- */
 typedef struct tpss_c0ip tpss_c0ip;
+/* tpss_c0ip_desc.problem: the form on the FE_Q node grid */
+#define TPSS_C0IP_BIHARMONIC 0 /* the clamped C0IP biharmonic form above */
+#define TPSS_Q_POISSON 1       /* the Poisson problem with continuous FE_Q(k) (Dirichlet): the
+                                  Laplacian A = M x L + L x M on the interior nodes, vertex patches
+                                  of the (2k-1)^2 nodes inside their 2 x 2 cells (the Q layout of
+                                  TPSS/dof_info.h:344-355, TPSS/patch_dof_worker.h:265-300;
+                                  apps/laplace_integrator.h:800-1198 for the CFEM operator); the
+                                  fast-diagonalization local solver is exact here */
 typedef struct tpss_c0ip_desc
 {
   int degree;          /* 2..7 */
@@ -377,6 +391,7 @@ typedef struct tpss_c0ip_desc
   int local_solver;    /* TPSS_LOCAL_EXACT or TPSS_LOCAL_FD */
   int precision;       /* smoother arithmetic, TPSS_FP64 / TPSS_FP32 */
   double relaxation;   /* Schwarz damping (vertex patches, 2D: 0.25 in TPSS.h:121-163) */
+  int problem;         /* TPSS_C0IP_BIHARMONIC (0) or TPSS_Q_POISSON */
 } tpss_c0ip_desc;
 
 int tpss_c0ip_create(const tpss_c0ip_desc *desc, tpss_c0ip **out);
@@ -432,6 +447,26 @@ int tpss_learned_targets(const tpss_layout *layout, const tpss_operator *op, dou
  * patch-local lexicographic DoFs, device FP64) from the mapped level operator */
 int tpss_local_matrices(const tpss_layout *layout, const tpss_operator *op, int64_t first,
                         int64_t count, double *out);
+/* Low Kronecker-rank approximation of a batch of matrices on the GPU (compute_kcp /
+ * compute_ksvd, TPSS/kroneckersvd.h:306-402, 501-585): K_i ~ sum_r F_{dim-1,r} x .. x F_{0,r}
+ * with factors F_{d,r} of m[d] x n[d] (dim = 2 or 3, rank <= 4) by `iterations` alternating
+ * least-squares sweeps (rank^2 + 10 in the reference) from the initial factors given in
+ * `factors`, which receives the result. mats: count x prod(m) x prod(n), row-major, direction 0
+ * fastest in rows and columns; factors: per matrix, per direction d, per term r an m[d] x n[d]
+ * row-major block (device FP64). */
+int tpss_kronecker_approx(const double *mats, int64_t count, int dim, const int *m, const int *n,
+                          int rank, int iterations, double *factors, void *stream);
+/* The local inverses a preconditioner applies, as dense matrices: patches [first, first + count),
+ * count x n_loc x n_loc row-major device FP64 (S diag(1/sum lambda) S^T of its fast-diagonalization
+ * tables, or the stored dense inverses of TPSS_LOCAL_EXACT). TensorProductMatrix::as_inverse_table
+ * for the separable state (tensor_product_matrix.h), without the damping. */
+int tpss_precond_local_inverse(const tpss_precond *p, int64_t first, int64_t count, double *out);
+/* Measured local inverse error (no counterpart in the reference): err[i] (host) =
+ * ||A_j^-1 - B_j||_F / ||A_j^-1||_F for the patches j = first + i, A_j the exact patch matrix
+ * of the mapped level operator `op` (inverted in FP64 on the GPU) and B_j the preconditioner's
+ * local inverse (tpss_precond_local_inverse). */
+int tpss_local_inverse_error(const tpss_precond *p, const tpss_operator *op, int64_t first,
+                             int64_t count, double *err);
 
 int tpss_diag_fma_peak(int precision, int iters, double *flops_per_second, void *stream);
 

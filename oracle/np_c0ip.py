@@ -120,11 +120,40 @@ def matrices_1d(k, h, ip=1.0, keep_boundary=False):
     return M[s, s], L[s, s], B[s, s]
 
 
-def level_matrix(k, nc, ip=1.0):
-    """2-D C0IP matrix on the unit square, nc x nc cells (Kronecker form)."""
+def level_matrix(k, nc, ip=1.0, problem="c0ip"):
+    """2-D C0IP matrix on the unit square, nc x nc cells (Kronecker form); problem "poisson": the
+    Laplacian of continuous FE_Q(k), M x L + L x M."""
     h = [1.0 / nc] * nc
     M, L, B = matrices_1d(k, h, ip)
+    if problem == "poisson":
+        return np.kron(M, L) + np.kron(L, M)
     return np.kron(M, B) + 2.0 * np.kron(L, L) + np.kron(B, M)
+
+
+def poisson_q_matrix_quadrature(k, nc):
+    """The FE_Q(k) Laplacian on the unit square by plain 2-D quadrature over the cells (interior
+    nodes, x fastest) -- independent of the Kronecker form."""
+    h = 1.0 / nc
+    nodes, P, P1, _ = basis_1d(k)
+    qx, qw = npleg.leggauss(k + 1)
+    qx, qw = 0.5 * (qx + 1.0), 0.5 * qw
+    V = np.array([[p(x) for x in qx] for p in P])
+    D = np.array([[p(x) for x in qx] for p in P1]) / h
+    ng = nc * k + 1
+    A = np.zeros((ng * ng, ng * ng))
+    for cy in range(nc):
+        for cx in range(nc):
+            ii = np.array([(cy * k + b) * ng + cx * k + a for b in range(k + 1) for a in range(k + 1)])
+            Kc = np.zeros((len(ii), len(ii)))
+            for qy in range(k + 1):
+                for qxi in range(k + 1):
+                    w = qw[qy] * qw[qxi] * h * h
+                    gx = np.array([D[a, qxi] * V[b, qy] for b in range(k + 1) for a in range(k + 1)])
+                    gy = np.array([V[a, qxi] * D[b, qy] for b in range(k + 1) for a in range(k + 1)])
+                    Kc += w * (np.outer(gx, gx) + np.outer(gy, gy))
+            A[np.ix_(ii, ii)] += Kc
+    inner = [j * ng + i for j in range(1, ng - 1) for i in range(1, ng - 1)]
+    return A[np.ix_(inner, inner)]
 
 
 def matrix_2d_quadrature(k, nc, ip=1.0):
@@ -222,14 +251,17 @@ def patches(nc):
     return out
 
 
-def schwarz_vmult(k, nc, src, omega, local="exact", ip=1.0):
+def schwarz_vmult(k, nc, src, omega, local="exact", ip=1.0, problem="c0ip"):
     """Additive vertex-patch Schwarz: sum_j omega R_j^T A_j^-1 R_j src with the exact patch
     matrices (local = "exact", LocalSolverVariant::Exact) or their Kronecker sum without the
     mixed-derivative term B (x) M + M (x) B (local = "bilaplacian", solved by fast
-    diagonalization in the product)."""
-    A = level_matrix(k, nc, ip)
+    diagonalization in the product). problem "poisson": the FE_Q Laplacian, whose patch matrix
+    is the Kronecker sum M x L + L x M of the restricted 1-D matrices (both locals coincide)."""
+    A = level_matrix(k, nc, ip, problem)
     h = [1.0 / nc] * nc
     M, L, B = matrices_1d(k, h, ip)
+    if problem == "poisson":
+        B = L
     out = np.zeros_like(src)
     m = 2 * k - 1
     for vx, vy, _ in patches(nc):
@@ -265,24 +297,24 @@ def prolongation_1d(k, nc_coarse):
 
 
 def mg_cg_solve(k, n_rep, nc_fine, f, omega, local="exact", rel_tol=1e-8, abs_tol=1e-14,
-                max_iter=200, ip=1.0):
+                max_iter=200, ip=1.0, problem="c0ip"):
     """CG + V-cycle (one pre-/post-step of the additive patch smoother, exact coarse solve)."""
     nl, n = 0, n_rep
     while n <= nc_fine:
         nl += 1
         n *= 2
     ncs = [n_rep << l for l in range(nl)]
-    A = [level_matrix(k, c, ip) for c in ncs]
+    A = [level_matrix(k, c, ip, problem) for c in ncs]
     P = [None] + [np.kron(prolongation_1d(k, ncs[l - 1]), prolongation_1d(k, ncs[l - 1])) for l in range(1, nl)]
     A0inv = np.linalg.inv(A[0])
 
     def vcycle(l, b):
         if l == 0:
             return A0inv @ b
-        x = schwarz_vmult(k, ncs[l], b, omega, local, ip)
+        x = schwarz_vmult(k, ncs[l], b, omega, local, ip, problem)
         bc = P[l].T @ (b - A[l] @ x)
         x = x + P[l] @ vcycle(l - 1, bc)
-        return x + schwarz_vmult(k, ncs[l], b - A[l] @ x, omega, local, ip)
+        return x + schwarz_vmult(k, ncs[l], b - A[l] @ x, omega, local, ip, problem)
 
     u = np.zeros_like(f)
     r = f.copy()

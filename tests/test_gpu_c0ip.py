@@ -50,6 +50,49 @@ def test_c0ip_smoother(tpss, c0, cuda, k, nc, local, prec):
     assert rel_err(y.cpu().numpy(), ref) <= (1e-12 if prec == 0 else 2e-5)
 
 
+@pytest.mark.parametrize("k,nc", [(2, 4), (3, 3), (5, 2)])
+def test_q_poisson_operator(tpss, c0, cuda, k, nc):
+    """Poisson with continuous FE_Q(k) (the Q vertex-patch layout): level operator 1e-12."""
+    import torch
+    P = tpss.C0IPBiharmonic(k, nc, nc, problem=tpss.C0IPBiharmonic.Q_POISSON)
+    A = c0.level_matrix(k, nc, problem="poisson")
+    x = philox(30 + k, A.shape[0])
+    y = torch.full((A.shape[0],), 3.0, dtype=torch.float64, device=cuda)
+    P.vmult(y, torch.tensor(x, dtype=torch.float64, device=cuda))
+    assert rel_err(y.cpu().numpy(), A @ x) <= 1e-12
+
+
+@pytest.mark.parametrize("k,nc,local,prec", [(2, 6, 1, 0), (3, 4, 0, 0), (3, 4, 1, 0), (4, 4, 0, 1), (6, 4, 0, 0)])
+def test_q_poisson_smoother(tpss, c0, cuda, k, nc, local, prec):
+    """Additive Q vertex patches ((2k-1)^2 nodes): exact and fast-diagonalization local solvers
+    (identical here), FP64 1e-12 and FP32 2e-5 against the numpy dense patch solves."""
+    import torch
+    P = tpss.C0IPBiharmonic(k, nc // 2, nc, local_solver=local, precision=prec, relaxation=0.3,
+                            problem=tpss.C0IPBiharmonic.Q_POISSON)
+    n = (nc * k - 1) ** 2
+    x = philox(40 + k, n)
+    y = torch.full((n,), 7.0, dtype=torch.float64, device=cuda)
+    P.smooth(y, torch.tensor(x, dtype=torch.float64, device=cuda))
+    ref = c0.schwarz_vmult(k, nc, x, 0.3, "exact", problem="poisson")
+    assert rel_err(y.cpu().numpy(), ref) <= (1e-12 if prec == 0 else 2e-5)
+
+
+@pytest.mark.parametrize("k,n_rep,ncf,local", [(2, 2, 16, 0), (3, 2, 8, 1), (4, 2, 8, 0)])
+def test_q_poisson_cg_mg_iterations(tpss, c0, cuda, k, n_rep, ncf, local):
+    """CG + V-cycle with the Q vertex-patch smoother (damping 0.25, TPSS.h:121-163): iteration
+    counts identical to the numpy oracle, solution 1e-8."""
+    import torch
+    n = (ncf * k - 1) ** 2
+    f = philox(50 + k, n)
+    it_ref, _, u_ref = c0.mg_cg_solve(k, n_rep, ncf, f, 0.25, "exact", problem="poisson")
+    P = tpss.C0IPBiharmonic(k, n_rep, ncf, local_solver=local, relaxation=0.25,
+                            problem=tpss.C0IPBiharmonic.Q_POISSON)
+    u = torch.zeros(n, dtype=torch.float64, device=cuda)
+    it, _ = P.solve(u, torch.tensor(f, dtype=torch.float64, device=cuda))
+    assert it == it_ref
+    assert rel_err(u.cpu().numpy(), u_ref) <= 1e-8
+
+
 @pytest.mark.parametrize("k,n_rep,ncf,local", [(2, 2, 8, 1), (3, 2, 8, 1), (3, 2, 16, 0), (4, 2, 8, 0)])
 def test_c0ip_cg_mg_iterations(tpss, c0, cuda, k, n_rep, ncf, local):
     import torch

@@ -63,8 +63,40 @@ def test_local_matrices_are_level_submatrices(tpss, oracle, nd, xcheck, cuda, di
         assert rel_err(got[p], A[np.ix_(idx, idx)]) <= 1e-12
 
 
+@pytest.mark.parametrize("dim,k,nc,seed", [(2, 3, (5, 4), 11), (3, 3, (3, 3, 3), 12)])
+def test_local_inverse_error(tpss, oracle, nd, xcheck, cuda, dim, k, nc, seed):
+    """tpss_precond_local_inverse and tpss_local_inverse_error against numpy: the dense local
+    inverses the preconditioner applies, the relative Frobenius error of each against the FP64
+    inverse of the exact patch matrix (1e-8 relative agreement with numpy), zero error (1e-10)
+    for the exact local solver and for surrogate patches on an undistorted mesh."""
+    X = oracle.distorted_coords(dim, list(nc), seed, 0.25)
+    A = nd.sipg_matrix_mapped(dim, k, list(nc), X)
+    sh, op = level(tpss, dim, k, nc, X)
+    P = sh.n_subdomains()
+    lo, _ = sh.patches()
+    exact_inv = [np.linalg.inv(A[np.ix_(ix, ix)])
+                 for ix in (xcheck.patch_dofs(dim, k, list(nc), lo[p][:dim], 2) for p in range(P))]
+    for ls in (tpss.LocalSolver.fd, tpss.LocalSolver.ksum, tpss.LocalSolver.exact):
+        p = tpss.SchwarzPreconditioner()
+        p.initialize(sh, op, tpss.SchwarzPreconditioner.AdditionalData(relaxation=0.5, local_solver=ls))
+        B = tpss.precond_local_inverse(p, 0, P, device=cuda).cpu().numpy()
+        err = tpss.local_inverse_error(p, op, 0, P)
+        ref = np.array([np.linalg.norm(B[j] - exact_inv[j]) / np.linalg.norm(exact_inv[j]) for j in range(P)])
+        np.testing.assert_allclose(err, ref, rtol=1e-8, atol=1e-13)
+        if ls == tpss.LocalSolver.exact:
+            assert err.max() <= 1e-10
+        else:
+            assert err.min() > 1e-6  # a distorted patch is not separable
+    # an undistorted level: surrogate fast diagonalization is the exact local inverse
+    Xc = oracle.distorted_coords(dim, list(nc), seed, 0.0)
+    shc, opc = level(tpss, dim, k, nc, Xc)
+    pc = tpss.SchwarzPreconditioner()
+    pc.initialize(shc, opc, tpss.SchwarzPreconditioner.AdditionalData(relaxation=0.5))
+    assert tpss.local_inverse_error(pc, opc, 0, shc.n_subdomains()).max() <= 1e-10
+
+
 @pytest.mark.parametrize("dim,k,nc,seed,precision", [(2, 3, (5, 4), 4, 0), (2, 2, (6, 6), 5, 1),
-                                                      (3, 1, (4, 3, 3), 6, 0)])
+                                                      (3, 1, (4, 3, 3), 6, 0), (3, 3, (3, 3, 3), 13, 0)])
 def test_exact_local_solver_vs_dense_patch_solves(tpss, oracle, nd, xcheck, cuda, dim, k, nc, seed, precision):
     X = oracle.distorted_coords(dim, list(nc), seed, 0.25)
     A = nd.sipg_matrix_mapped(dim, k, list(nc), X)

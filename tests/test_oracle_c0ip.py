@@ -16,6 +16,28 @@ def test_kronecker_form_equals_2d_quadrature(c0, k, nc):
     assert np.abs(A - Q).max() <= 1e-13 * np.abs(Q).max()
 
 
+@pytest.mark.parametrize("k,nc", [(2, 3), (3, 2), (4, 3)])
+def test_q_poisson_kronecker_form_and_patch_matrices(c0, k, nc):
+    """Poisson with continuous FE_Q(k): the Kronecker form M x L + L x M equals a plain 2-D
+    quadrature assembly, and every vertex patch matrix of the (2k-1)^2 interior patch nodes (the
+    Q layout, TPSS/patch_dof_worker.h:265-300) equals the Kronecker sum of the restricted 1-D
+    matrices -- the relation of FDAssemblyVertexPatch / FDInverseVertexPatch for Q
+    (tests/apps_laplace_integrator.cc:393-430), so fast diagonalization is the exact local solver."""
+    A = c0.level_matrix(k, nc, problem="poisson")
+    Q = c0.poisson_q_matrix_quadrature(k, nc)
+    assert np.abs(A - Q).max() <= 1e-13 * np.abs(Q).max()
+    M, L, _ = c0.matrices_1d(k, [1.0 / nc] * nc)
+    m = 2 * k - 1
+    for vx, vy, _ in c0.patches(nc):
+        idx = c0.patch_indices(k, nc, vx, vy)
+        sx = slice((vx - 1) * k, (vx - 1) * k + m)
+        sy = slice((vy - 1) * k, (vy - 1) * k + m)
+        K = np.kron(M[sy, sy], L[sx, sx]) + np.kron(L[sy, sy], M[sx, sx])
+        assert np.abs(A[np.ix_(idx, idx)] - K).max() <= 1e-13 * np.abs(K).max()
+        Ki = np.linalg.inv(K)
+        assert np.abs(Ki @ K - np.eye(len(idx))).max() <= 1e-10
+
+
 def test_level_matrix_spd(c0):
     A = c0.level_matrix(3, 4)
     assert np.abs(A - A.T).max() <= 1e-13 * np.abs(A).max()

@@ -44,6 +44,27 @@ def test_ksvd_is_best_approximation(oracle):
     np.testing.assert_allclose(err, np.sqrt(np.sum(s[2:] ** 2)), rtol=1e-10)
 
 
+def test_als_reproduces_reference_order3_case():
+    from oracle import np_ksvd
+    K, m, n, init = np_ksvd.reference_order3_case()
+    F = np_ksvd.kcp_als(K, m, n, init, 14)  # rank^2 + 10 sweeps, compute_kcp's default
+    assert np.abs(np_ksvd.kron_matrix(F) - K).max() <= 1e-12 * np.abs(K).max()
+
+
+def test_als_rank2_matches_ksvd_of_reference_diagonal(oracle):
+    """For two factors the ALS fixed point is the truncated SVD of the reshuffled matrix: on the
+    reference's known-answer input diag(1..12) (4x4 (x) 3x3), the rank-2 approximation from ALS
+    equals the one from the oracle's KSVD, whose first term is pinned to the reference's numbers."""
+    from oracle import np_ksvd
+    K = np.diag(np.arange(1.0, 13.0))
+    B, A = oracle.ksvd(K, (4, 4), (3, 3), 2)
+    ref = sum(np.kron(B[r], A[r]) for r in range(2))
+    g = np.random.default_rng(3)
+    init = [g.standard_normal((2, 3, 3)), g.standard_normal((2, 4, 4))]
+    F = np_ksvd.kcp_als(K, (3, 4), (3, 4), init, 300)
+    np.testing.assert_allclose(np_ksvd.kron_matrix(F), ref, atol=1e-9 * np.abs(ref).max())
+
+
 def test_ksvd_separable_patch_matrix(oracle):
     """A Cartesian 2D FD patch matrix M (x) L + L (x) M has Kronecker rank 2 exactly."""
     M1, L1 = oracle.patch_matrices_1d(3, [0.25, 0.25], 0, 0)

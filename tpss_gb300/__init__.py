@@ -434,13 +434,18 @@ class SchwarzSmoother:
 class C0IPBiharmonic:
     """Clamped C0IP biharmonic problem on the unit square (FE_Q(k), Gauss-Lobatto nodes):
     level operators, the additive vertex-patch smoother and CG + V-cycle. Vectors: interior
-    nodes, x fastest, float64 CUDA tensors."""
+    nodes, x fastest, float64 CUDA tensors. With problem = Q_POISSON the same node grid carries
+    the Poisson problem with continuous FE_Q(k) (Laplacian M x L + L x M, Q vertex patches)."""
+
+    BIHARMONIC = 0  # tpss_c0ip_desc.problem: TPSS_C0IP_BIHARMONIC
+    Q_POISSON = 1   # TPSS_Q_POISSON: Laplacian with continuous FE_Q(k), the Q vertex-patch layout
 
     def __init__(self, degree, n_rep, n_cells_fine, ip_factor=1.0, local_solver=1, precision=0,
-                 relaxation=0.25):
+                 relaxation=0.25, problem=0):
         d = _lib.C0ipDesc()
         d.degree, d.n_rep, d.n_cells_fine = degree, n_rep, n_cells_fine
         d.ip_factor, d.local_solver, d.precision, d.relaxation = float(ip_factor), int(local_solver), int(precision), float(relaxation)
+        d.problem = int(problem)
         h = C.c_void_p()
         check(load().tpss_c0ip_create(C.byref(d), C.byref(h)))
         self._h = h
@@ -558,6 +563,7 @@ class LocalSolver:
     exact = 1    # dense inverse of the exact patch matrix (basic state + InverseTable)
     ksum = 2     # FD of the Kronecker sum fitted to the exact patch matrix
     learned = 3  # surrogate 1-D problems corrected by a trained MLP
+    ksvd = 4     # rank-2 Kronecker approximation of the exact patch matrix (CP/ALS), simultaneously diagonalized
 
 
 class MLP:
@@ -659,6 +665,51 @@ def local_matrices(subdomain_handler, operator, first, count, device="cuda"):
     check(load().tpss_local_matrices(subdomain_handler.handle, operator.handle, int(first), int(count),
                                      C.c_void_p(out.data_ptr())))
     return out
+
+
+def kronecker_approx(mats, m, n, init, iterations=14, stream=None):
+    """Low Kronecker-rank approximation K_i ~ sum_r F_{dim-1,r} x .. x F_{0,r} of a batch of
+    matrices by alternating least squares (compute_kcp / compute_ksvd), on the GPU.
+
+    mats: [count, prod(m), prod(n)] float64 CUDA tensor (direction 0 fastest in rows and columns);
+    m, n: factor shapes per direction; init: per matrix the initial factors, a list over
+    directions of [rank, m_d, n_d] float64 CUDA tensors of shape [count, rank, m_d, n_d].
+    Returns the fitted factors in the same layout."""
+    import torch
+    dim = len(m)
+    count = mats.shape[0]
+    rank = init[0].shape[1]
+    flat = torch.cat([f.reshape(count, -1) for f in init], dim=1).contiguous()
+    mm = (C.c_int * 3)(*(list(m) + [1] * (3 - dim)))
+    nn = (C.c_int * 3)(*(list(n) + [1] * (3 - dim)))
+    check(load().tpss_kronecker_approx(C.c_void_p(mats.contiguous().data_ptr()), count, dim, mm, nn, rank,
+                                       int(iterations), C.c_void_p(flat.data_ptr()), _stream(stream)))
+    out, o = [], 0
+    for d in range(dim):
+        sz = rank * m[d] * n[d]
+        out.append(flat[:, o:o + sz].reshape(count, rank, m[d], n[d]))
+        o += sz
+    return out
+
+
+def precond_local_inverse(preconditioner, first, count, device="cuda"):
+    """Dense local inverses [count, n_loc, n_loc] (FP64) that the preconditioner applies to the
+    patches first..first+count-1 (without the damping)."""
+    import torch
+    n_loc = preconditioner.subdomain_handler.n_dofs_per_patch()
+    out = torch.empty((count, n_loc, n_loc), dtype=torch.float64, device=device)
+    check(load().tpss_precond_local_inverse(preconditioner.handle, int(first), int(count),
+                                            C.c_void_p(out.data_ptr())))
+    return out
+
+
+def local_inverse_error(preconditioner, operator, first, count):
+    """||A_j^-1 - B_j||_F / ||A_j^-1||_F per patch j (numpy array): A_j the exact patch matrix of
+    the mapped level operator, B_j the preconditioner's local inverse."""
+    err = np.zeros(count)
+    check(load().tpss_local_inverse_error(preconditioner.handle, operator.handle, int(first), int(count),
+                                          err.ctypes.data_as(C.POINTER(C.c_double))))
+    return err
 
 
 class MultigridSolver:

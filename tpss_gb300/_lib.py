@@ -74,7 +74,7 @@ class PrecondDesc(C.Structure):
 class C0ipDesc(C.Structure):
     _fields_ = [("degree", C.c_int), ("n_rep", C.c_int), ("n_cells_fine", C.c_int),
                 ("ip_factor", C.c_double), ("local_solver", C.c_int), ("precision", C.c_int),
-                ("relaxation", C.c_double)]
+                ("relaxation", C.c_double), ("problem", C.c_int)]
 
 
 class MlpDesc(C.Structure):
@@ -166,6 +166,10 @@ SIGNATURES = {
     "tpss_learned_features": (C.c_int, [_vp, _vp]),
     "tpss_learned_targets": (C.c_int, [_vp, _vp, C.c_double, _vp]),
     "tpss_local_matrices": (C.c_int, [_vp, _vp, C.c_int64, C.c_int64, _vp]),
+    "tpss_precond_local_inverse": (C.c_int, [_vp, C.c_int64, C.c_int64, _vp]),
+    "tpss_kronecker_approx": (C.c_int, [_vp, C.c_int64, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                        C.c_int, C.c_int, _vp, _vp]),
+    "tpss_local_inverse_error": (C.c_int, [_vp, _vp, C.c_int64, C.c_int64, _dp]),
     "tpss_last_error": (C.c_char_p, []),
     "tpss_version": (C.c_char_p, []),
 }

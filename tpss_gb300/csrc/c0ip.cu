@@ -227,11 +227,13 @@ __global__ void __launch_bounds__(256) c0ip_x_kernel(const double *__restrict__ 
   }
 }
 
-// dst = M_y t_b + 2 L_y t_l + B_y t_m along the columns
+// dst = M_y t_b + mixed L_y t_l + B_y t_m along the columns (mixed = 2 for the biharmonic
+// form, 0 for the Laplacian, whose "B" is the stiffness matrix)
 __global__ void __launch_bounds__(256) c0ip_y_kernel(const double *__restrict__ tm, const double *__restrict__ tl,
                                                      const double *__restrict__ tb, int n, int bw,
                                                      const double *__restrict__ M, const double *__restrict__ L,
-                                                     const double *__restrict__ B, double *__restrict__ dst)
+                                                     const double *__restrict__ B, double mixed,
+                                                     double *__restrict__ dst)
 {
   const int64_t total = (int64_t)n * n;
   const int w = 2 * bw + 1;
@@ -247,7 +249,7 @@ __global__ void __launch_bounds__(256) c0ip_y_kernel(const double *__restrict__ 
       const int64_t src = (int64_t)j * n + x;
       const int at = y * w + o + bw;
       s += B[at] * tm[src];
-      if(o >= -bh && o <= bh) s += M[at] * tb[src] + 2.0 * L[at] * tl[src];
+      if(o >= -bh && o <= bh) s += M[at] * tb[src] + mixed * L[at] * tl[src];
     }
     dst[t] = s;
   }
@@ -387,6 +389,7 @@ struct tpss_c0ip
 {
   tpss_c0ip_desc desc{};
   int bw = 0, m = 0;
+  double mixed = 2.0;  // weight of L (x) L: 2 (biharmonic), 0 (Laplacian)
   std::vector<C0ipLevel> lv;
   tpss::DeviceBuffer<double> coarse_inv, partial, scal, cr, cp, cAp, cz;
   // the CG preconditioner step (z = V-cycle(r)) as one CUDA graph, captured on a private stream
@@ -455,6 +458,7 @@ void build_level(tpss_c0ip &c, C0ipLevel &L, const Poly1D &poly, int nc)
   L.n = nc * k - 1;
   Band1D M, Lm, B;
   global_1d(poly, nc, d.ip_factor, M, Lm, B);
+  if(d.problem == TPSS_Q_POISSON) B = Lm;  // A = M (x) L + L (x) M
   L.bandM.upload(to_band(M, na, bw).data(), (size_t)L.n * (2 * bw + 1));
   L.bandL.upload(to_band(Lm, na, bw).data(), (size_t)L.n * (2 * bw + 1));
   L.bandB.upload(to_band(B, na, bw).data(), (size_t)L.n * (2 * bw + 1));
@@ -514,7 +518,7 @@ void build_level(tpss_c0ip &c, C0ipLevel &L, const Poly1D &poly, int nc)
             for(int b2 = 0; b2 < m; ++b2)
               for(int a2 = 0; a2 < m; ++a2)
                 K[(size_t)(b * m + a) * m2 + b2 * m + a2] =
-                  My[b * m + b2] * Bx[a * m + a2] + 2.0 * Ly[b * m + b2] * Lx[a * m + a2] +
+                  My[b * m + b2] * Bx[a * m + a2] + c.mixed * Ly[b * m + b2] * Lx[a * m + a2] +
                   By[b * m + b2] * Mx[a * m + a2];
         const auto Ki = cholesky_inv(K, m2);
         double *dst = &tab[(size_t)(kx + 4 * ky) * m2 * m2];
@@ -601,7 +605,7 @@ void op_apply(const tpss_c0ip &c, const C0ipLevel &L, double *dst, const double 
   c0ip_x_kernel<<<grid_for_c(N), 256, 0, s>>>(src, L.n, c.bw, L.bandM.ptr, L.bandL.ptr, L.bandB.ptr,
                                              L.tm.ptr, L.tl.ptr, L.tb.ptr);
   c0ip_y_kernel<<<grid_for_c(N), 256, 0, s>>>(L.tm.ptr, L.tl.ptr, L.tb.ptr, L.n, c.bw, L.bandM.ptr,
-                                             L.bandL.ptr, L.bandB.ptr, dst);
+                                             L.bandL.ptr, L.bandB.ptr, c.mixed, dst);
   TPSS_CUDA(cudaGetLastError());
 }
 
@@ -756,11 +760,13 @@ extern "C" int tpss_c0ip_create(const tpss_c0ip_desc *d, tpss_c0ip **out)
     TPSS_REQUIRE(d->local_solver == TPSS_LOCAL_EXACT || d->local_solver == TPSS_LOCAL_FD,
                  "C0IP: local_solver must be TPSS_LOCAL_EXACT or TPSS_LOCAL_FD (no mixed derivatives)");
     TPSS_REQUIRE(d->precision == TPSS_FP64 || d->precision == TPSS_FP32, "invalid precision");
+    TPSS_REQUIRE(d->problem == TPSS_C0IP_BIHARMONIC || d->problem == TPSS_Q_POISSON, "invalid problem");
     int nl = 0;
     for(int nc = d->n_rep; nc <= d->n_cells_fine; nc *= 2) ++nl;
     TPSS_REQUIRE((d->n_rep << (nl - 1)) == d->n_cells_fine, "n_cells_fine must be n_rep * 2^L");
     auto c = std::make_unique<tpss_c0ip>();
     c->desc = *d;
+    c->mixed = d->problem == TPSS_Q_POISSON ? 0.0 : 2.0;
     c->bw = 2 * d->degree;
     c->m = 2 * d->degree - 1;
     const Poly1D poly = make_poly(d->degree);
@@ -776,6 +782,7 @@ extern "C" int tpss_c0ip_create(const tpss_c0ip_desc *d, tpss_c0ip **out)
       TPSS_REQUIRE(N0 <= 4096, "C0IP: coarse level too large for the dense solve");
       Band1D M, Lm, B;
       global_1d(poly, nc0, d->ip_factor, M, Lm, B);
+      if(d->problem == TPSS_Q_POISSON) B = Lm;
       std::vector<double> A((size_t)N0 * N0);
       for(int y = 0; y < n0; ++y)
         for(int x = 0; x < n0; ++x)
@@ -784,7 +791,7 @@ extern "C" int tpss_c0ip_create(const tpss_c0ip_desc *d, tpss_c0ip **out)
             {
               auto at = [&](const Band1D &X, int i, int j) { return X.get(i + 1, j + 1); };
               A[(size_t)(y * n0 + x) * N0 + y2 * n0 + x2] = at(M, y, y2) * at(B, x, x2) +
-                                                            2.0 * at(Lm, y, y2) * at(Lm, x, x2) +
+                                                            c->mixed * at(Lm, y, y2) * at(Lm, x, x2) +
                                                             at(B, y, y2) * at(M, x, x2);
             }
       const auto inv = cholesky_inv(A, N0);

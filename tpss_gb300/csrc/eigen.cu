@@ -158,9 +158,11 @@ __global__ void gen_eig_kernel(int n, int n_problems, const double *__restrict__
 }  // namespace
 
 // Solves all problems; Ms/As/S/lam are host arrays of n_problems * n*n (n) doubles.
+// With `status` given, a problem whose M is not positive definite sets its entry (non-zero)
+// instead of failing the call.
 void gen_eig_batched(int n, int n_problems, const std::vector<double> &Ms,
                      const std::vector<double> &As, std::vector<double> &S,
-                     std::vector<double> &lam)
+                     std::vector<double> &lam, std::vector<int> *status)
 {
   TPSS_REQUIRE(n >= 1 && n <= kMaxN, "gen_eig_batched: 1-D size out of range");
   if(n_problems == 0)
@@ -189,6 +191,11 @@ void gen_eig_batched(int n, int n_problems, const std::vector<double> &Ms,
   TPSS_CUDA(cudaMemcpy(S.data(), dS.ptr, S.size() * sizeof(double), cudaMemcpyDeviceToHost));
   TPSS_CUDA(cudaMemcpy(lam.data(), dl.ptr, lam.size() * sizeof(double), cudaMemcpyDeviceToHost));
   TPSS_CUDA(cudaMemcpy(st.data(), dst.ptr, st.size() * sizeof(int), cudaMemcpyDeviceToHost));
+  if(status)
+  {
+    *status = st;
+    return;
+  }
   for(int i = 0; i < n_problems; ++i)
     if(st[i]) fail(TPSS_ERR_INVALID_ARGUMENT, "local mass matrix is not positive definite");
 }

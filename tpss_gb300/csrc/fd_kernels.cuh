@@ -334,8 +334,9 @@ struct KernelArgs
   const void *__restrict__ fd_eo;     // even/odd forms (nullptr: none)
   const int32_t *__restrict__ sym;    // entry is mirror-symmetric (nullptr: none)
   int eo_stride;                      // elements per even/odd entry
-  const void *__restrict__ rcp;       // reciprocal eigenvalue sums per entry combination (or nullptr)
-  int rcp_E;                          // entries per direction of the combinations
+  const void *__restrict__ rcp;       // reciprocal eigenvalue combinations (or nullptr)
+  int rcp_E;                          // > 0: tables per entry combination, E entries per
+                                      // direction; < 0: one table per patch of the range
   const unsigned char *__restrict__ keep_mask;  // RAS boolean: [class][NLOC] 1 = scatter (or nullptr)
   const int32_t *__restrict__ keep_class;       // RAS boolean: class of each patch of the range
   int ppc;                                      // patches per CTA (Cfg::ppc of the variant)
@@ -397,8 +398,11 @@ __global__ void __launch_bounds__(Cfg<T, DIM, NCP, K1>::MAX_THREADS)
     if(rcp && tid < nvalid)
     {
       int c = 0;
+      if(a.rcp_E < 0)
+        c = int(p0 + tid);  // one table per patch
+      else
 #pragma unroll
-      for(int d = DIM - 1; d >= 0; --d) c = c * a.rcp_E + a.patch_fd[(p0 + tid) * DIM + d];
+        for(int d = DIM - 1; d >= 0; --d) c = c * a.rcp_E + a.patch_fd[(p0 + tid) * DIM + d];
       s_combo[tid] = c;
     }
     if(a.keep_mask && tid < nvalid) s_cls[tid] = a.keep_class[p0 + tid];

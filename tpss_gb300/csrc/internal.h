@@ -261,6 +261,8 @@ struct FdTables
   // (e_d the entry of direction d, E = n_entries) the n^dim values 1 / (lambda_0 + .. +
   // lambda_{dim-1}) in the kernels' eigenvalue order; empty when E^dim n^dim > 4 Mi (many
   // distinct 1-D problems) or for per-patch entries, which keep the division
+  // (rcp_E = -1: one table per patch, P x n^dim values -- the product-form eigenvalue
+  // combinations 1 / (1 + prod_d mu_d) of the rank-2 Kronecker local solver)
   DeviceBuffer<double> rcp64;
   DeviceBuffer<float> rcp32;
   int rcp_E = 0;
@@ -384,7 +386,12 @@ std::vector<double> mapped_dense(const tpss_operator &op);
 // FD setup helpers (precond.cu, eigen.cu)
 void gen_eig_batched(int n, int n_problems, const std::vector<double> &Ms,
                      const std::vector<double> &As, std::vector<double> &S,
-                     std::vector<double> &lam);
+                     std::vector<double> &lam, std::vector<int> *status = nullptr);
+// rank-2 Kronecker approximations of the exact patch matrices (local.cu)
+std::vector<double> ksvd_fit(const tpss_layout &L, const tpss_operator &op, const std::vector<double> &Mp,
+                             const std::vector<double> &Ap, int iters);
+void kcp_als(int dim, const int *m, const int *n, int rank, int iters, const double *K_dev, int64_t count,
+             double *F_dev, cudaStream_t s);
 void key_matrices(const tpss_layout &L, Penalty ip, std::vector<double> &Ms, std::vector<double> &As);
 std::vector<double> per_patch(const tpss_layout &L, const std::vector<double> &keyed);
 int64_t keep_definite(const tpss_layout &L, const std::vector<double> &Mp, std::vector<double> &Ap,

@@ -154,6 +154,277 @@ __global__ void __launch_bounds__(512) gj_inverse_kernel(const double *__restric
   }
 }
 
+// The same Gauss-Jordan inversion for patches beyond shared memory (n_loc > 160, e.g. 512 for
+// 3D DGQ3 vertex patches): one CTA per patch works in place on the patch's matrix in global
+// memory (n^3 FP64 multiply-adds, setup only), then stores the inverse transposed like
+// gj_inverse_kernel (out64 / out32 at patch p0 + pp; either may be null).
+__global__ void __launch_bounds__(512) gj_inverse_global_kernel(double *__restrict__ A_all, int n, int64_t count,
+                                                                double *out64, float *out32, int64_t p0,
+                                                                int *bad)
+{
+  const int64_t pp = blockIdx.x;
+  if(pp >= count) return;
+  const int64_t nn = (int64_t)n * n;
+  double *A = A_all + pp * nn;
+  __shared__ double piv;
+  for(int k = 0; k < n; ++k)
+  {
+    if(threadIdx.x == 0)
+    {
+      piv = A[(int64_t)k * n + k];
+      if(!(piv > 0.0))
+      {
+        atomicOr(bad, 1);
+        piv = 1.0;
+      }
+    }
+    __syncthreads();
+    const double p = piv;
+    for(int j = threadIdx.x; j < n; j += blockDim.x)
+      if(j != k) A[(int64_t)k * n + j] /= p;
+    __syncthreads();
+    // rows i != k: A[i][j] -= A[i][k] A[k][j]; a warp sweeps one row, lanes the columns
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32, nw = blockDim.x / 32;
+    for(int i = warp; i < n; i += nw)
+    {
+      if(i == k) continue;
+      const double aik = A[(int64_t)i * n + k];
+      for(int j = lane; j < n; j += 32)
+        if(j != k) A[(int64_t)i * n + j] -= aik * A[(int64_t)k * n + j];
+    }
+    __syncthreads();
+    for(int i = threadIdx.x; i < n; i += blockDim.x)
+      if(i != k) A[(int64_t)i * n + k] = -A[(int64_t)i * n + k] / p;
+    if(threadIdx.x == 0) A[(int64_t)k * n + k] = 1.0 / p;
+    __syncthreads();
+  }
+  const int64_t base = (p0 + pp) * nn;
+  for(int64_t i = threadIdx.x; i < nn; i += blockDim.x)
+  {
+    const int r = int(i / n), c = int(i % n);
+    const double v = A[(int64_t)c * n + r];
+    if(out64) out64[base + i] = v;
+    if(out32) out32[base + i] = float(v);
+  }
+}
+
+// Dense local inverse of a fast-diagonalization solver, one CTA per (patch, column c):
+// column c of S diag(1 / sum_d lambda_d) S^T with S = S_(dim-1) x .. x S_0 is
+// S (D (S^T e_c)), where (S^T e_c)_t = prod_d S_d(c_d, t_d) is a product of eigenvector
+// components; the outer S is applied by sum factorization. FD entries as in the kernels' FP64
+// table: [S^T n x npad][S n x npad][lambda npad]. Output row-major, out[pp][t][c].
+struct FdInvArgs
+{
+  int dim, n, nloc, npad, es;
+  const double *fd;
+  const int32_t *patch_fd;  // entry of patch p, direction d at p * dim + d
+  const double *rcp;        // per-patch reciprocal eigenvalue combinations (P x nloc), or null:
+                            // 1 / sum_d lambda_d
+  int64_t p0, count;
+  double *out;
+};
+
+__global__ void __launch_bounds__(512) fd_local_inverse_kernel(const FdInvArgs a)
+{
+  extern __shared__ double fbuf[];
+  double *v = fbuf, *w = fbuf + a.nloc;
+  const int64_t pp = blockIdx.y;
+  const int c = blockIdx.x, n = a.n;
+  if(pp >= a.count || c >= a.nloc) return;
+  const int64_t p = a.p0 + pp;
+  const double *E[3] = {nullptr, nullptr, nullptr};
+  for(int d = 0; d < a.dim; ++d) E[d] = a.fd + (size_t)a.patch_fd[p * a.dim + d] * a.es;
+  int cd[3] = {0, 0, 0};
+  for(int d = 0, rem = c; d < a.dim; ++d, rem /= n) cd[d] = rem % n;
+  for(int t = threadIdx.x; t < a.nloc; t += blockDim.x)
+  {
+    double prod = 1.0, lsum = 0.0;
+    for(int d = 0, rem = t; d < a.dim; ++d, rem /= n)
+    {
+      const int td = rem % n;
+      prod *= E[d][a.n * a.npad + cd[d] * a.npad + td];  // S_d(c_d, t_d): S rows
+      lsum += E[d][2 * a.n * a.npad + td];
+    }
+    v[t] = a.rcp ? prod * a.rcp[p * a.nloc + t] : prod / lsum;
+  }
+  __syncthreads();
+  int stride = 1;
+  for(int d = 0; d < a.dim; ++d)
+  {
+    for(int t = threadIdx.x; t < a.nloc; t += blockDim.x)
+    {
+      const int td = (t / stride) % n, base = t - td * stride;
+      const double *row = E[d] + a.n * a.npad + td * a.npad;  // S_d(t_d, m)
+      double s = 0.0;
+      for(int m = 0; m < n; ++m) s += row[m] * v[base + m * stride];
+      w[t] = s;
+    }
+    __syncthreads();
+    double *x = v;
+    v = w;
+    w = x;
+    stride *= n;
+  }
+  for(int t = threadIdx.x; t < a.nloc; t += blockDim.x)
+    a.out[pp * (int64_t)a.nloc * a.nloc + (int64_t)t * a.nloc + c] = v[t];
+}
+
+// Low Kronecker-rank approximation by alternating least squares (the CP/ALS of compute_kcp,
+// kroneckersvd.h:501-585; for two factors its fixed point is the truncated SVD of the
+// reshuffled matrix that compute_ksvd, kroneckersvd.h:306-402, computes by Lanczos):
+//   K ~ sum_r F_{dim-1,r} x ... x F_{0,r},  F_{d,r} of size m_d x n_d,
+// K of size (prod m_d) x (prod n_d) with direction 0 fastest in rows and columns. With the
+// reshuffled tensor T(a_0, .., a_{dim-1}), a_d = i_d n_d + j_d, a mode-d update is
+//   F_d = T_(d) (khatri-rao of the other factors) V^-1,  V = hadamard_{e != d} F_e^T F_e,
+// (r x r, inverted directly for r <= 2 with a pseudo-inverse fallback), `iters` sweeps over
+// d = 0 .. dim-1 from the given initial factors. One CTA per matrix; the products of the other
+// modes' factors are tabulated in shared memory.
+struct KcpArgs
+{
+  int dim, rank, iters;
+  int m[3], n[3];
+  const double *K;   // count * rows * cols
+  double *F;         // count * sum_d rank m_d n_d (in: initial factors, out: result)
+  int64_t count;
+  int prod_max;      // max over d of prod_{e != d} m_e n_e
+};
+
+__global__ void __launch_bounds__(256) kcp_als_kernel(const KcpArgs a)
+{
+  extern __shared__ double ks[];
+  const int64_t pp = blockIdx.x;
+  if(pp >= a.count) return;
+  const int dim = a.dim, R = a.rank;
+  int sz[3] = {1, 1, 1}, off[3] = {0, 0, 0}, total = 0;
+  for(int d = 0; d < dim; ++d)
+  {
+    sz[d] = a.m[d] * a.n[d];
+    off[d] = total;
+    total += R * sz[d];
+  }
+  int rows = 1, cols = 1;
+  for(int d = 0; d < dim; ++d)
+  {
+    rows *= a.m[d];
+    cols *= a.n[d];
+  }
+  const double *K = a.K + pp * (int64_t)rows * cols;
+  double *F = ks;                     // total
+  double *Pt = F + total;             // prod_max * R
+  double *V = Pt + (size_t)a.prod_max * R;  // R * R and its inverse
+  double *Vi = V + 16;
+  for(int i = threadIdx.x; i < total; i += blockDim.x) F[i] = a.F[pp * total + i];
+  __syncthreads();
+  for(int it = 0; it < a.iters; ++it)
+    for(int d = 0; d < dim; ++d)
+    {
+      // other modes e1 (< e2) and the product table Pt[(ae1 + sz[e1] ae2) R + r]
+      int e[2] = {-1, -1}, ne = 0;
+      for(int x = 0; x < dim; ++x)
+        if(x != d) e[ne++] = x;
+      const int s1 = sz[e[0]], s2 = ne > 1 ? sz[e[1]] : 1;
+      for(int idx = threadIdx.x; idx < s1 * s2 * R; idx += blockDim.x)
+      {
+        const int r = idx % R, q = idx / R, a1 = q % s1, a2 = q / s1;
+        double v = F[off[e[0]] + r * s1 + a1];
+        if(ne > 1) v *= F[off[e[1]] + r * s2 + a2];
+        Pt[idx] = v;
+      }
+      if(threadIdx.x < R * R)
+      {
+        const int r1 = threadIdx.x / R, r2 = threadIdx.x % R;
+        double h = 1.0;
+        for(int x = 0; x < ne; ++x)
+        {
+          double g = 0.0;
+          for(int i = 0; i < sz[e[x]]; ++i) g += F[off[e[x]] + r1 * sz[e[x]] + i] * F[off[e[x]] + r2 * sz[e[x]] + i];
+          h *= g;
+        }
+        V[threadIdx.x] = h;
+      }
+      __syncthreads();
+      if(threadIdx.x == 0)
+      {
+        // inverse of V (R <= 2 directly; singular or larger: diagonal pseudo-inverse)
+        if(R == 1)
+          Vi[0] = V[0] != 0.0 ? 1.0 / V[0] : 0.0;
+        else if(R == 2 && fabs(V[0] * V[3] - V[1] * V[2]) > 1e-14 * fabs(V[0] * V[3]))
+        {
+          const double det = V[0] * V[3] - V[1] * V[2];
+          Vi[0] = V[3] / det;
+          Vi[1] = -V[1] / det;
+          Vi[2] = -V[2] / det;
+          Vi[3] = V[0] / det;
+        }
+        else
+          for(int r1 = 0; r1 < R; ++r1)
+            for(int r2 = 0; r2 < R; ++r2) Vi[r1 * R + r2] = (r1 == r2 && V[r1 * R + r1] != 0.0) ? 1.0 / V[r1 * R + r1] : 0.0;
+      }
+      __syncthreads();
+      // G(a_d, r) = sum over the other modes of T(a) Pt; F_d = G Vi
+      const int sd = sz[d];
+      for(int ad = threadIdx.x; ad < sd; ad += blockDim.x)
+      {
+        double g[4] = {0.0, 0.0, 0.0, 0.0};
+        const int id = ad / a.n[d], jd = ad % a.n[d];
+        for(int q = 0; q < s1 * s2; ++q)
+        {
+          int ai[3], row = 0, col = 0, rs = 1, cs = 1;
+          ai[d] = 0;
+          ai[e[0]] = q % s1;
+          if(ne > 1) ai[e[1]] = q / s1;
+          for(int x = 0; x < dim; ++x)
+          {
+            const int i = x == d ? id : ai[x] / a.n[x], j = x == d ? jd : ai[x] % a.n[x];
+            row += i * rs;
+            col += j * cs;
+            rs *= a.m[x];
+            cs *= a.n[x];
+          }
+          const double t = K[(int64_t)row * cols + col];
+          for(int r = 0; r < R; ++r) g[r] += t * Pt[q * R + r];
+        }
+        for(int r = 0; r < R; ++r)
+        {
+          double v = 0.0;
+          for(int r2 = 0; r2 < R; ++r2) v += g[r2] * Vi[r2 * R + r];
+          F[off[d] + r * sd + ad] = v;
+        }
+      }
+      __syncthreads();
+    }
+  for(int i = threadIdx.x; i < total; i += blockDim.x) a.F[pp * total + i] = F[i];
+}
+
+// err[pp] = ||X_pp - Y_pp||_F / ||Y_pp||_F for count pairs of n x n matrices (one CTA each)
+__global__ void __launch_bounds__(256) frob_error_kernel(const double *__restrict__ X, const double *__restrict__ Y,
+                                                         int64_t nn, int64_t count, double *err)
+{
+  __shared__ double sd[256], sy[256];
+  const int64_t pp = blockIdx.x;
+  if(pp >= count) return;
+  double a = 0.0, b = 0.0;
+  for(int64_t i = threadIdx.x; i < nn; i += blockDim.x)
+  {
+    const double y = Y[pp * nn + i], d = X[pp * nn + i] - y;
+    a += d * d;
+    b += y * y;
+  }
+  sd[threadIdx.x] = a;
+  sy[threadIdx.x] = b;
+  __syncthreads();
+  for(int s = 128; s > 0; s >>= 1)
+  {
+    if(threadIdx.x < s)
+    {
+      sd[threadIdx.x] += sd[threadIdx.x + s];
+      sy[threadIdx.x] += sy[threadIdx.x + s];
+    }
+    __syncthreads();
+  }
+  if(threadIdx.x == 0) err[pp] = sqrt(sd[0] / sy[0]);
+}
+
 struct DenseArgs
 {
   LocalMap m;
@@ -362,8 +633,9 @@ void build_dense_inverses(const tpss_layout &L, const tpss_operator &op, bool fp
                           DeviceBuffer<double> &inv64, DeviceBuffer<float> &inv32)
 {
   check_exact_local(L, &op);
-  TPSS_REQUIRE(L.nloc <= 160, "dense local inverses are limited to patches of at most 160 DoFs");
+  TPSS_REQUIRE(L.nloc <= 4096, "dense local inverses are limited to patches of at most 4096 DoFs");
   const int64_t nn = (int64_t)L.nloc * L.nloc;
+  TPSS_REQUIRE(L.P <= ((int64_t)1 << 62) / nn, "too many patch matrix entries");
   if(fp32)
     inv32.resize((size_t)(L.P * nn));
   else
@@ -374,14 +646,22 @@ void build_dense_inverses(const tpss_layout &L, const tpss_operator &op, bool fp
   DeviceBuffer<double> K((size_t)(B * nn));
   DeviceBuffer<int> bad(1);
   TPSS_CUDA(cudaMemset(bad.ptr, 0, sizeof(int)));
+  // up to 160 DoFs the matrix lives in shared memory; larger patches are inverted in place in
+  // global memory
+  const bool in_smem = L.nloc <= 160;
   const size_t smem = sizeof(double) * nn;
-  TPSS_CUDA(cudaFuncSetAttribute(gj_inverse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  if(in_smem)
+    TPSS_CUDA(cudaFuncSetAttribute(gj_inverse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   for(int64_t p0 = 0; p0 < L.P; p0 += B)
   {
     const int64_t cnt = std::min(B, L.P - p0);
     extract_batch(L, op, p0, cnt, lower, K.ptr);
-    gj_inverse_kernel<<<(unsigned)cnt, 512, smem>>>(K.ptr, L.nloc, cnt, fp32 ? nullptr : inv64.ptr,
-                                                   fp32 ? inv32.ptr : nullptr, p0, bad.ptr);
+    if(in_smem)
+      gj_inverse_kernel<<<(unsigned)cnt, 512, smem>>>(K.ptr, L.nloc, cnt, fp32 ? nullptr : inv64.ptr,
+                                                     fp32 ? inv32.ptr : nullptr, p0, bad.ptr);
+    else
+      gj_inverse_global_kernel<<<(unsigned)cnt, 512>>>(K.ptr, L.nloc, cnt, fp32 ? nullptr : inv64.ptr,
+                                                      fp32 ? inv32.ptr : nullptr, p0, bad.ptr);
     TPSS_CUDA(cudaGetLastError());
   }
   int h = 0;
@@ -456,7 +736,200 @@ void extract_local_matrices(const tpss_layout &L, const tpss_operator &op, int64
   lower.upload(L.lower.data(), L.lower.size());
   if(count) extract_batch(L, op, p0, count, lower, out_dev);
 }
+
+namespace
+{
+__global__ void transpose_copy_kernel(const double *in64, const float *in32, int n, int64_t count, double *out)
+{
+  const int64_t nn = (int64_t)n * n;
+  for(int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count * nn; i += (int64_t)gridDim.x * blockDim.x)
+  {
+    const int64_t pp = i / nn, rc = i % nn, r = rc / n, c = rc % n;
+    const int64_t src = pp * nn + c * n + r;
+    out[i] = in64 ? in64[src] : double(in32[src]);
+  }
+}
+}  // namespace
+
+// Dense local inverses of patches [p0, p0 + count) as the preconditioner applies them
+// (row-major, device FP64): the stored exact inverses, or S D S^T of the FD tables.
+void precond_local_inverse(const tpss_precond &p, int64_t p0, int64_t count, double *out_dev)
+{
+  const FdTables &T = *p.tables;
+  const tpss_layout &L = *T.layout;
+  TPSS_REQUIRE(p0 >= 0 && count >= 0 && p0 + count <= L.P, "patch range out of bounds");
+  if(count == 0) return;
+  const int64_t nn = (int64_t)L.nloc * L.nloc;
+  if(T.dense)
+  {
+    const double *in64 = T.dense64.n ? T.dense64.ptr + p0 * nn : nullptr;
+    const float *in32 = T.dense64.n ? nullptr : T.dense32.ptr + p0 * nn;
+    transpose_copy_kernel<<<(unsigned)std::min<int64_t>((count * nn + 255) / 256, 65535), 256>>>(
+      in64, in32, L.nloc, count, out_dev);
+    TPSS_CUDA(cudaGetLastError());
+    return;
+  }
+  TPSS_REQUIRE(L.nloc <= 4096, "local inverses: at most 4096 DoFs per patch");
+  FdInvArgs a;
+  a.dim = L.dim;
+  a.n = L.n;
+  a.nloc = L.nloc;
+  a.npad = T.npad64;
+  a.es = (2 * L.n + 1) * T.npad64;
+  a.fd = T.fd64.ptr;
+  a.patch_fd = T.own_fd.n ? T.own_fd.ptr : L.d_patch_fd.ptr;
+  a.rcp = T.rcp_E < 0 ? T.rcp64.ptr : nullptr;
+  const size_t smem = 2 * sizeof(double) * L.nloc;
+  TPSS_CUDA(cudaFuncSetAttribute(fd_local_inverse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  for(int64_t q = 0; q < count; q += 65535)
+  {
+    a.p0 = p0 + q;
+    a.count = std::min<int64_t>(65535, count - q);
+    a.out = out_dev + q * nn;
+    fd_local_inverse_kernel<<<dim3((unsigned)L.nloc, (unsigned)a.count), 256, smem>>>(a);
+    TPSS_CUDA(cudaGetLastError());
+  }
+}
+
+// err[i] = ||A_j^-1 - B_j||_F / ||A_j^-1||_F for the patches j = p0 + i, A_j the exact patch
+// matrix of the mapped level operator (inverted in FP64) and B_j the preconditioner's local
+// inverse
+void local_inverse_error(const tpss_precond &p, const tpss_operator &op, int64_t p0, int64_t count,
+                         double *err_host)
+{
+  const tpss_layout &L = *p.tables->layout;
+  check_exact_local(L, &op);
+  TPSS_REQUIRE(p0 >= 0 && count >= 0 && p0 + count <= L.P, "patch range out of bounds");
+  if(count == 0) return;
+  const int64_t nn = (int64_t)L.nloc * L.nloc;
+  const int64_t B = std::max<int64_t>(1, std::min<int64_t>(count, ((int64_t)1 << 29) / (nn * 8)));
+  DeviceBuffer<int32_t> lower;
+  lower.upload(L.lower.data(), L.lower.size());
+  DeviceBuffer<double> K((size_t)(B * nn)), Ainv((size_t)(B * nn)), Bj((size_t)(B * nn)), err((size_t)B);
+  DeviceBuffer<int> bad(1);
+  TPSS_CUDA(cudaMemset(bad.ptr, 0, sizeof(int)));
+  for(int64_t q = 0; q < count; q += B)
+  {
+    const int64_t cnt = std::min(B, count - q);
+    extract_batch(L, op, p0 + q, cnt, lower, K.ptr);
+    // the inverse kernels write patch p0' + pp at (p0' + pp) nn: pass p0' = 0 into Ainv
+    gj_inverse_global_kernel<<<(unsigned)cnt, 512>>>(K.ptr, L.nloc, cnt, Ainv.ptr, nullptr, 0, bad.ptr);
+    TPSS_CUDA(cudaGetLastError());
+    // gj stores the inverse transposed; the inverse of a symmetric matrix is symmetric
+    precond_local_inverse(p, p0 + q, cnt, Bj.ptr);
+    frob_error_kernel<<<(unsigned)cnt, 256>>>(Bj.ptr, Ainv.ptr, nn, cnt, err.ptr);
+    TPSS_CUDA(cudaGetLastError());
+    TPSS_CUDA(cudaMemcpy(err_host + q, err.ptr, sizeof(double) * cnt, cudaMemcpyDeviceToHost));
+  }
+  int h = 0;
+  TPSS_CUDA(cudaMemcpy(&h, bad.ptr, sizeof(int), cudaMemcpyDeviceToHost));
+  if(h) fail(TPSS_ERR_INVALID_ARGUMENT, "a local patch matrix is not positive definite");
+}
 }  // namespace tpss
+
+namespace tpss
+{
+void kcp_als(int dim, const int *m, const int *n, int rank, int iters, const double *K_dev, int64_t count,
+             double *F_dev, cudaStream_t s)
+{
+  TPSS_REQUIRE(dim >= 2 && dim <= 3, "Kronecker approximation: 2 or 3 factors");
+  TPSS_REQUIRE(rank >= 1 && rank <= 4, "Kronecker approximation: rank 1..4");
+  TPSS_REQUIRE(iters >= 0, "Kronecker approximation: iterations >= 0");
+  KcpArgs a;
+  a.dim = dim;
+  a.rank = rank;
+  a.iters = iters;
+  int total = 0;
+  for(int d = 0; d < 3; ++d)
+  {
+    a.m[d] = d < dim ? m[d] : 1;
+    a.n[d] = d < dim ? n[d] : 1;
+    TPSS_REQUIRE(a.m[d] >= 1 && a.n[d] >= 1 && a.m[d] <= 64 && a.n[d] <= 64, "Kronecker approximation: factor size");
+    if(d < dim) total += rank * a.m[d] * a.n[d];
+  }
+  a.prod_max = 1;
+  for(int d = 0; d < dim; ++d)
+  {
+    int p = 1;
+    for(int e = 0; e < dim; ++e)
+      if(e != d) p *= a.m[e] * a.n[e];
+    a.prod_max = std::max(a.prod_max, p);
+  }
+  const size_t smem = sizeof(double) * ((size_t)total + (size_t)a.prod_max * rank + 32);
+  TPSS_REQUIRE(smem <= 200 * 1024, "Kronecker approximation: factors too large for shared memory");
+  a.K = K_dev;
+  a.F = F_dev;
+  a.count = count;
+  if(count == 0) return;
+  TPSS_CUDA(cudaFuncSetAttribute(kcp_als_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  kcp_als_kernel<<<(unsigned)count, 256, smem, s>>>(a);
+  TPSS_CUDA(cudaGetLastError());
+}
+
+// Rank-2 Kronecker approximation of every exact patch matrix of a mapped level, initialised
+// from the patch's surrogate 1-D problems: term 0 = (A_0, M_1[, M_2]), term 1 = (M_0, A_1[, M_2])
+// (the Cartesian 2D patch matrix M_1 x A_0 + A_1 x M_0 is reproduced exactly); `iters` ALS
+// sweeps. Returns P x dim x 2 x n^2 (direction d, term r at (p dim + d) 2 n^2 + r n^2).
+std::vector<double> ksvd_fit(const tpss_layout &L, const tpss_operator &op, const std::vector<double> &Mp,
+                             const std::vector<double> &Ap, int iters)
+{
+  check_exact_local(L, &op);
+  const int n = L.n, n2 = n * n, dim = L.dim;
+  const int64_t nn = (int64_t)L.nloc * L.nloc;
+  DeviceBuffer<int32_t> lower;
+  lower.upload(L.lower.data(), L.lower.size());
+  const int64_t B = batch_patches(L);
+  DeviceBuffer<double> K((size_t)(B * nn)), F((size_t)(B * dim * 2 * n2));
+  // kernel layout per patch: direction d block of 2 terms (rank r at d 2 n2 + r n2)
+  std::vector<double> out((size_t)L.P * dim * 2 * n2), init((size_t)B * dim * 2 * n2);
+  const int mm[3] = {n, n, n};
+  for(int64_t p0 = 0; p0 < L.P; p0 += B)
+  {
+    const int64_t cnt = std::min(B, L.P - p0);
+    for(int64_t q = 0; q < cnt; ++q)
+      for(int d = 0; d < dim; ++d)
+        for(int r = 0; r < 2; ++r)
+        {
+          const bool lap = (r == 0 && d == 0) || (r == 1 && d == 1);
+          const double *src = &(lap ? Ap : Mp)[((size_t)(p0 + q) * dim + d) * n2];
+          std::copy(src, src + n2, &init[(((size_t)q * dim + d) * 2 + r) * n2]);
+        }
+    TPSS_CUDA(cudaMemcpy(F.ptr, init.data(), sizeof(double) * cnt * dim * 2 * n2, cudaMemcpyHostToDevice));
+    extract_batch(L, op, p0, cnt, lower, K.ptr);
+    kcp_als(dim, mm, mm, 2, iters, K.ptr, cnt, F.ptr, nullptr);
+    TPSS_CUDA(cudaMemcpy(&out[(size_t)p0 * dim * 2 * n2], F.ptr, sizeof(double) * cnt * dim * 2 * n2,
+                         cudaMemcpyDeviceToHost));
+  }
+  return out;
+}
+}  // namespace tpss
+
+extern "C" int tpss_kronecker_approx(const double *mats, int64_t count, int dim, const int *m, const int *n,
+                                     int rank, int iterations, double *factors, void *stream)
+{
+  return tpss::guarded([&] {
+    TPSS_REQUIRE(mats && factors && m && n && count >= 0, "invalid argument");
+    tpss::kcp_als(dim, m, n, rank, iterations, mats, count, factors, tpss::as_stream(stream));
+  });
+}
+
+extern "C" int tpss_precond_local_inverse(const tpss_precond *p, int64_t first, int64_t count, double *out)
+{
+  return tpss::guarded([&] {
+    TPSS_REQUIRE(p && out, "null argument");
+    tpss::precond_local_inverse(*p, first, count, out);
+    TPSS_CUDA(cudaDeviceSynchronize());
+  });
+}
+
+extern "C" int tpss_local_inverse_error(const tpss_precond *p, const tpss_operator *op, int64_t first,
+                                        int64_t count, double *err)
+{
+  return tpss::guarded([&] {
+    TPSS_REQUIRE(p && op && err, "null argument");
+    tpss::local_inverse_error(*p, *op, first, count, err);
+  });
+}
 
 using namespace tpss;
 

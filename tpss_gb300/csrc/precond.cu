@@ -16,9 +16,6 @@
 
 namespace tpss
 {
-void gen_eig_batched(int n, int n_problems, const std::vector<double> &Ms,
-                     const std::vector<double> &As, std::vector<double> &S,
-                     std::vector<double> &lam);
 
 namespace
 {
@@ -327,6 +324,104 @@ std::shared_ptr<FdTables> build_local_solvers(const tpss_layout &L, const tpss_o
     return build_learned_tables(L, d, [&](const std::vector<double> *Mp, const std::vector<double> *Ap) {
       return build_tables(L, pen, ras, Mp, Ap);
     });
+  case TPSS_LOCAL_KSVD:
+  {
+    // Rank-2 Kronecker approximation X = F_(D-1),0 x .. x F_0,0 + F_(D-1),1 x .. x F_0,1 of the
+    // exact patch matrix (ksvd_fit), inverted by simultaneous diagonalization of the two terms:
+    // S_d^T F_d,0 S_d = I, S_d^T F_d,1 S_d = diag(mu_d) gives
+    // X^-1 = S diag(1 / (1 + prod_d mu_d)) S^T, S = S_(D-1) x .. x S_0 -- fast diagonalization
+    // with product-form eigenvalue combinations, which the kernels read from per-patch
+    // reciprocal tables. A patch whose fit is not safely positive definite keeps its surrogate.
+    check_exact_local(L, op);
+    auto t0 = std::chrono::steady_clock::now();
+    const int n = L.n, nn = n * n, dim = L.dim, nloc = L.nloc;
+    std::vector<double> Mk, Ak;
+    key_matrices(L, pen, Mk, Ak);
+    const std::vector<double> Msur = per_patch(L, Mk), Asur = per_patch(L, Ak);
+    const std::vector<double> F = ksvd_fit(L, *op, Msur, Asur, 14);  // rank^2 + 10 sweeps (compute_kcp)
+    std::vector<double> F0((size_t)L.P * dim * nn), F1((size_t)L.P * dim * nn);
+    for(int64_t p = 0; p < L.P; ++p)
+      for(int dd = 0; dd < dim; ++dd)
+      {
+        const double *f = &F[((size_t)p * dim + dd) * 2 * nn];
+        double *g0 = &F0[((size_t)p * dim + dd) * nn], *g1 = &F1[((size_t)p * dim + dd) * nn];
+        double tr = 0.0;
+        for(int i = 0; i < n; ++i) tr += f[i * n + i];
+        const double sg = tr < 0.0 ? -1.0 : 1.0;  // sign pairs of term 0 so that every factor is positive
+        for(int i = 0; i < n; ++i)
+          for(int j = 0; j < n; ++j)
+          {
+            g0[i * n + j] = sg * 0.5 * (f[i * n + j] + f[j * n + i]);
+            g1[i * n + j] = 0.5 * (f[nn + i * n + j] + f[nn + j * n + i]);
+          }
+      }
+    std::vector<double> S, mu;
+    std::vector<int> status;
+    gen_eig_batched(n, (int)(L.P * dim), F0, F1, S, mu, &status);
+    std::vector<char> use_ksvd((size_t)L.P, 1);
+    for(int64_t p = 0; p < L.P; ++p)
+    {
+      // term 0 positive definite in every direction (after the sign flips, which must pair up)
+      // and 1 + prod mu clearly positive
+      for(int dd = 0; dd < dim; ++dd)
+        if(status[(size_t)p * dim + dd]) use_ksvd[p] = 0;
+      if(!use_ksvd[p]) continue;
+      int flips = 0;
+      for(int dd = 0; dd < dim; ++dd)
+      {
+        const double *f = &F[((size_t)p * dim + dd) * 2 * nn];
+        double tr = 0.0;
+        for(int i = 0; i < n; ++i) tr += f[i * n + i];
+        flips += tr < 0.0;
+      }
+      double lo = 1e300, hi = 0.0;
+      bool ok = flips % 2 == 0;
+      for(int i = 0; i < nloc && ok; ++i)
+      {
+        double prod = 1.0;
+        for(int dd = 0, rem = i; dd < dim; ++dd, rem /= n) prod *= mu[((size_t)p * dim + dd) * n + rem % n];
+        const double v = 1.0 + prod;
+        ok = std::isfinite(v);
+        lo = std::min(lo, v);
+        hi = std::max(hi, v);
+      }
+      use_ksvd[p] = ok && lo > 1e-3 * hi;
+    }
+    std::vector<double> Mp(F0), Ap(F1);
+    int64_t kept = 0;
+    for(int64_t p = 0; p < L.P; ++p)
+      if(!use_ksvd[p])
+      {
+        ++kept;
+        std::copy_n(&Msur[(size_t)p * dim * nn], (size_t)dim * nn, &Mp[(size_t)p * dim * nn]);
+        std::copy_n(&Asur[(size_t)p * dim * nn], (size_t)dim * nn, &Ap[(size_t)p * dim * nn]);
+      }
+    auto T = build_tables(L, pen, ras, &Mp, &Ap);
+    // per-patch reciprocal eigenvalue combinations: product form for the fitted patches, the
+    // Kronecker sum for the surrogate ones
+    std::vector<double> r64((size_t)L.P * nloc);
+    std::vector<float> r32(r64.size());
+    for(int64_t p = 0; p < L.P; ++p)
+      for(int i = 0; i < nloc; ++i)
+      {
+        double prod = 1.0, lsum = 0.0;
+        for(int dd = 0, rem = i; dd < dim; ++dd, rem /= n)
+        {
+          const double l = T->lam_host[((size_t)p * dim + dd) * n + rem % n];
+          prod *= l;
+          lsum += l;
+        }
+        const double v = use_ksvd[p] ? 1.0 / (1.0 + prod) : 1.0 / lsum;
+        r64[(size_t)p * nloc + i] = v;
+        r32[(size_t)p * nloc + i] = float(v);
+      }
+    T->rcp64.upload(r64.data(), r64.size());
+    T->rcp32.upload(r32.data(), r32.size());
+    T->rcp_E = -1;  // one table per patch
+    T->learned_fallbacks = kept;
+    T->setup_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    return T;
+  }
   default:
     return build_tables(L, pen, ras);
   }
@@ -341,7 +436,7 @@ void validate_desc(const tpss_precond_desc &d)
   TPSS_REQUIRE(d.precision == TPSS_FP64 || d.precision == TPSS_FP32, "invalid precision");
   TPSS_REQUIRE(d.penalty_mode == TPSS_PENALTY_REFERENCE || d.penalty_mode == TPSS_PENALTY_2KP1SQ,
                "invalid penalty_mode");
-  TPSS_REQUIRE(d.local_solver >= TPSS_LOCAL_FD && d.local_solver <= TPSS_LOCAL_LEARNED,
+  TPSS_REQUIRE(d.local_solver >= TPSS_LOCAL_FD && d.local_solver <= TPSS_LOCAL_KSVD,
                "invalid local solver");
   if(d.local_solver == TPSS_LOCAL_EXACT && d.use_ras_weights)
     fail(TPSS_ERR_NOT_IMPLEMENTED, "RAS weights are implemented for the FD local solvers");
@@ -548,12 +643,14 @@ void apply_color(tpss_precond *p, int color, double *dst, const double *src, cud
   const bool eo = p->tables->has_eo && !p->tables->own_fd.n;
   const int h = L.n / 2;
   a.sym = eo ? p->tables->sym.ptr : nullptr;
-  // reciprocal eigenvalue sums (keyed tables of few distinct 1-D problems)
-  const bool rcp = p->tables->rcp_E > 0 && !p->tables->own_fd.n;
+  // reciprocal eigenvalue combinations: per combination of keyed entries (rcp_E > 0) or per
+  // patch (rcp_E < 0, the first patch of the color at offset b)
+  const bool rcp = p->tables->rcp_E != 0;
+  const int64_t rcp_off = p->tables->rcp_E < 0 ? b * (int64_t)L.nloc : 0;
   a.rcp_E = p->tables->rcp_E;
   if(p->desc.precision == TPSS_FP32)
   {
-    a.rcp = rcp ? (const void *)p->tables->rcp32.ptr : nullptr;
+    a.rcp = rcp ? (const void *)(p->tables->rcp32.ptr + rcp_off) : nullptr;
     a.fd = p->tables->fd32.ptr;
     a.entry_stride = (2 * L.n + 1) * p->tables->npad32;
     a.fd_eo = eo ? (const void *)p->tables->fd32_eo.ptr : nullptr;
@@ -562,7 +659,7 @@ void apply_color(tpss_precond *p, int color, double *dst, const double *src, cud
   }
   else
   {
-    a.rcp = rcp ? (const void *)p->tables->rcp64.ptr : nullptr;
+    a.rcp = rcp ? (const void *)(p->tables->rcp64.ptr + rcp_off) : nullptr;
     a.fd = p->tables->fd64.ptr;
     a.entry_stride = (2 * L.n + 1) * p->tables->npad64;
     a.fd_eo = eo ? (const void *)p->tables->fd64_eo.ptr : nullptr;
