@@ -60,6 +60,10 @@ def parse():
     ap.add_argument("--level-kernels", action="store_true",
                     help="time only the level operator (FP64, FP32) and the transfers on the "
                          "--cells level (also the command the operator profile captures)")
+    ap.add_argument("--precision-sweep", action="store_true",
+                    help="only the CG + V-cycle solve of the --cells level with FP32 smoothers on all "
+                         "levels but one, which computes in FP64 (each level in turn), next to "
+                         "all-FP32 and all-FP64: iterations and seconds, one JSON line")
     ap.add_argument("--no-dgq3-2d", action="store_true",
                     help="skip the 2D SIPG DGQ3 64^2 section (both penalty modes)")
     ap.add_argument("--profile-case", choices=["bsr", "c0ip", "mlp", "host"],
@@ -173,15 +177,18 @@ def measured_peaks():
 
 
 def ncu_traffic(dim, k):
-    """DRAM bytes per launch of the streamed kernel at 64^3 cells from the committed ncu summary."""
+    """DRAM bytes per vmult of the streamed kernel plus its fix-up pass at 64^3 cells, from the
+    committed ncu summary (each captured on its own at 48^3 and scaled by DoFs)."""
     path = os.path.join(ROOT, "profiles", f"stream_kernel_{dim}d_k{k}_48cubed.md")
     if not os.path.exists(path):
         return None
+    total, found = 0.0, False
     for line in open(path):
-        m = re.match(r"\s*dram_bytes_per_launch_full_size:\s*([0-9.eE+]+)", line)
+        m = re.match(r"\s*(fixup_)?dram_bytes_per_launch_full_size:\s*([0-9.eE+]+)", line)
         if m:
-            return float(m.group(1))
-    return None
+            total += float(m.group(2))
+            found = True
+    return total if found else None
 
 
 def cpu_baseline(args, W):
@@ -356,15 +363,21 @@ def run_ours(args):
     roofline = {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
                 "frac": achieved_gbs / hbm_peak, "traffic": traffic,
                 "peak_source": f"{hbm_kind} (MEASURED_PEAKS.json hbm_gbs)",
-                "kernel": (f"stream_kernel<SCfg<{k + 1},{VARIANT_SHAPES[tuned]}>> + fixup_kernel" if streamed
+                "kernel": (f"stream_kernel<SCfg<{k + 1},{VARIANT_SHAPES[tuned]}>> + fixup_list_kernel" if streamed
                            else f"schwarz_color_kernel<{args.precision},3,2,{k + 1}>"),
                 "per_launch_ms": per_launch * 1e3,
                 "algorithmic_bytes_per_launch": bytes_launch,
+                "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum of stream_kernel and of "
+                                   "fixup_list_kernel, each captured at 48^3 and scaled by DoFs "
+                                   "(profiles/stream_kernel_3d_k4_48cubed.md)") if traffic is not None else None,
                 "binding": "fp32 FMA pipe (CUDA cores)" if prec == tpss.Precision.fp32 else "fp64 FMA pipe",
                 "compute": {"achieved": achieved_tf, "peak": fma_peak / 1e12, "unit": "TFLOP/s",
                             "frac": achieved_tf * 1e12 / fma_peak,
                             "peak_source": "measured in this run (tpss_diag_fma_peak)",
-                            "algorithmic_flops_per_launch": flops_launch}}
+                            "algorithmic_flops_per_launch": flops_launch,
+                            "executed_flops_per_launch": executed_fd_flops(n, k, dim) if dim == 3 else None,
+                            "executed_frac": (executed_fd_flops(n, k, dim) / per_launch / fma_peak
+                                              if dim == 3 else None)}}
 
     out = {"metric": METRIC, "value": value, "unit": "DoF/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": t_max, "higher_is_better": True, "scaling": "weak",
@@ -845,6 +858,37 @@ def level_kernels(args):
     print(json.dumps(out))
 
 
+def precision_sweep(args):
+    """Where the FP32 smoothers' extra CG iterations come from: the solve of solve_times (one root
+    cell, dense coarse solve, graphs) with FP32 smoothers everywhere, FP64 everywhere, and FP32
+    except one level l (l = 1 .. L) that computes in FP64."""
+    import numpy as np
+    import torch
+    import tpss_gb300 as tpss
+    n, k, dim = args.cells, args.degree, args.dim
+    N = n ** dim * (k + 1) ** dim
+    f = torch.tensor(philox_src(N, args.seed), dtype=torch.float64, device="cuda")
+    nl = n.bit_length()  # levels 0 .. L with 1, 2, .., n cells per direction
+    cases = [("all_fp32", tpss.Precision.fp32, 0), ("all_fp64", tpss.Precision.fp64, 0)]
+    cases += [(f"fp64_level_{l}", tpss.Precision.fp32, 1 << l) for l in range(1, nl)]
+    out = {"workload": f"CG + V-cycle, 3D SIPG DGQ{k} {n}^3, f ~ U[-1,1] seed {args.seed}, damping "
+                       f"{args.omega}, to 1e-8; level 0 is the coarse level (dense solve)"}
+    for name, prec, mask in cases:
+        mg = tpss.MultigridSolver(dim, k, 1, n, relaxation=args.omega, precision=prec, coarse_solver=1,
+                                  use_graph=True, fp64_level_mask=mask)
+        u = torch.zeros_like(f)
+        mg.vmult(u, f)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        it, hist = mg.solve(u, f, rel_tol=1e-8)
+        torch.cuda.synchronize()
+        out[name] = {"iterations": it, "seconds": time.perf_counter() - t0,
+                     "residual_1e-4_at": int(np.argmax(hist / hist[0] < 1e-4)),
+                     "final_rel_residual": float(hist[-1] / hist[0])}
+        del mg
+    print(json.dumps(out))
+
+
 def profile_case(args):
     """One small workload of a secondary kernel, run three times (--profile-case)."""
     import torch
@@ -894,6 +938,8 @@ def main():
         raise SystemExit("need --steps >= 1 and --warmup >= 3")
     if args.profile_case:
         profile_case(args)
+    elif args.precision_sweep:
+        precision_sweep(args)
     elif args.level_kernels:
         level_kernels(args)
     elif args.impl == "reference":

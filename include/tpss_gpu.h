@@ -314,6 +314,8 @@ typedef struct tpss_mg_desc
                                   operator and the coarse solve stay FP64 (no counterpart in the
                                   reference, whose multigrid runs in the vector precision) */
   int penalty_mode;            /* TPSS_PENALTY_* of every level's operator and local solvers */
+  int fp64_level_mask;         /* bit l set: the smoother of level l computes in FP64 whatever
+                                  `precision` says (a mixed-precision hierarchy; 0 = none) */
   int autotune;                /* 1: every level's smoother kernel decomposition is chosen by the
                                   autotuner (tpss_precond_autotune) at setup; levels of a shape
                                   tuned before in this process (e.g. in another problem of a

@@ -720,7 +720,7 @@ class MultigridSolver:
                  precision=Precision.fp64, coarse_tol=1e-12, coarse_solver=0, use_graph=True,
                  vertex_coords=None, surrogate_n_q=5, local_solver=0, model=None,
                  auto_relaxation=False, vcycle_precision=Precision.fp64,
-                 penalty_mode=Penalty.reference, autotune=False):
+                 penalty_mode=Penalty.reference, autotune=False, fp64_level_mask=0):
         if relaxation is None:
             relaxation = lookup_damping_factor(patch_variant, smoother_variant, dim)
         d = _lib.MgDesc()
@@ -735,6 +735,7 @@ class MultigridSolver:
         d.vcycle_precision = int(vcycle_precision)
         d.penalty_mode = int(penalty_mode)
         d.autotune = int(autotune)
+        d.fp64_level_mask = int(fp64_level_mask)
         self._model = model
         d.dim, d.degree, d.n_rep, d.n_cells_fine = dim, degree, n_rep, n_cells_fine
         d.ip_factor, d.patch_variant, d.smoother_variant = float(ip_factor), patch_variant, smoother_variant

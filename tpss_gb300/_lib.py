@@ -94,7 +94,8 @@ class MgDesc(C.Structure):
                 ("coarse_solver", C.c_int), ("use_graph", C.c_int),
                 ("vertex_coords", C.POINTER(C.c_double)), ("surrogate_n_q", C.c_int),
                 ("local_solver", C.c_int), ("model", C.c_void_p), ("auto_relaxation", C.c_int),
-                ("vcycle_precision", C.c_int), ("penalty_mode", C.c_int), ("autotune", C.c_int)]
+                ("vcycle_precision", C.c_int), ("penalty_mode", C.c_int), ("fp64_level_mask", C.c_int),
+                ("autotune", C.c_int)]
 
 
 _vp = C.c_void_p

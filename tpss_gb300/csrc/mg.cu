@@ -450,7 +450,8 @@ void autotune_level(MgLevel &lv, const tpss_mg_desc &d)
   TPSS_CUDA(cudaGetDevice(&dev));
   const tpss_layout &L = *lv.L;
   const std::vector<int> key = {dev, L.dim, L.k, L.nc[0], L.nc[1], L.nc[2], d.patch_variant,
-                                d.smoother_variant, d.precision, d.local_solver, d.vertex_coords != nullptr};
+                                d.smoother_variant, lv.P->desc.precision, d.local_solver,
+                                d.vertex_coords != nullptr};
   std::lock_guard<std::mutex> lock(g_tune_mutex);
   auto it = g_tuned.find(key);
   if(it == g_tuned.end())
@@ -520,7 +521,7 @@ extern "C" int tpss_mg_create(const tpss_mg_desc *d, tpss_mg **out)
       {
         tpss_precond_desc pd{};
         pd.relaxation = d->relaxation;
-        pd.precision = d->precision;
+        pd.precision = (d->fp64_level_mask >> l) & 1 ? TPSS_FP64 : d->precision;
         pd.ip_factor = d->ip_factor;
         pd.penalty_mode = d->penalty_mode;
         pd.local_solver = d->local_solver;
