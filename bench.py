@@ -36,6 +36,14 @@ METRIC = "smoother DoF/s (SchwarzPreconditioner::vmult; CG+MG solve s to 1e-8 re
 # decompositions, for k = 4
 VARIANT_SHAPES = ["4,4,8,4", "4,4,8,5", "4,4,4,4", "4,4,16,4", "4,4,8,4,true", "4,4,4,4,true"]
 
+
+def stream_kernel_name(k1, v):
+    """Kernel name of decomposition v of the streamed smoother (pencil or plane passes)."""
+    if v in (6, 7):
+        return f"plane_kernel<PCfg<{k1},8,{8 if v == 6 else 4}>>"
+    return f"stream_kernel<SCfg<{k1},{VARIANT_SHAPES[v]}>>"
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -57,6 +65,9 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--kernel", choices=["auto", "color", "stream"], default="auto")
+    ap.add_argument("--stream-variant", type=int, default=-1,
+                    help="run this decomposition of the streamed kernel instead of the autotuned one "
+                         "(profiling; also skips the FP64 arm)")
     ap.add_argument("--level-kernels", action="store_true",
                     help="time only the level operator (FP64, FP32) and the transfers on the "
                          "--cells level (also the command the operator profile captures)")
@@ -290,12 +301,13 @@ def run_ours(args):
         dim=dim, degree=k, n_cells=(n,) * dim, patch_variant=tpss.PatchVariant.vertex))
     p = tpss.SchwarzPreconditioner()
     variant = {"auto": 0, "color": 1, "stream": 2}[args.kernel]
-    p.initialize(sh, None, tpss.SchwarzPreconditioner.AdditionalData(relaxation=args.omega,
-                                                                     precision=prec,
-                                                                     kernel_variant=variant))
+    forced = args.stream_variant >= 0
+    p.initialize(sh, None, tpss.SchwarzPreconditioner.AdditionalData(
+        relaxation=args.omega, precision=prec, kernel_variant=2 if forced else variant,
+        stream_variant=max(0, args.stream_variant)))
     # the column-streamed kernel runs for 3D vertex patches in FP32 with k <= 4
-    streamed = (args.kernel == "stream" or (args.kernel == "auto" and prec == tpss.Precision.fp32
-                                            and dim == 3 and k <= 4))
+    streamed = forced or (args.kernel == "stream" or (args.kernel == "auto" and prec == tpss.Precision.fp32
+                                                      and dim == 3 and k <= 4))
     n_colors = sh.n_colors()
     launches_per_step = 2 if streamed else n_colors  # stream + fix-up, or one per color
     src_h = philox_src(W["N"], args.seed + rank)
@@ -303,7 +315,10 @@ def run_ours(args):
     dst = torch.empty_like(src)
     stream = torch.cuda.current_stream()
     # the library's autotuner picks the work decomposition of the kernel for this level
-    tuned, tuned_ms = p.autotune(dst, src, reps=5)
+    if forced:
+        tuned, tuned_ms = args.stream_variant, []
+    else:
+        tuned, tuned_ms = p.autotune(dst, src, reps=5)
 
     def barrier():
         if dist is not None:
@@ -363,7 +378,7 @@ def run_ours(args):
     roofline = {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
                 "frac": achieved_gbs / hbm_peak, "traffic": traffic,
                 "peak_source": f"{hbm_kind} (MEASURED_PEAKS.json hbm_gbs)",
-                "kernel": (f"stream_kernel<SCfg<{k + 1},{VARIANT_SHAPES[tuned]}>> + fixup_list_kernel" if streamed
+                "kernel": (f"{stream_kernel_name(k + 1, tuned)} + fixup_list_kernel" if streamed
                            else f"schwarz_color_kernel<{args.precision},3,2,{k + 1}>"),
                 "per_launch_ms": per_launch * 1e3,
                 "algorithmic_bytes_per_launch": bytes_launch,
@@ -394,7 +409,7 @@ def run_ours(args):
 
     if not args.no_e2e:
         out["e2e"] = e2e(tpss, p, src_h, args, W, world, dist)
-    if prec == tpss.Precision.fp32:
+    if prec == tpss.Precision.fp32 and not forced:
         out["fp64"] = fp64_arm(tpss, sh, src, src_h, args, W, world, dist)
     if not args.no_solve:
         out["operator"] = operator_time(tpss, sh, src, W)

@@ -164,7 +164,9 @@ typedef struct tpss_precond_desc
                                   (one fused launch per color) or TPSS_KERNEL_STREAM (3D vertex
                                   patches, FP32, k <= 4: column-streamed, one pass) */
   int stream_variant;          /* initial work decomposition of the smoother kernel (see
-                                  tpss_precond_autotune): 0..5 for the column-streamed kernel,
+                                  tpss_precond_autotune): 0..5 for the column-streamed kernel
+                                  (6, 7: plane passes in registers, degree 4 only; other
+                                  degrees use 0 instead),
                                   0..2 (patches per CTA x1, x2, x4) for the per-color kernel, which
                                   uses 0 where the level offers fewer; 0 by default */
   int local_solver;            /* TPSS_LOCAL_*: how the patch inverses are formed */
@@ -231,18 +233,18 @@ int tpss_precond_Tvmult(tpss_precond *p, double *dst, const double *src, void *s
 int tpss_precond_vmult_static_scratch(tpss_precond *p, double *dst, const double *src, void *stream);
 
 /* Autotuner (no counterpart in the reference): times every work decomposition of the smoother
- * kernel for this level (for the column-streamed kernel: pencils per thread and vertex layers per
- * work item; for the per-color kernel, which serves 2D, cell patches, FP64, k > 4 and the
+ * kernel for this level (for the column-streamed kernel: pencils per thread, vertex layers per
+ * work item and, for degree 4, pencil or plane passes; for the per-color kernel, which serves 2D, cell patches, FP64, k > 4 and the
  * multiplicative smoother: 1, 2 or 4 times its base number of patches per CTA, as far as 512
  * threads and 200 KB of shared memory allow) on the caller's vectors, `reps` applications each,
  * and keeps the fastest for later vmult calls.  On return dst = P src, *chosen is the selected variant, ms_per_variant (optional,
- * >= 6 entries) the measured milliseconds per application and *n_variants their count (1 when the
+ * >= 8 entries) the measured milliseconds per application and *n_variants their count (1 when the
  * level has a single kernel). */
 /* vmult with dst and src in HOST memory (the reference's vmult on host vectors; a device-vector
  * adapter would copy in, apply and copy out). For the streamed smoother the copies are pipelined
  * with the kernel along z (three internal streams), in chunks of one work item deep; the pipeline
  * runs the 4-layer-deep decomposition of the chosen kind (variant 5 when variant 4 or 5 is chosen,
- * else 2) for a short fill and drain, so its result carries that variant's FP32 rounding.
+ * 7 when 6 or 7 is chosen, else 2) for a short fill and drain, so its result carries that variant's FP32 rounding.
  * Otherwise copy-in, vmult, copy-out on `stream`. Stream-ordered: dst is complete when `stream`
  * reaches this point. Pin the host buffers (cudaHostRegister / cudaMallocHost) for the copies to
  * overlap. */

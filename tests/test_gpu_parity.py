@@ -499,7 +499,8 @@ def test_streamed_variants_and_autotune(tpss, oracle, cuda, k, nc):
     ad = tpss.SubdomainHandler.AdditionalData(dim=3, degree=k, n_cells=nc, patch_variant=1)
     sh = tpss.SubdomainHandler(ad)
     s = torch.tensor(src, dtype=torch.float64, device=cuda)
-    for v in range(6):
+    nv = 8 if k == 4 else 6  # degree 4 adds the two plane-pass decompositions
+    for v in range(nv):
         p = tpss.SchwarzPreconditioner()
         p.initialize(sh, None, tpss.SchwarzPreconditioner.AdditionalData(
             relaxation=0.15, precision=1, kernel_variant=2, stream_variant=v))
@@ -508,7 +509,7 @@ def test_streamed_variants_and_autotune(tpss, oracle, cuda, k, nc):
         assert rel_err(d.cpu().numpy(), ref) <= 2e-5, v
     d = torch.full_like(s, float("nan"))
     chosen, ms = p.autotune(d, s, reps=2)
-    assert 0 <= chosen < 6 and len(ms) == 6 and all(t > 0 for t in ms)
+    assert 0 <= chosen < nv and len(ms) == nv and all(t > 0 for t in ms)
     assert rel_err(d.cpu().numpy(), ref) <= 2e-5
     d2 = torch.empty_like(s)
     p.vmult(d2, s)
@@ -551,19 +552,20 @@ def test_color_kernel_variants_and_autotune(tpss, oracle, cuda, dim, k, nc, pv, 
 
 
 @pytest.mark.parametrize("k,nc,variant", [(4, (9, 6, 19), 0), (3, (7, 5, 33), 2), (2, (6, 6, 17), 3), (1, (5, 9, 40), 1),
-                                         (4, (10, 7, 21), 4), (3, (6, 9, 18), 5)])
+                                         (4, (10, 7, 21), 4), (3, (6, 9, 18), 5), (4, (8, 11, 23), 6),
+                                         (4, (7, 5, 12), 7)])
 def test_vmult_host_buffers_pipelined(tpss, oracle, cuda, k, nc, variant):
     """The host-buffer entry point (copies pipelined with the streamed kernel along z) gives
     the oracle's result and the bits of the device path with the decomposition the pipeline
     runs (the 4-layer-deep twin of the chosen one: 5 for the warp-per-patch variants 4 and 5,
-    2 otherwise); also for the per-color path."""
+    7 for the plane-pass variants 6 and 7, 2 otherwise); also for the per-color path."""
     import torch
     N = int(np.prod(nc)) * (k + 1) ** 3
     src = philox(500 + k, N)
     ref = oracle.schwarz_vmult(3, k, nc, src, patch_variant=1, omega=0.15)
     ad = tpss.SubdomainHandler.AdditionalData(dim=3, degree=k, n_cells=nc, patch_variant=1)
     sh = tpss.SubdomainHandler(ad)
-    host_variant = 5 if variant in (4, 5) else 2
+    host_variant = 5 if variant in (4, 5) else 7 if variant in (6, 7) else 2
     for kv in (2, 1):
         p = tpss.SchwarzPreconditioner()
         p.initialize(sh, None, tpss.SchwarzPreconditioner.AdditionalData(

@@ -335,9 +335,9 @@ struct tpss_precond
   tpss::DeviceBuffer<double> residual;  // multiplicative scratch
   tpss::DeviceBuffer<int> flag;         // finiteness check
   tpss::DeviceBuffer<float> halo;       // streamed kernel: partial sums of shared cells
-  tpss::DeviceBuffer<int64_t> fix_rec[6];  // streamed kernel: shared-cell list per variant
-  int64_t fix_n[6] = {-1, -1, -1, -1, -1, -1};
-  std::vector<int64_t> fix_layer[6];
+  tpss::DeviceBuffer<int64_t> fix_rec[8];  // streamed kernel: shared-cell list per variant
+  int64_t fix_n[8] = {-1, -1, -1, -1, -1, -1, -1, -1};
+  std::vector<int64_t> fix_layer[8];
   tpss::HostPipe pipe;                  // host-buffer entry point
   int stream_variant = 0;               // streamed kernel variant (autotuner)
   int color_variant = 0;                // per-color kernel variant: patches per CTA (autotuner)
@@ -461,6 +461,13 @@ struct StreamLaunch
 bool launch_stream3d_host(const tpss_layout &L, const StreamLaunch &l, HostPipe &pipe, double *h_dst,
                           const double *h_src, cudaStream_t caller);
 bool stream_supported(const tpss_layout &L);
+// plane-pass decompositions of the streamed smoother (k = 4; 8 or 4 vertex layers per item)
+bool launch_plane3d_bz8(const tpss_layout &L, const StreamLaunch &l, cudaStream_t s);
+bool launch_plane3d_bz4(const tpss_layout &L, const StreamLaunch &l, cudaStream_t s);
+bool launch_plane3d_host_bz8(const tpss_layout &L, const StreamLaunch &l, HostPipe &pipe, double *h_dst,
+                             const double *h_src, cudaStream_t s);
+bool launch_plane3d_host_bz4(const tpss_layout &L, const StreamLaunch &l, HostPipe &pipe, double *h_dst,
+                             const double *h_src, cudaStream_t s);
 int stream_variant_count(const tpss_layout &L);
 bool launch_stream3d(const tpss_layout &L, const StreamLaunch &l, cudaStream_t s);
 

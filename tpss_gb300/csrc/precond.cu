@@ -431,7 +431,7 @@ void validate_desc(const tpss_precond_desc &d)
 {
   TPSS_REQUIRE(d.kernel_variant >= TPSS_KERNEL_AUTO && d.kernel_variant <= TPSS_KERNEL_STREAM,
                "invalid kernel variant");
-  TPSS_REQUIRE(d.stream_variant >= 0 && d.stream_variant <= 5, "stream_variant must be in 0..5");
+  TPSS_REQUIRE(d.stream_variant >= 0 && d.stream_variant <= 7, "stream_variant must be in 0..7");
   TPSS_REQUIRE(d.relaxation > 0.0, "Invalid relaxation factor.");
   TPSS_REQUIRE(d.precision == TPSS_FP64 || d.precision == TPSS_FP32, "invalid precision");
   TPSS_REQUIRE(d.penalty_mode == TPSS_PENALTY_REFERENCE || d.penalty_mode == TPSS_PENALTY_2KP1SQ,
@@ -825,7 +825,8 @@ extern "C" int tpss_precond_create(const tpss_layout *layout, tpss_operator *op,
     auto p = std::make_unique<tpss_precond>();
     p->desc = *desc;
     p->op = op;
-    p->stream_variant = desc->stream_variant;
+    // a decomposition the level does not offer (the plane passes need k = 4) falls back to 0
+    p->stream_variant = desc->stream_variant < stream_variant_count(*layout) ? desc->stream_variant : 0;
     p->color_variant = desc->stream_variant;  // variants the kernel does not offer fall back to 0
     p->tables = build_local_solvers(*layout, op, *desc);
     if(desc->use_ras_boolean_weights) build_keep_tables(*layout, *p->tables);
@@ -1067,9 +1068,11 @@ extern "C" int tpss_precond_vmult_host(tpss_precond *p, double *dst, const doubl
     {
       // The pipeline is copy-bound (262 MB each way at 64^3 DGQ4 against a 1.3 ms kernel); its
       // fill and drain are one chunk of one z-item, so it runs the 4-layer-deep twin of the
-      // chosen decomposition (warp per patch: 4 -> 5, otherwise 2), which halves both.
+      // chosen decomposition (warp per patch: 4 -> 5, plane passes: 6 -> 7, otherwise 2), which
+      // halves both.
       StreamLaunch l = stream_launch(p, p->pipe.dst.ptr, p->pipe.src.ptr);
-      const int hv = (p->stream_variant == 4 || p->stream_variant == 5) ? 5 : 2;
+      const int sv = p->stream_variant;
+      const int hv = (sv == 4 || sv == 5) ? 5 : (sv == 6 || sv == 7) ? 7 : 2;
       l.variant = hv;
       l.fix_rec = &p->fix_rec[hv];
       l.fix_n = &p->fix_n[hv];

@@ -70,6 +70,7 @@ struct SCfg
 {
   static constexpr int K1 = K1_, BX = BX_, BY = BY_, BZ = BZ_, NPT = NPT_;
   static constexpr bool WARP_PER_PATCH = WARP_PER_PATCH_;
+  static constexpr bool PLANE = false;  // pencil passes (plane3d.cuh holds the plane kernel)
   static constexpr int N = 2 * K1;
   static constexpr int NLOC = N * N * N;
   static constexpr int NPENCIL = N * N;
