@@ -14,8 +14,9 @@
 
 namespace tpss
 {
-namespace
-{
+// (templates only: every translation unit that includes this header instantiates the same
+// definitions, and each launch configuration keeps one per-device cache in stream_cap)
+
 // the kernel of a decomposition: pencil passes (SCfg) or plane passes (PCfg)
 template<class C>
 constexpr void (*kernel_of())(stream::StreamArgs)
@@ -227,5 +228,4 @@ bool launch_stream(const tpss_layout &L, const StreamLaunch &l, cudaStream_t s)
   TPSS_CUDA(cudaGetLastError());
   return true;
 }
-}  // namespace
 }  // namespace tpss
