@@ -7,15 +7,16 @@
 //
 //  - a work item is a column of BX x BY vertices (patches) and BZ vertex layers; persistent
 //    CTAs take items round-robin (one CTA per SM);
-//  - the item's cells are staged layer by layer in shared memory (FP32), the next layer is
-//    prefetched into registers while the current vertex layer is solved;
+//  - the item's cells are staged layer by layer in shared memory: each cell layer lands as FP64
+//    (cp.async, issued one vertex layer ahead) and is converted once to an FP32 layer;
 //  - the 16 patches of a vertex layer are solved together; each thread owns NPT pencils of one
 //    patch, so every 1-D matrix row read from shared memory feeds NPT pencils;
-//  - patch results are summed in a shared-memory accumulator (x/y parity sub-steps, so no
-//    two patches write the same cell at once); a cell layer is final once the vertex layer
-//    above it is done and is written out once: cells owned by the item go straight to dst,
-//    cells on the item's faces shared with neighbouring items go to a halo buffer (scratch),
-//    which a fix-up kernel sums in a fixed order -- the result is deterministic.
+//  - patch results are summed per cell in a shared-memory accumulator (each accumulator cell
+//    adds the up to four patches of the vertex layer that touch it, in a fixed order); a cell
+//    layer is final once the vertex layer above it is done and is written out once: cells owned
+//    by the item go straight to dst, cells on the item's faces shared with neighbouring items go
+//    to a halo buffer (scratch), which a fix-up kernel sums in a fixed order -- the result is
+//    deterministic.
 #pragma once
 
 #include <cuda_runtime.h>
