@@ -417,10 +417,13 @@ def test_fp32_streamed_and_color_kernels(tpss, oracle, cuda, k, nc, variant):
     assert rel_err(d.cpu().numpy(), ref) <= 2e-5
 
 
-def test_streamed_kernel_general_layouts(tpss, oracle, cuda):
-    """Permuted cell numbering, non-uniform tensor-product h and RAS weights."""
+@pytest.mark.parametrize("k,nc,variant", [(3, (6, 5, 10), 0), (4, (8, 11, 9), 4), (4, (8, 11, 9), 6),
+                                         (4, (7, 5, 12), 7)])
+def test_streamed_kernel_general_layouts(tpss, oracle, cuda, k, nc, variant):
+    """Permuted cell numbering, non-uniform tensor-product h (1-D problems without mirror
+    symmetry everywhere, so the plane passes run their full-matrix path) and RAS weights, for
+    pencil and plane decompositions."""
     import torch
-    k, nc = 3, (6, 5, 10)
     g = np.random.default_rng(11)
     h = [g.uniform(0.5, 1.5, n) for n in nc]
     h = [x / x.sum() for x in h]
@@ -433,7 +436,7 @@ def test_streamed_kernel_general_layouts(tpss, oracle, cuda):
         sh = tpss.SubdomainHandler(ad)
         p = tpss.SchwarzPreconditioner()
         p.initialize(sh, None, tpss.SchwarzPreconditioner.AdditionalData(
-            relaxation=0.7, precision=1, kernel_variant=2, use_ras_weights=ras))
+            relaxation=0.7, precision=1, kernel_variant=2, stream_variant=variant, use_ras_weights=ras))
         s = torch.tensor(src, dtype=torch.float64, device=cuda)
         d = torch.empty_like(s)
         p.vmult(d, s)
@@ -442,14 +445,15 @@ def test_streamed_kernel_general_layouts(tpss, oracle, cuda):
         assert rel_err(d.cpu().numpy(), ref) <= 2e-5, ras
 
 
-def test_streamed_kernel_is_deterministic(tpss, cuda):
+@pytest.mark.parametrize("variant", [0, 6])
+def test_streamed_kernel_is_deterministic(tpss, cuda, variant):
     import torch
     k, nc = 4, (20, 12, 17)
     ad = tpss.SubdomainHandler.AdditionalData(dim=3, degree=k, n_cells=nc, patch_variant=1)
     sh = tpss.SubdomainHandler(ad)
     p = tpss.SchwarzPreconditioner()
     p.initialize(sh, None, tpss.SchwarzPreconditioner.AdditionalData(relaxation=0.15, precision=1,
-                                                                     kernel_variant=2))
+                                                                     kernel_variant=2, stream_variant=variant))
     s = torch.tensor(philox(5, sh.n_dofs()), dtype=torch.float64, device=cuda)
     a, b = torch.empty_like(s), torch.empty_like(s)
     p.vmult(a, s)
