@@ -658,7 +658,7 @@ def dgq3_2d_section(tpss, args):
 def distorted_section(tpss, args):
     """Distorted 3D DGQ3 32^3 level (interior vertices moved by `distortion` x the shortest
     edge in random directions, as the reference's distort_random): train the learned local
-    solver's network on the patches of four other meshes, then solve CG + V-cycle to 1e-8 with
+    solver's network on the ~200k patches of seven other meshes, then solve CG + V-cycle to 1e-8 with
     surrogate (FP64, FP32), Kronecker-sum-fitted, rank-2 Kronecker (KSVD), learned and exact
     (FP32) local solvers; measured local inverse errors of the separable solvers."""
     import numpy as np
@@ -670,7 +670,7 @@ def distorted_section(tpss, args):
                        f"8 / (1.05 lambda_max(P A)), dense coarse solve"}
     t0 = time.perf_counter()
     xs, ys = [], []
-    for seed in range(100, 104):
+    for seed in range(100, 107):
         X = distorted_cube(dim, [n] * dim, seed, fac)
         sh = tpss.SubdomainHandler(tpss.SubdomainHandler.AdditionalData(
             dim=dim, degree=k, n_cells=(n,) * dim, patch_variant=tpss.PatchVariant.vertex, vertex_coords=X))
