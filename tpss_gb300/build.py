@@ -25,7 +25,7 @@ FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", 
 
 UNITS = [
     ("setup.cu", []), ("eigen.cu", []), ("layout.cu", []), ("precond.cu", []),
-    ("operator.cu", []), ("mg.cu", []), ("diag.cu", []), ("stream3d.cu", []), ("mapped.cu", []), ("local.cu", []), ("mlp.cu", []), ("learned.cu", []), ("c0ip.cu", []),
+    ("operator.cu", []), ("mg.cu", []), ("diag.cu", []), ("stream3d.cu", []), ("mapped.cu", []), ("mapped_mf.cu", []), ("local.cu", []), ("mlp.cu", []), ("learned.cu", []), ("c0ip.cu", []),
     ("plane_inst.cu", ["-DPLANE_BZ=8"]), ("plane_inst.cu", ["-DPLANE_BZ=4"]),
     ("fd_inst.cu", ["-DFD_T=float", "-DFD_DIM=2"]),
     ("fd_inst.cu", ["-DFD_T=float", "-DFD_DIM=3"]),

@@ -216,6 +216,8 @@ struct MappedOperator
   DeviceBuffer<double> vals;    // n_cells * nb blocks of nd x nd, entry (i, j) at j * nd + i
   DeviceBuffer<float> vals32;   // FP32 copy (single-precision V-cycle), made on first use
   DeviceBuffer<int32_t> col;    // n_cells * nb column cell (lexicographic), -1 = none
+  DeviceBuffer<double> fgeo;    // per cell and face: geometry of the face coupling (mapped_tab.cuh)
+  int fg = 0;                   // doubles per face record
 };
 }  // namespace tpss
 
@@ -383,6 +385,10 @@ void mapped_apply(const tpss_operator &op, double *dst, const double *src, cudaS
 void mapped_apply_f32(tpss_operator &op, double *dst, const double *src, cudaStream_t s,
                       const double *rhs = nullptr);
 std::vector<double> mapped_dense(const tpss_operator &op);
+// the same product with the face couplings applied matrix-free (mapped_mf.cu); false when the
+// level has no face geometry or its degree has no kernel
+bool mapped_apply_mf(const tpss_operator &op, double *dst, const double *src, cudaStream_t s,
+                     const double *rhs = nullptr);
 // FD setup helpers (precond.cu, eigen.cu)
 void gen_eig_batched(int n, int n_problems, const std::vector<double> &Ms,
                      const std::vector<double> &As, std::vector<double> &S,

@@ -19,19 +19,13 @@
 // so that the threads of a block row read consecutive addresses in the product.
 // Slots: 0 = the cell, 1 + 2d + side = face neighbour in direction d (side 0 lower, 1 upper).
 #include "internal.h"
+#include "mapped_tab.cuh"
 
 namespace tpss
 {
 namespace
 {
-constexpr int kMaxNp = 8;
-
-struct MapTab
-{
-  double qx[kMaxNp], qw[kMaxNp];
-  double V[kMaxNp * kMaxNp], D[kMaxNp * kMaxNp];  // [i * np + q]
-  double F[2 * kMaxNp], G[2 * kMaxNp];            // [side * np + i]: value, derivative
-};
+constexpr int kMaxNp = kMapMaxNp;
 
 struct AsmArgs
 {
@@ -41,6 +35,8 @@ struct AsmArgs
   double ip, ip_bd, gamma;  // interior / boundary ip factors
   double *vals;
   int32_t *col;
+  double *fgeo;  // face geometry records (mapped_tab.cuh), n_cells * 2 dim of fg doubles, or null
+  int fg;
 };
 
 template<int DIM>
@@ -333,6 +329,20 @@ __global__ void __launch_bounds__(256) assemble_kernel(const AsmArgs a, const Ma
       const double sigma = boundary ? a.ip_bd * 2.0 * a.gamma / hh[0]
                                     : a.ip * a.gamma * (1.0 / hh[0] + 1.0 / hh[1]) * 0.5;
       const double beta = boundary ? 1.0 : 0.5;
+      if(a.fgeo && !boundary)
+      {
+        double *rec = a.fgeo + ((size_t)cell * 2 * DIM + (2 * d + side)) * a.fg;
+        for(int q = threadIdx.x; q < nfq; q += blockDim.x)
+        {
+          rec[q] = wq[q];
+          for(int e = 0; e < DIM; ++e)
+          {
+            rec[nfq + q * DIM + e] = cnc[q * DIM + e];
+            rec[nfq + nfq * DIM + q * DIM + e] = cnn[q * DIM + e];
+          }
+        }
+        if(threadIdx.x == 0) rec[nfq * (1 + 2 * DIM)] = sigma;
+      }
       for(int e = threadIdx.x; e < nd * nd; e += blockDim.x)
       {
         const int i = e % nd, j = e / nd;
@@ -400,6 +410,8 @@ __global__ void d2f_copy_kernel(int64_t n, const double *__restrict__ x, float *
     y[i] = float(x[i]);
 }
 
+}  // namespace
+
 MapTab make_tab(int k)
 {
   const Shape1D s = make_shape_1d(k);
@@ -425,7 +437,6 @@ MapTab make_tab(int k)
   }
   return t;
 }
-}  // namespace
 
 size_t mapped_smem_bytes(int dim, int np)
 {
@@ -457,6 +468,12 @@ void mapped_build(tpss_operator &op, const tpss_layout &L, Penalty ip)
   a.gamma = L.k == 0 ? 1.0 : L.k * (L.k + 1.0);
   a.vals = M->vals.ptr;
   a.col = M->col.ptr;
+  // face geometry of the matrix-free face couplings (mapped_mf.cu)
+  M->fg = face_geo_size(L.dim, ipow(L.np, L.dim - 1));
+  M->fgeo.resize((size_t)L.n_cells * 2 * L.dim * M->fg);
+  TPSS_CUDA(cudaMemset(M->fgeo.ptr, 0, sizeof(double) * M->fgeo.n));
+  a.fgeo = M->fgeo.ptr;
+  a.fg = M->fg;
   const MapTab t = make_tab(L.k);
   if(L.dim == 2)
   {
@@ -508,6 +525,9 @@ int d2f_grid(int64_t n)
 
 void mapped_apply(const tpss_operator &op, double *dst, const double *src, cudaStream_t s, const double *rhs)
 {
+  // the cell blocks plus matrix-free face couplings (2.4x fewer FP64 FLOPs than the seven
+  // blocks); the block-sparse product where that path has no kernel
+  if(mapped_apply_mf(op, dst, src, s, rhs)) return;
   launch_bsr<double>(op, op.mapped->vals.ptr, src, dst, rhs, s);
 }
 
