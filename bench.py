@@ -77,9 +77,9 @@ def parse():
                          "all-FP32 and all-FP64: iterations and seconds, one JSON line")
     ap.add_argument("--no-dgq3-2d", action="store_true",
                     help="skip the 2D SIPG DGQ3 64^2 section (both penalty modes)")
-    ap.add_argument("--profile-case", choices=["bsr", "c0ip", "mlp", "host"],
+    ap.add_argument("--profile-case", choices=["mapped", "c0ip", "mlp", "host"],
                     help="run one small workload of a secondary kernel three times and exit (the "
-                         "commands the ncu profiles capture): bsr = mapped SIPG operator on a "
+                         "commands the ncu profiles capture): mapped = mapped SIPG operator on a "
                          "distorted 3D DGQ3 24^3 level; c0ip = C0IP FE_Q(3) 512^2 operator and "
                          "FP32 Bilaplacian-FD smoother; mlp = one training epoch of the "
                          "87 -> 3 x 64 -> 108 network on 119,164 samples; host = the FP32 "
@@ -911,7 +911,8 @@ def profile_case(args):
     from tpss_gb300.mesh import distorted_cube
 
     name = args.profile_case
-    if name == "bsr":
+    if name == "mapped":
+        # FP64 operator of a distorted level: cell blocks + matrix-free face couplings
         n, k = 24, 3
         X = distorted_cube(3, [n] * 3, 7, 0.15)
         sh = tpss.SubdomainHandler(tpss.SubdomainHandler.AdditionalData(
