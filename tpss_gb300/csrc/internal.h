@@ -218,6 +218,8 @@ struct MappedOperator
   DeviceBuffer<int32_t> col;    // n_cells * nb column cell (lexicographic), -1 = none
   DeviceBuffer<double> fgeo;    // per cell and face: geometry of the face coupling (mapped_tab.cuh)
   int fg = 0;                   // doubles per face record
+  DeviceBuffer<float> self32;   // FP32 cell blocks, nd x nd per cell (single-precision V-cycle)
+  DeviceBuffer<float> fgeo32;   // FP32 face geometry (single-precision V-cycle)
 };
 }  // namespace tpss
 
@@ -389,6 +391,9 @@ std::vector<double> mapped_dense(const tpss_operator &op);
 // level has no face geometry or its degree has no kernel
 bool mapped_apply_mf(const tpss_operator &op, double *dst, const double *src, cudaStream_t s,
                      const double *rhs = nullptr);
+// its FP32 arithmetic (FP32 copies of the cell blocks, face geometry and source; FP64 result)
+bool mapped_apply_mf_f32(tpss_operator &op, double *dst, const double *src, cudaStream_t s,
+                         const double *rhs = nullptr);
 // FD setup helpers (precond.cu, eigen.cu)
 void gen_eig_batched(int n, int n_problems, const std::vector<double> &Ms,
                      const std::vector<double> &As, std::vector<double> &S,

@@ -533,6 +533,7 @@ void mapped_apply(const tpss_operator &op, double *dst, const double *src, cudaS
 
 void mapped_apply_f32(tpss_operator &op, double *dst, const double *src, cudaStream_t s, const double *rhs)
 {
+  if(mapped_apply_mf_f32(op, dst, src, s, rhs)) return;
   MappedOperator &M = *op.mapped;
   if(M.vals32.n != M.vals.n)
   {
