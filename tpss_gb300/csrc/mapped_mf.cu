@@ -79,9 +79,9 @@ struct MfShape
   static constexpr int OFF_C = OFF_P + 3 * WORK;            // a, c_t1, c_t2, c_d
   static constexpr int OFF_R = OFF_C + 4 * WORK;            // R0V, R0D, R1V (3D)
   static constexpr int OFF_A = OFF_R + 3 * WORK;            // A0, A1
-  static constexpr int DOUBLES = OFF_A + 2 * WORK;
+  static constexpr int VALUES = OFF_A + 2 * WORK;
   template<typename T>
-  static constexpr size_t smem_bytes() { return sizeof(T) * DOUBLES + sizeof(int) * 8; }
+  static constexpr size_t smem_bytes() { return sizeof(T) * VALUES + sizeof(int) * 8; }
 };
 
 template<typename T, int DIM, int NP>
@@ -97,7 +97,7 @@ __global__ void __launch_bounds__(MfShape<DIM, NP>::THREADS) mf_apply_kernel(con
   T *Ca = smd + S::OFF_C, *C1 = Ca + WORK, *C2 = C1 + WORK, *Cd = C2 + WORK;
   T *R0V = smd + S::OFF_R, *R0D = R0V + WORK, *R1V = R0D + WORK;
   T *A0 = smd + S::OFF_A, *A1 = A0 + WORK;
-  int *nbr = reinterpret_cast<int *>(smd + S::DOUBLES);
+  int *nbr = reinterpret_cast<int *>(smd + S::VALUES);
   const int tid = threadIdx.x;
   const int64_t cell = blockIdx.x;
   if(cell >= a.n_cells) return;
