@@ -49,6 +49,29 @@ def test_mapped_operator_vs_quadrature(tpss, oracle, mapped, cuda, dim, k, nc, s
     assert rel_err(dst.cpu().numpy(), A @ x) <= 1e-12
 
 
+@pytest.mark.parametrize("dim,k,nc,seed", [(2, 3, (5, 4), 12), (3, 2, (3, 4, 3), 13)])
+def test_mapped_operator_permuted_cells(tpss, oracle, mapped, cuda, dim, k, nc, seed):
+    """Distorted level with a permuted cell numbering (cell_dof_start): the product with the
+    matrix-free face couplings addresses cells and neighbours through the permutation."""
+    import torch
+    X = oracle.distorted_coords(dim, list(nc), seed, 0.2)
+    A = mapped.sipg_matrix_mapped(dim, k, list(nc), X, 1.0)
+    ncell, nd = int(np.prod(nc)), (k + 1) ** dim
+    cs = np.random.default_rng(seed).permutation(ncell) * nd
+    xp = philox(seed, ncell * nd)
+    idx = (cs[:, None] + np.arange(nd)[None, :]).reshape(-1)  # lexicographic DoF -> permuted DoF
+    ad = tpss.SubdomainHandler.AdditionalData(dim=dim, degree=k, n_cells=nc, patch_variant=1,
+                                              vertex_coords=X, cell_dof_start=cs)
+    sh = tpss.SubdomainHandler(ad)
+    op = tpss.LaplaceOperator(sh)
+    src = torch.tensor(xp, dtype=torch.float64, device=cuda)
+    dst = torch.full_like(src, float("nan"))
+    op.vmult(dst, src)
+    ref = np.empty_like(xp)
+    ref[idx] = A @ xp[idx]
+    assert rel_err(dst.cpu().numpy(), ref) <= 1e-12
+
+
 @pytest.mark.parametrize("dim,k,nc,seed,amp", [(2, 3, (4, 5), 2, 0.25), (3, 3, (3, 3, 2), 6, 0.25)])
 def test_mapped_operator_fp32(tpss, oracle, mapped, cuda, dim, k, nc, seed, amp):
     """The single-precision product on a distorted level (FP32 copy of the block-sparse matrix)
