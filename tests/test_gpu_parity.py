@@ -492,6 +492,36 @@ def test_surrogate_patches_on_distorted_mesh(tpss, oracle, cuda, dim, k, nc, pre
     assert rel_err(d.cpu().numpy(), ref) <= (1e-12 if precision == 0 else 2e-5)
 
 
+@pytest.mark.parametrize("k,nc", [(3, (7, 5, 13)), (2, (6, 9, 17)), (1, (5, 6, 11))])
+def test_streamed_kernel_per_patch_tables(tpss, oracle, cuda, k, nc):
+    """Distorted 3D level: the streamed kernel on per-patch 1-D problems (surrogate widths, and
+    Kronecker sums fitted per patch) gives the oracle's / the per-color kernel's result in every
+    work decomposition, ragged item tiles included."""
+    import torch
+    X = oracle.distorted_coords(3, list(nc), 31, 0.2)
+    ad = tpss.SubdomainHandler.AdditionalData(dim=3, degree=k, n_cells=nc, patch_variant=1,
+                                              vertex_coords=X)
+    sh = tpss.SubdomainHandler(ad)
+    op = tpss.LaplaceOperator(sh, 1.0)
+    src = philox(78, sh.n_dofs())
+    s = torch.tensor(src, dtype=torch.float64, device=cuda)
+    ref = oracle.schwarz_vmult_surrogate(3, k, nc, oracle.surrogate_h(3, nc, X), src, omega=0.6)
+
+    def run(local_solver, kv, sv=0):
+        p = tpss.SchwarzPreconditioner()
+        p.initialize(sh, op, tpss.SchwarzPreconditioner.AdditionalData(
+            relaxation=0.6, precision=1, kernel_variant=kv, stream_variant=sv, local_solver=local_solver))
+        d = torch.full_like(s, 3.0)
+        p.vmult(d, s)
+        torch.cuda.synchronize()
+        return d.cpu().numpy()
+
+    ksum_color = run(tpss.LocalSolver.ksum, 1)
+    for v in range(6):
+        assert rel_err(run(tpss.LocalSolver.fd, 2, v), ref) <= 2e-5, v
+        assert rel_err(run(tpss.LocalSolver.ksum, 2, v), ksum_color) <= 2e-5, v
+
+
 @pytest.mark.parametrize("k,nc", [(4, (9, 6, 19)), (3, (7, 5, 13)), (2, (6, 6, 17)), (1, (5, 9, 18))])
 def test_streamed_variants_and_autotune(tpss, oracle, cuda, k, nc):
     """Every work decomposition of the streamed kernel gives the oracle's result; the autotuner

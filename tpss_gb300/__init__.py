@@ -264,7 +264,7 @@ class SchwarzPreconditioner:
         ip_factor: float = 1.0
         check_finite: bool = False
         kernel_variant: int = 0  # 0 auto, 1 one launch per color, 2 column-streamed (3D, FP32)
-        stream_variant: int = 0  # work decomposition of the column-streamed kernel (0..3)
+        stream_variant: int = 0  # work decomposition of the column-streamed kernel (0..7 at degree 4, else 0..5)
         local_solver: int = 0    # LocalSolver.fd / exact / ksum / learned
         model: "MLP" = None      # trained network for LocalSolver.learned
         penalty_mode: int = Penalty.reference  # must match the level operator's

@@ -276,6 +276,7 @@ struct FdTables
   DeviceBuffer<unsigned char> keep_mask;
   // per-patch entries (entry p * dim + d) instead of the layout's shared keys
   DeviceBuffer<int32_t> own_fd;
+  DeviceBuffer<int32_t> vpatch;  // streamed smoother on per-patch tables: patch of each vertex
   // exact local inverses (local solver TPSS_LOCAL_EXACT): P x nloc x nloc, transposed
   DeviceBuffer<double> dense64;
   DeviceBuffer<float> dense32;
@@ -466,6 +467,10 @@ struct StreamLaunch
   DeviceBuffer<int64_t> *fix_rec = nullptr;
   int64_t *fix_n = nullptr;
   std::vector<int64_t> *fix_layer = nullptr;  // first record of every cell layer (nc_z + 1)
+  // per-patch 1-D problems (distorted levels): vertex -> patch map and the patches' FD entries
+  bool per_patch = false;
+  const int32_t *vpatch = nullptr;
+  const int32_t *pfd = nullptr;
 };
 
 // pipelined streamed smoother between host buffers: returns false when not applicable

@@ -705,8 +705,11 @@ int fd_variants(bool fp32, int dim, int k, int ncp)
 bool stream_eligible(const tpss_precond *p)
 {
   const tpss_layout &L = *p->tables->layout;
+  // per-patch tables (distorted levels) need Kronecker-sum patch inverses: not the product-form
+  // eigenvalues of the rank-2 Kronecker solver (rcp_E < 0)
+  const bool per_patch = L.per_patch_fd || p->tables->own_fd.n != 0;
   return L.smoother_variant == TPSS_ADDITIVE && p->desc.precision == TPSS_FP32 &&
-         stream_supported(L) && !p->tables->dense && p->tables->own_fd.n == 0 &&
+         stream_supported(L) && !p->tables->dense && (!per_patch || L.k <= 3) && p->tables->rcp_E >= 0 &&
          !p->desc.use_ras_boolean_weights;
 }
 
@@ -736,6 +739,29 @@ StreamLaunch stream_launch(tpss_precond *p, double *dst, const double *src)
   l.fix_rec = &p->fix_rec[p->stream_variant];
   l.fix_n = &p->fix_n[p->stream_variant];
   l.fix_layer = &p->fix_layer[p->stream_variant];
+  l.per_patch = L.per_patch_fd || p->tables->own_fd.n != 0;
+  if(l.per_patch)
+  {
+    FdTables &T = *p->tables;
+    {
+      // vertex -> patch map, built on first use (tables are shared by shallow copies)
+      static std::mutex mu;
+      std::lock_guard<std::mutex> lock(mu);
+      if(T.vpatch.n == 0)
+      {
+        const int64_t nvx = L.nc[0] + 1, nvy = L.nc[1] + 1, nvz = L.nc[2] + 1;
+        std::vector<int32_t> vp((size_t)(nvx * nvy * nvz), -1);
+        for(int64_t q = 0; q < L.P; ++q)
+        {
+          const int64_t v = (L.lower[q * 3] + 1) + nvx * ((L.lower[q * 3 + 1] + 1) + nvy * (L.lower[q * 3 + 2] + 1));
+          vp[(size_t)v] = (int32_t)q;
+        }
+        T.vpatch.upload(vp.data(), vp.size());
+      }
+    }
+    l.vpatch = T.vpatch.ptr;
+    l.pfd = T.own_fd.n ? T.own_fd.ptr : L.d_patch_fd.ptr;
+  }
   return l;
 }
 

@@ -17,9 +17,21 @@ using Cfg3 = stream::SCfg<K1, 4, 4, 8, 4>;
 
 bool stream_supported(const tpss_layout &L)
 {
-  return L.dim == 3 && L.patch_variant == TPSS_PATCH_VERTEX && !L.per_patch_fd && L.k >= 1 && L.k <= 4 &&
-         L.nc[0] >= 2 && L.nc[1] >= 2 && L.nc[2] >= 2;
+  // per-patch 1-D problems (distorted levels) up to k = 3: their table slots for the 16 patches
+  // of a vertex layer fit next to the staged layers
+  return L.dim == 3 && L.patch_variant == TPSS_PATCH_VERTEX && (!L.per_patch_fd || L.k <= 3) && L.k >= 1 &&
+         L.k <= 4 && L.nc[0] >= 2 && L.nc[1] >= 2 && L.nc[2] >= 2;
 }
+
+// the same decomposition with per-patch 1-D problems (registers hold these kernels to one CTA per
+// SM, so the 48 table slots of 4 x 4 vertex columns cost no occupancy)
+template<class C>
+struct WithPP;
+template<int K1, int BX, int BY, int BZ, int NPT, bool W>
+struct WithPP<stream::SCfg<K1, BX, BY, BZ, NPT, W, false>>
+{
+  using type = stream::SCfg<K1, BX, BY, BZ, NPT, W, true>;
+};
 
 // Variants the autotuner chooses from (same mathematics, different work decomposition):
 //   0: 4x4 vertex columns, 8 vertex layers per item, 4 pencils per thread
@@ -67,22 +79,46 @@ struct VariantCfg<K1, 5>
 {
   using type = stream::SCfg<K1, 4, 4, 4, npt_warp<K1>(), true>;
 };
+// variant V with keyed or per-patch tables
+template<int K1, int V>
+bool launch_kv(const tpss_layout &L, const StreamLaunch &l, cudaStream_t s)
+{
+  using C = typename VariantCfg<K1, V>::type;
+  if(!l.per_patch) return launch_stream<C>(L, l, s);
+  if constexpr(K1 <= 4)
+    return launch_stream<typename WithPP<C>::type>(L, l, s);
+  else
+    return false;
+}
+
+template<int K1, int V>
+bool launch_kv_host(const tpss_layout &L, const StreamLaunch &l, HostPipe &pp, double *h_dst,
+                    const double *h_src, cudaStream_t s)
+{
+  using C = typename VariantCfg<K1, V>::type;
+  if(!l.per_patch) return launch_stream_host<C>(L, l, pp, h_dst, h_src, s);
+  if constexpr(K1 <= 4)
+    return launch_stream_host<typename WithPP<C>::type>(L, l, pp, h_dst, h_src, s);
+  else
+    return false;
+}
+
 template<int K1>
 bool launch_variant(const tpss_layout &L, const StreamLaunch &l, cudaStream_t s, int v)
 {
   switch(v)
   {
-  case 0: return launch_stream<typename VariantCfg<K1, 0>::type>(L, l, s);
-  case 1: return launch_stream<typename VariantCfg<K1, 1>::type>(L, l, s);
-  case 2: return launch_stream<typename VariantCfg<K1, 2>::type>(L, l, s);
-  case 3: return launch_stream<typename VariantCfg<K1, 3>::type>(L, l, s);
-  case 4: return launch_stream<typename VariantCfg<K1, 4>::type>(L, l, s);
-  case 5: return launch_stream<typename VariantCfg<K1, 5>::type>(L, l, s);
+  case 0: return launch_kv<K1, 0>(L, l, s);
+  case 1: return launch_kv<K1, 1>(L, l, s);
+  case 2: return launch_kv<K1, 2>(L, l, s);
+  case 3: return launch_kv<K1, 3>(L, l, s);
+  case 4: return launch_kv<K1, 4>(L, l, s);
+  case 5: return launch_kv<K1, 5>(L, l, s);
   case 6:
   case 7:
-    // plane passes (k = 4 only), compiled in plane_inst.cu
+    // plane passes (k = 4, keyed tables only), compiled in plane_inst.cu
     if constexpr(K1 == 5)
-      return v == 6 ? launch_plane3d_bz8(L, l, s) : launch_plane3d_bz4(L, l, s);
+      return !l.per_patch && (v == 6 ? launch_plane3d_bz8(L, l, s) : launch_plane3d_bz4(L, l, s));
     else
       return false;
   default: return false;
@@ -95,17 +131,17 @@ bool launch_variant_host(const tpss_layout &L, const StreamLaunch &l, HostPipe &
 {
   switch(v)
   {
-  case 0: return launch_stream_host<typename VariantCfg<K1, 0>::type>(L, l, pp, h_dst, h_src, s);
-  case 1: return launch_stream_host<typename VariantCfg<K1, 1>::type>(L, l, pp, h_dst, h_src, s);
-  case 2: return launch_stream_host<typename VariantCfg<K1, 2>::type>(L, l, pp, h_dst, h_src, s);
-  case 3: return launch_stream_host<typename VariantCfg<K1, 3>::type>(L, l, pp, h_dst, h_src, s);
-  case 4: return launch_stream_host<typename VariantCfg<K1, 4>::type>(L, l, pp, h_dst, h_src, s);
-  case 5: return launch_stream_host<typename VariantCfg<K1, 5>::type>(L, l, pp, h_dst, h_src, s);
+  case 0: return launch_kv_host<K1, 0>(L, l, pp, h_dst, h_src, s);
+  case 1: return launch_kv_host<K1, 1>(L, l, pp, h_dst, h_src, s);
+  case 2: return launch_kv_host<K1, 2>(L, l, pp, h_dst, h_src, s);
+  case 3: return launch_kv_host<K1, 3>(L, l, pp, h_dst, h_src, s);
+  case 4: return launch_kv_host<K1, 4>(L, l, pp, h_dst, h_src, s);
+  case 5: return launch_kv_host<K1, 5>(L, l, pp, h_dst, h_src, s);
   case 6:
   case 7:
     if constexpr(K1 == 5)
-      return v == 6 ? launch_plane3d_host_bz8(L, l, pp, h_dst, h_src, s)
-                    : launch_plane3d_host_bz4(L, l, pp, h_dst, h_src, s);
+      return !l.per_patch && (v == 6 ? launch_plane3d_host_bz8(L, l, pp, h_dst, h_src, s)
+                                     : launch_plane3d_host_bz4(L, l, pp, h_dst, h_src, s));
     else
       return false;
   default: return false;
@@ -197,6 +233,8 @@ void launch_stream_static(const tpss_layout &L, const tpss_precond &p, const dou
   a.fd_eo = p.tables->fd32_eo.ptr;
   a.sym = p.tables->sym.ptr;
   a.es_eo = 4 * (L.n / 2) * p.tables->hpad32 + p.tables->npad32;
+  a.vpatch = nullptr;
+  a.pfd = nullptr;
   for(int d = 0; d < 3; ++d)
   {
     a.vfd[d] = L.d_vertex_fd[d].ptr;
@@ -245,6 +283,9 @@ extern "C" int tpss_precond_vmult_static_scratch(tpss_precond *p, double *dst, c
     TPSS_REQUIRE(!p->desc.check_finite,
                  "the allocation-free smoother has no finiteness check (its flag would need a buffer); "
                  "create the preconditioner with check_finite = 0");
+    TPSS_REQUIRE(!L.per_patch_fd && p->tables->own_fd.n == 0,
+                 "the allocation-free smoother runs on levels whose patches share their 1-D problems "
+                 "(Cartesian levels with fast-diagonalization tables)");
     TPSS_REQUIRE(p->desc.kernel_variant != TPSS_KERNEL_COLOR,
                  "the allocation-free smoother is the column-streamed kernel; kernel_variant asks for "
                  "the per-color kernel");

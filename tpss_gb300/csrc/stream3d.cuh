@@ -9,7 +9,7 @@
 //    CTAs take items round-robin (one CTA per SM);
 //  - the item's cells are staged layer by layer in shared memory: each cell layer lands as FP64
 //    (cp.async, issued one vertex layer ahead) and is converted once to an FP32 layer;
-//  - the 16 patches of a vertex layer are solved together; each thread owns NPT pencils of one
+//  - the BX x BY patches of a vertex layer are solved together; each thread owns NPT pencils of one
 //    patch, so every 1-D matrix row read from shared memory feeds NPT pencils;
 //  - patch results are summed per cell in a shared-memory accumulator (each accumulator cell
 //    adds the up to four patches of the vertex layer that touch it, in a fixed order); a cell
@@ -66,11 +66,16 @@ __host__ __device__ constexpr bool bank_order_conflict_free()
   return true;
 }
 
-template<int K1_, int BX_, int BY_, int BZ_, int NPT_, bool WARP_PER_PATCH_ = false>
+template<int K1_, int BX_, int BY_, int BZ_, int NPT_, bool WARP_PER_PATCH_ = false, bool PP_ = false>
 struct SCfg
 {
   static constexpr int K1 = K1_, BX = BX_, BY = BY_, BZ = BZ_, NPT = NPT_;
   static constexpr bool WARP_PER_PATCH = WARP_PER_PATCH_;
+  // PP: every patch has its own 1-D problems (distorted levels: surrogate, fitted or learned
+  // local solvers): the table slots hold the 3 directions of each patch of the vertex layer and
+  // are refilled per vertex layer (cp.async, issued while the previous layer's results are
+  // accumulated); otherwise one slot per vertex coordinate of the item
+  static constexpr bool PP = PP_;
   static constexpr bool PLANE = false;  // pencil passes (plane3d.cuh holds the plane kernel)
   static constexpr int N = 2 * K1;
   static constexpr int NLOC = N * N * N;
@@ -108,14 +113,18 @@ struct SCfg
   static constexpr int G = THREADS / CD;   // thread groups sharing an e
   static_assert(G >= 1, "need at least one thread per cell DoF");
   // shared memory carve-up (in floats; the staged FP64 cell layers take two floats per value)
-  static constexpr int OFF_FD = 0;                                   // (BX + BY + BZ) entries
-  static constexpr int OFF_SYM = OFF_FD + (BX + BY + BZ) * ESLOT;          // int flags
+  static constexpr int NSLOT = PP_ ? 3 * BX * BY : BX + BY + BZ;     // 1-D table slots
+  static constexpr int OFF_FD = 0;                                   // NSLOT entries
+  static constexpr int OFF_SYM = OFF_FD + NSLOT * ESLOT;             // int flags
+  // PP: table entry code of every slot of the item's vertex layers (2 entry + mirror-symmetric
+  // flag, -1 none), looked up once per item
+  static constexpr int OFF_EN = OFF_SYM + NSLOT;
   // cell layers are copied in as FP64 (two landing layers) and converted once to FP32 (two
   // layers, rows of cells padded by RPAD floats so that the x pass reads conflict free)
   static constexpr int RPAD = K1 == 5 ? 4 : K1 == 4 ? 1 : K1 == 3 ? (WARP_PER_PATCH_ ? 0 : 6) : (WARP_PER_PATCH_ ? 5 : 1);
   static constexpr int RSTRIDE = CX * CD + RPAD;                     // floats per row of cells
   static constexpr int LAYERF = ((CY * RSTRIDE + 3) / 4) * 4;        // floats per FP32 layer
-  static constexpr int OFF_RAW = ((OFF_SYM + (BX + BY + BZ) + 3) / 4) * 4;  // 2 FP64 layers
+  static constexpr int OFF_RAW = ((OFF_EN + (PP_ ? BZ * NSLOT : 0) + 3) / 4) * 4;  // 2 FP64 layers
   static constexpr int OFF_F32 = OFF_RAW + 2 * 2 * LAYER;            // 2 FP32 cell layers
   static constexpr int OFF_ACC = OFF_F32 + 2 * LAYERF;               // 2 FP32 accumulator layers
   static constexpr int OFF_WORK = OFF_ACC + 2 * LAYER;               // NPATCH patches
@@ -153,6 +162,10 @@ struct StreamArgs
   float omega;
   int ras;                                 // scale by 1/multiplicity
   int item_begin, item_end;                // items of this launch (z-major item order)
+  // per-patch 1-D problems (SCfg::PP): patch index of each vertex (lexicographic over the
+  // (n+1)^3 vertices, -1 on the boundary) and the patches' FD entries (3 per patch)
+  const int32_t *__restrict__ vpatch;
+  const int32_t *__restrict__ pfd;
 };
 
 // tiles (t, local index l) of direction d that contain cell c; returns the count (1 or 2)
@@ -608,6 +621,35 @@ __device__ __forceinline__ void copy_layer_async(const StreamArgs &a, const int 
 
 __device__ __forceinline__ void wait_async_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
+// asynchronous copy (cp.async, 16 bytes) of one vertex layer's per-patch 1-D problems into the
+// table slots (SCfg::PP): slot sl takes the full or even/odd entry of code en[sl], zero-filled
+// beyond the entry and for en[sl] < 0; the mirror-symmetric flags are stored directly
+template<class C>
+__device__ __forceinline__ void fill_tables_async(const StreamArgs &a, float *s_fd, int *s_sym, const int *en,
+                                                  int tid)
+{
+  constexpr int Q = C::ESLOT / 4;  // 16-byte chunks per slot
+  for(int i = tid; i < C::NSLOT * Q; i += C::THREADS)
+  {
+    const int sl = i / Q, o = 4 * (i % Q), code = en[sl];
+    const float *src = a.fd;
+    int bytes = 0;
+    if(code >= 0)
+    {
+      const int e = code >> 1;
+      if(code & 1)
+      {
+        if(o < C::ES_EO) { src = a.fd_eo + (size_t)e * a.es_eo + o; bytes = 16; }
+      }
+      else if(o < C::ES) { src = a.fd + (size_t)e * C::ES + o; bytes = 16; }
+    }
+    const unsigned saddr = (unsigned)__cvta_generic_to_shared(s_fd + sl * C::ESLOT + o);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(saddr), "l"(src), "r"(bytes) : "memory");
+    if(o == 0) s_sym[sl] = code >= 0 ? (code & 1) : 0;
+  }
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+
 // FP64 landing layer -> FP32 cell layer (rows padded to RSTRIDE). Each thread converts the values
 // its own copy_layer_async put there (same cell/DoF assignment), so after its wait_async_all no
 // barrier is needed in between.
@@ -688,6 +730,7 @@ __global__ void __launch_bounds__(C::THREADS, 1) stream_kernel(StreamArgs a)
   extern __shared__ __align__(16) float sm[];
   float *s_fd = sm + C::OFF_FD;
   int *s_sym = reinterpret_cast<int *>(sm + C::OFF_SYM);
+  int *s_en = reinterpret_cast<int *>(sm + C::OFF_EN);
   double *s_raw = reinterpret_cast<double *>(sm + C::OFF_RAW);
   float *s_f32 = sm + C::OFF_F32;
   float *s_acc = sm + C::OFF_ACC;
@@ -734,8 +777,28 @@ __global__ void __launch_bounds__(C::THREADS, 1) stream_kernel(StreamArgs a)
     const int bz = min(BZ, a.nc[2] - 1 - BZ * tz);
     const int x0 = BX * tx, y0 = BY * ty, z0 = BZ * tz;  // first cell of the item
     __syncthreads();  // the previous item is done with shared memory
+    if constexpr(C::PP)
+    {
+      // entry codes of the item's patches, per vertex layer and slot (3 directions per patch);
+      // the slots are filled per vertex layer by fill_tables_async
+      const int nvx = a.nc[0] + 1, nvy = a.nc[1] + 1;
+      for(int i = tid; i < BZ * C::NSLOT; i += C::THREADS)
+      {
+        const int jj = i / C::NSLOT, sl = i % C::NSLOT, pp = sl / 3, d = sl % 3;
+        const int ppx = pp % BX, ppy = pp / BX;
+        int code = -1;
+        if(jj < bz && ppx < bx && ppy < by)
+        {
+          const int32_t patch =
+            a.vpatch[(x0 + 1 + ppx) + (int64_t)nvx * ((y0 + 1 + ppy) + (int64_t)nvy * (z0 + 1 + jj))];
+          const int32_t en = patch >= 0 ? a.pfd[(int64_t)patch * 3 + d] : -1;
+          if(en >= 0) code = 2 * en + (a.sym[en] ? 1 : 0);
+        }
+        s_en[i] = code;
+      }
+    }
     // 1-D eigenbases of the item's x, y and z vertices: full entry or even/odd split
-    for(int i = tid; i < (BX + BY + BZ) * C::ESLOT; i += C::THREADS)
+    for(int i = tid; i < (C::PP ? 0 : (BX + BY + BZ) * C::ESLOT); i += C::THREADS)
     {
       const int sl = i / C::ESLOT, o = i % C::ESLOT;
       int en = -1;
@@ -777,6 +840,7 @@ __global__ void __launch_bounds__(C::THREADS, 1) stream_kernel(StreamArgs a)
     __syncthreads();
     copy_layer_async<C>(a, s_cxy, z0, s_raw, e, g);
     copy_layer_async<C>(a, s_cxy, z0 + 1, s_raw + C::LAYER, e, g);
+    if constexpr(C::PP) fill_tables_async<C>(a, s_fd, s_sym, s_en, tid);
     for(int i = tid; i < 2 * C::LAYER; i += C::THREADS) s_acc[i] = 0.f;
     wait_async_all();
     convert_layer<C>(s_raw, s_f32, e, g);
@@ -789,12 +853,15 @@ __global__ void __launch_bounds__(C::THREADS, 1) stream_kernel(StreamArgs a)
       const bool more = j + 2 <= bz;
       // (cell layer j+2 lands in the FP64 slot of layer j, converted at the end of iteration j-2)
       if(more) copy_layer_async<C>(a, s_cxy, z0 + j + 2, s_raw + (j % 2) * C::LAYER, e, g);
+      // (PP: the slots hold this vertex layer's 1-D problems, copied during iteration j-1)
       const float *lo = s_f32 + (j % 2) * C::LAYERF, *hi = s_f32 + ((j + 1) % 2) * C::LAYERF;
       const bool active = px < bx && py < by && q < TPP;
       float *my = s_work + slot * PS;
       constexpr int ESL = C::ESLOT, HP = C::HPAD;
-      const float *ex = s_fd + px * ESL, *ey = s_fd + (BX + py) * ESL, *ez = s_fd + (BX + BY + j) * ESL;
-      const bool sx = s_sym[px], sy = s_sym[BX + py], sz = s_sym[BX + BY + j];
+      const int slx = C::PP ? 3 * slot : px, sly = C::PP ? 3 * slot + 1 : BX + py,
+                slz = C::PP ? 3 * slot + 2 : BX + BY + j;
+      const float *ex = s_fd + slx * ESL, *ey = s_fd + sly * ESL, *ez = s_fd + slz * ESL;
+      const bool sx = s_sym[slx], sy = s_sym[sly], sz = s_sym[slz];
       const float *lamx = ex + (sx ? C::EO_LAM : Entry<float, N>::LAM);
       const float *lamy = ey + (sy ? C::EO_LAM : Entry<float, N>::LAM);
       const float *lamz = ez + (sz ? C::EO_LAM : Entry<float, N>::LAM);
@@ -830,6 +897,10 @@ __global__ void __launch_bounds__(C::THREADS, 1) stream_kernel(StreamArgs a)
         else spass<false, false, M0, true, N, SX, SXY, NPAD, HP, 0, NPT, TPP>(my, ex, pm0, q, a.omega);
       }
       __syncthreads();
+      // PP: the passes are done with the slots; the next vertex layer's 1-D problems stream in
+      // behind the accumulation and the write (waited for at the end of this iteration)
+      if constexpr(C::PP)
+        if(j + 1 < bz) fill_tables_async<C>(a, s_fd, s_sym, s_en + (j + 1) * C::NSLOT, tid);
       // accumulate per cell: the (up to) 4 patches of this layer touching the cell, fixed order
       float *alo = s_acc + (j % 2) * C::LAYER, *ahi = s_acc + ((j + 1) % 2) * C::LAYER;
       if(g < C::G)
@@ -866,11 +937,8 @@ __global__ void __launch_bounds__(C::THREADS, 1) stream_kernel(StreamArgs a)
       __syncthreads();
       // cell layer j is complete: write it, clear its accumulator for layer j+2
       write_layer<C>(a, alo, item, j, z0 + j, j == 0 && tz > 0, s_cxy, s_cshared, e, g, true);
-      if(more)
-      {
-        wait_async_all();
-        convert_layer<C>(s_raw + (j % 2) * C::LAYER, s_f32 + (j % 2) * C::LAYERF, e, g);
-      }
+      if(more || C::PP) wait_async_all();
+      if(more) convert_layer<C>(s_raw + (j % 2) * C::LAYER, s_f32 + (j % 2) * C::LAYERF, e, g);
       __syncthreads();
     }
     // last cell layer of the item

@@ -95,6 +95,12 @@ stream::StreamArgs make_args(const tpss_layout &L, const StreamLaunch &l)
   a.T[2] = (L.nc[2] - 1 + C::BZ - 1) / C::BZ;
   a.omega = (float)l.omega;
   a.ras = l.ras;
+  a.vpatch = l.vpatch;
+  a.pfd = l.pfd;
+  if constexpr(!C::PLANE)
+    if(C::PP)
+      TPSS_REQUIRE(l.vpatch && l.pfd && l.es_eo % 4 == 0,
+                   "per-patch streamed smoother: vertex-patch map, patch entries and 16-byte table rows");
   const int64_t n_items = (int64_t)a.T[0] * a.T[1] * a.T[2];
   a.item_begin = 0;
   a.item_end = (int)n_items;
