@@ -77,10 +77,12 @@ def parse():
                          "all-FP32 and all-FP64: iterations and seconds, one JSON line")
     ap.add_argument("--no-dgq3-2d", action="store_true",
                     help="skip the 2D SIPG DGQ3 64^2 section (both penalty modes)")
-    ap.add_argument("--profile-case", choices=["mapped", "c0ip", "mlp", "host"],
+    ap.add_argument("--profile-case", choices=["mapped", "perpatch", "c0ip", "mlp", "host"],
                     help="run one small workload of a secondary kernel three times and exit (the "
                          "commands the ncu profiles capture): mapped = mapped SIPG operator on a "
-                         "distorted 3D DGQ3 24^3 level; c0ip = C0IP FE_Q(3) 512^2 operator and "
+                         "distorted 3D DGQ3 24^3 level; perpatch = FP32 smoother on per-patch 1-D "
+                         "problems (distorted 3D DGQ3 56^3, surrogate widths), streamed decomposition 4 "
+                         "and the per-color kernel; c0ip = C0IP FE_Q(3) 512^2 operator and "
                          "FP32 Bilaplacian-FD smoother; mlp = one training epoch of the "
                          "87 -> 3 x 64 -> 108 network on 119,164 samples; host = the FP32 "
                          "smoother between pinned host buffers on 3D DGQ4 64^3")
@@ -924,6 +926,31 @@ def profile_case(args):
         y = torch.empty_like(x)
         for _ in range(3):
             op.vmult(y, x)
+    elif name == "perpatch":
+        # streamed FP32 smoother on per-patch 1-D problems against the per-color kernel (src and
+        # dst 90 MB each: together larger than L2)
+        n, k = 56, 3
+        X = distorted_cube(3, [n] * 3, 7, 0.15)
+        sh = tpss.SubdomainHandler(tpss.SubdomainHandler.AdditionalData(
+            dim=3, degree=k, n_cells=(n,) * 3, vertex_coords=X))
+        x = torch.rand(sh.n_dofs(), dtype=torch.float64, device="cuda")
+        y = torch.empty_like(x)
+        ms = {}
+        for label, kv in (("streamed_variant4", 2), ("per_color", 1)):
+            p = tpss.SchwarzPreconditioner()
+            p.initialize(sh, None, tpss.SchwarzPreconditioner.AdditionalData(
+                relaxation=0.15, precision=tpss.Precision.fp32, kernel_variant=kv, stream_variant=4))
+            for _ in range(3):
+                p.vmult(y, x)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(10):
+                p.vmult(y, x)
+            e1.record()
+            torch.cuda.synchronize()
+            ms[label] = e0.elapsed_time(e1) / 10
+            del p
+        print(json.dumps({"profile_case": name, "n_dofs": sh.n_dofs(), "ms_per_vmult": ms}))
     elif name == "c0ip":
         P = tpss.C0IPBiharmonic(3, 2, 512, local_solver=tpss.LocalSolver.fd, precision=tpss.Precision.fp32)
         x = torch.rand(P.n_dofs(), dtype=torch.float64, device="cuda")
