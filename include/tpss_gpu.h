@@ -332,15 +332,21 @@ int tpss_mg_vmult(tpss_mg *mg, double *dst, const double *src, void *stream);
 /* SolverCG with ReductionControl (apps/poisson_problem.h:726-755, apps/rt_parameter.h:39-41):
  * solves A u = f (u := 0 first), stopping when ||r|| <= max(abs_tol, rel_tol ||r_0||).
  * On return *iterations holds the CG iteration count and res_history (host, length
- * max_iter+1, may be NULL) the residual norms. */
+ * max_iter+1, may be NULL) the residual norms. With use_graph and the dense coarse solve the
+ * iteration loop runs on the device: one CUDA graph (a conditional WHILE node whose body is one
+ * CG iteration and a one-thread kernel that tests the residual), captured at tpss_mg_create and
+ * launched once per solve, so a solve synchronizes with the host once; otherwise the host
+ * reads the residual norm every iteration. Both run the same kernels in the same order. */
 int tpss_mg_cg_solve(tpss_mg *mg, double *u, const double *f, double rel_tol, double abs_tol,
                      int max_iter, int *iterations, double *res_history, void *stream);
 /* Batched solves (no counterpart in the reference, which runs one problem per process): many
- * independent hierarchies (each described by a tpss_mg_desc; dense coarse solve and graphs
- * recommended) solved by CG in lockstep -- every round enqueues one iteration per active
- * problem on n_streams streams (V-cycles replay their CUDA graphs), then one host
- * synchronization reads all residual norms. iterations: n_problems entries (-1 if a problem
- * did not converge within max_iter, which also returns TPSS_ERR_NOT_CONVERGED). */
+ * independent hierarchies (each described by a tpss_mg_desc with the dense coarse solve and
+ * use_graph = 1) solved by CG concurrently -- every problem's device-side CG loop (see
+ * tpss_mg_cg_solve) is launched once on one of n_streams streams, the problems dealt largest
+ * first to the least-loaded stream, and one host synchronization at the end reads all
+ * iteration counts. Each problem's result is the one its own tpss_mg_cg_solve gives.
+ * iterations: n_problems entries (-1 if a problem did not converge within max_iter, which also
+ * returns TPSS_ERR_NOT_CONVERGED). */
 typedef struct tpss_batch tpss_batch;
 int tpss_batch_create(const tpss_mg_desc *descs, int n_problems, int n_streams, tpss_batch **out);
 int tpss_batch_problem(tpss_batch *b, int i, tpss_mg **mg);
@@ -351,7 +357,9 @@ void tpss_batch_destroy(tpss_batch *b);
 /* Damping used by the smoother of level 1..L and, with auto_relaxation, the estimate of
  * lambda_max(P A) it was scaled by (0 otherwise). No counterpart in the reference. */
 int tpss_mg_relaxation(const tpss_mg *mg, int level, double *relaxation, double *lambda_max);
-/* Level objects for direct use (level 0 = coarsest). */
+/* Level objects for direct use (level 0 = coarsest). The hierarchy's CUDA graphs (V-cycle,
+ * device CG loop) are captured at creation or first use with the levels' settings of that
+ * time; later changes to a level object are not seen by them. */
 int tpss_mg_level(tpss_mg *mg, int level, tpss_layout **layout, tpss_operator **op,
                   tpss_precond **precond);
 int tpss_mg_n_levels(const tpss_mg *mg, int *n_levels);

@@ -9,7 +9,7 @@
 //   SchwarzSmoother            smoother/schwarz_smoother.h:16-52, smoother_richardson.h:14-163
 //   MultigridSolver            apps/poisson_problem.h:642-755 (GMG + CG)
 //   C0IPBiharmonic             apps/biharmonic_problem.h, biharmonic_integrator.h (C0IP path)
-//   MLP, BatchSolver           no counterpart: learned local solver network, lockstep batches
+//   MLP, BatchSolver           no counterpart: learned local solver network, concurrent batches
 // Vectors are device pointers to FP64 arrays; streams are cudaStream_t passed as void*.
 // Header-only; link with libtpss_gpu.so.
 #pragma once
@@ -428,7 +428,7 @@ private:
   tpss_c0ip *handle_ = nullptr;
 };
 
-/* many independent CG + GMG problems solved in lockstep */
+/* many independent CG + GMG problems solved concurrently (device-side CG loops) */
 class BatchSolver
 {
 public:

@@ -1,4 +1,4 @@
-"""Batched lockstep solves: each problem gets its own CG + GMG result (same kernels, same order),
+"""Batched solves: each problem gets its own CG + GMG result (same kernels, same order),
 and a seeded sample of the benchmark family matches the CPU oracle's iteration counts."""
 import numpy as np
 import pytest
@@ -35,7 +35,7 @@ def test_batch_equals_individual_solves(tpss, cuda):
 def test_batch_sample_matches_oracle_iterations(tpss, oracle, cuda, precision):
     """A seeded sample of the batched problem family (drawn by tpss.draw_batch_problems, the
     rule of the 512-problem benchmark, with caps the CPU oracle finishes in seconds), solved in
-    lockstep with autotuned kernels and the dense coarse solve the batch needs: FP64 smoothers
+    a batch with autotuned kernels and the dense coarse solve the batch needs: FP64 smoothers
     give the oracle's CG + GMG iteration count within one (the oracle's coarse solver is CG to an
     absolute 1e-12, a slightly different preconditioner late in the solve than the exact dense
     coarse solve: on this sample 3D DGQ3 8^3 and 3D DGQ2 8^3 end one iteration apart, at 1.3 and

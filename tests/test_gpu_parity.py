@@ -520,6 +520,15 @@ def test_streamed_kernel_per_patch_tables(tpss, oracle, cuda, k, nc):
     for v in range(6):
         assert rel_err(run(tpss.LocalSolver.fd, 2, v), ref) <= 2e-5, v
         assert rel_err(run(tpss.LocalSolver.ksum, 2, v), ksum_color) <= 2e-5, v
+    # host buffers: the pipelined entry point runs the 4-layer-deep twin (5 for variant 4)
+    p = tpss.SchwarzPreconditioner()
+    p.initialize(sh, op, tpss.SchwarzPreconditioner.AdditionalData(
+        relaxation=0.6, precision=1, kernel_variant=2, stream_variant=4, local_solver=tpss.LocalSolver.ksum))
+    h_src = torch.tensor(src, dtype=torch.float64).pin_memory()
+    h_dst = torch.full((sh.n_dofs(),), float("nan"), dtype=torch.float64).pin_memory()
+    p.vmult_host(h_dst, h_src)
+    torch.cuda.synchronize()
+    assert np.array_equal(h_dst.numpy(), run(tpss.LocalSolver.ksum, 2, 5))
 
 
 @pytest.mark.parametrize("k,nc", [(4, (9, 6, 19)), (3, (7, 5, 13)), (2, (6, 6, 17)), (1, (5, 9, 18))])

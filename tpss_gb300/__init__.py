@@ -485,8 +485,9 @@ class C0IPBiharmonic:
 
 
 class BatchSolver:
-    """Many independent CG + GMG problems (unit-cube SIPG levels) solved in lockstep: one CG
-    iteration per active problem per round, one host synchronization per round."""
+    """Many independent CG + GMG problems (unit-cube SIPG levels) solved concurrently: every
+    problem's device-side CG loop (one CUDA graph) launched once on one of n_streams streams,
+    one host synchronization for the whole batch."""
 
     def __init__(self, problems, n_streams=8):
         """problems: list of dicts with MultigridSolver keyword arguments (dim, degree, n_rep,

@@ -14,6 +14,7 @@
 // The V-cycle can be captured in CUDA graphs: with the dense coarse solver the whole cycle is
 // one graph launch; with the CG coarse solver the down- and up-sweeps are two graphs around
 // the host-driven coarse iteration.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -45,6 +46,49 @@ __global__ void cg_update_p(int64_t n, double *__restrict__ p, const double *__r
   const double beta = *rz_new / *rz_old;
   for(int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     p[i] = fma(beta, p[i], z[i]);
+}
+
+// State of a CG solve whose iteration loop runs on the device: the loop is a conditional WHILE
+// node of a CUDA graph, its body one CG iteration followed by cg_loop_control, which sets the
+// condition (no host round trip per iteration).
+struct CgLoopState
+{
+  double tol;
+  int it, max_iter, hist_cap, converged;
+};
+
+__global__ void cg_loop_init(CgLoopState *st, double tol, int max_iter, int hist_cap)
+{
+  st->tol = tol;
+  st->it = 0;
+  st->max_iter = max_iter;
+  st->hist_cap = hist_cap;
+  st->converged = 0;
+}
+
+// p = z + beta p, beta = rz_new / rz_old; beta = 0 in the first iteration, whose p is zero
+// (the loop starts from p = 0), so that p = z
+__global__ void cg_update_p_loop(int64_t n, double *__restrict__ p, const double *__restrict__ z,
+                                 const double *__restrict__ rz_new, const double *__restrict__ rz_old,
+                                 const CgLoopState *__restrict__ st)
+{
+  const double beta = st->it == 0 ? 0.0 : *rz_new / *rz_old;
+  for(int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    p[i] = fma(beta, p[i], z[i]);
+}
+
+// counts the iteration, records ||r|| and continues the loop while ||r|| > tol and
+// it < max_iter (a NaN norm fails the test and runs to max_iter)
+__global__ void cg_loop_control(cudaGraphConditionalHandle h, const double *__restrict__ rr,
+                                double *__restrict__ hist, CgLoopState *__restrict__ st)
+{
+  const int it = st->it + 1;
+  st->it = it;
+  const double res = sqrt(*rr);
+  if(it < st->hist_cap) hist[it] = res;
+  const bool conv = res <= st->tol;
+  st->converged = conv;
+  cudaGraphSetConditional(h, (conv || it >= st->max_iter) ? 0u : 1u);
 }
 
 __global__ void dense_matvec(int n, const double *__restrict__ A, const double *__restrict__ x,
@@ -202,8 +246,11 @@ struct tpss_mg
   double *h_scal = nullptr;  // pinned
   const double *E = nullptr;
   cudaGraphExec_t g_full = nullptr, g_down = nullptr, g_up = nullptr;
-  cudaGraphExec_t g_iter = nullptr;  // one lockstep CG iteration of a batch (ub, r, p, ...)
-  DeviceBuffer<double> ub;           // batch solution vector the iteration graph updates
+  // the CG loop on the device (conditional WHILE node; body: one iteration on ub, r, p, ...)
+  cudaGraphExec_t g_loop = nullptr;
+  DeviceBuffer<double> ub;              // solution vector the loop graph updates
+  DeviceBuffer<double> hist;            // residual norms the loop records
+  DeviceBuffer<CgLoopState> loop_state;
   // graphs are captured on and launched into a private stream (capture is not possible on
   // the legacy default stream); events order it after / before the caller's stream
   cudaStream_t gstream = nullptr;
@@ -217,7 +264,7 @@ struct tpss_mg
     if(g_full) cudaGraphExecDestroy(g_full);
     if(g_down) cudaGraphExecDestroy(g_down);
     if(g_up) cudaGraphExecDestroy(g_up);
-    if(g_iter) cudaGraphExecDestroy(g_iter);
+    if(g_loop) cudaGraphExecDestroy(g_loop);
     for(auto &l : lv)
     {
       tpss_precond_destroy(l.P);
@@ -468,6 +515,12 @@ void autotune_level(MgLevel &lv, const tpss_mg_desc &d)
 }
 }  // namespace
 
+namespace
+{
+bool device_loop(const tpss_mg *mg);
+void prepare_loop(tpss_mg *mg, int max_iter);
+}  // namespace
+
 extern "C" int tpss_mg_create(const tpss_mg_desc *d, tpss_mg **out)
 {
   return guarded([&] {
@@ -563,6 +616,13 @@ extern "C" int tpss_mg_create(const tpss_mg_desc *d, tpss_mg **out)
       for(int l = 1; l < nl; ++l) scale_relaxation(*mg, mg->lv[l]);
     if(d->autotune)
       for(int l = 1; l < nl; ++l) autotune_level(mg->lv[l], *d);
+    // the device CG loop is captured here (after an eager V-cycle on r = 0), so that a solve
+    // launches it directly
+    if(device_loop(mg.get()))
+    {
+      TPSS_CUDA(cudaMemset(mg->r.ptr, 0, sizeof(double) * mg->r.n));
+      prepare_loop(mg.get(), 255);
+    }
     *out = mg.release();
   });
 }
@@ -607,6 +667,126 @@ extern "C" int tpss_mg_vmult(tpss_mg *mg, double *dst, const double *src, void *
   });
 }
 
+namespace
+{
+// r = f, ||r||^2 into the pinned host slot (u := 0 on the device loop's ub)
+void cg_start(tpss_mg *mg, double *u, const double *f, cudaStream_t s)
+{
+  MgLevel &top = mg->lv.back();
+  const int64_t n = top.L->n_dofs;
+  TPSS_CUDA(cudaMemsetAsync(u, 0, sizeof(double) * n, s));
+  TPSS_CUDA(cudaMemcpyAsync(mg->r.ptr, f, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+  vec_dot(n, mg->r.ptr, mg->r.ptr, mg->partial.ptr, mg->scal.ptr + 10, s);
+  TPSS_CUDA(cudaMemcpyAsync(mg->h_scal + 4, mg->scal.ptr + 10, sizeof(double), cudaMemcpyDeviceToHost, s));
+}
+
+// One CG iteration of the device loop: z = V(r); rz_new = r.z; p = z + beta p (beta = 0 first);
+// rz = rz_new; then alpha = rz / p.Ap, ub += alpha p, r -= alpha A p, ||r||^2 -- the order and
+// the kernels of the host loop of tpss_mg_cg_solve -- and cg_loop_control.
+void loop_body(tpss_mg *mg, cudaGraphConditionalHandle h, cudaStream_t s)
+{
+  MgLevel &top = mg->lv.back();
+  const int64_t n = top.L->n_dofs;
+  double *r = mg->r.ptr, *p = mg->p.ptr, *Ap = mg->Ap.ptr, *u = mg->ub.ptr;
+  double *d_rz = mg->scal.ptr + 8, *d_pAp = mg->scal.ptr + 9, *d_rr = mg->scal.ptr + 10,
+         *d_rz_new = mg->scal.ptr + 11;
+  CgLoopState *st = mg->loop_state.ptr;
+  TPSS_CUDA(cudaMemcpyAsync(top.b.ptr, r, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+  vcycle(mg, s);
+  vec_dot(n, r, top.x.ptr, mg->partial.ptr, d_rz_new, s);
+  cg_update_p_loop<<<grid_for(n), 256, 0, s>>>(n, p, top.x.ptr, d_rz_new, d_rz, st);
+  TPSS_CUDA(cudaMemcpyAsync(d_rz, d_rz_new, sizeof(double), cudaMemcpyDeviceToDevice, s));
+  operator_apply(top.op, Ap, p, s);
+  vec_dot(n, p, Ap, mg->partial.ptr, d_pAp, s);
+  cg_update_xr<<<grid_for(n), 256, 0, s>>>(n, u, r, p, Ap, d_rz, d_pAp);
+  vec_dot(n, r, r, mg->partial.ptr, d_rr, s);
+  cg_loop_control<<<1, 1, 0, s>>>(h, d_rr, mg->hist.ptr, st);
+  TPSS_CUDA(cudaGetLastError());
+}
+
+// The loop graph: one conditional WHILE node (condition 1 at every launch) whose body is
+// captured from loop_body with the V-cycle's kernels inline. Captured once per hierarchy after
+// an eager V-cycle (its lazy set-up -- scratch, lists -- happens outside the capture).
+void capture_loop(tpss_mg *mg, int hist_cap)
+{
+  MgLevel &top = mg->lv.back();
+  const int64_t n = top.L->n_dofs;
+  if(mg->ub.n < (size_t)n) mg->ub.resize(n);
+  if(mg->loop_state.n == 0) mg->loop_state.resize(1);
+  mg->hist.resize(hist_cap);
+  if(mg->g_loop)
+  {
+    TPSS_CUDA(cudaGraphExecDestroy(mg->g_loop));
+    mg->g_loop = nullptr;
+  }
+  cudaStream_t s = mg->gstream;
+  TPSS_CUDA(cudaMemcpyAsync(top.b.ptr, mg->r.ptr, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+  vcycle(mg, s);
+  TPSS_CUDA(cudaStreamSynchronize(s));
+  cudaGraph_t g = nullptr;
+  TPSS_CUDA(cudaGraphCreate(&g, 0));
+  const int use_graph = mg->desc.use_graph;
+  try
+  {
+    cudaGraphConditionalHandle h = 0;
+    TPSS_CUDA(cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams np = {};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = h;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t node = nullptr;
+    TPSS_CUDA(cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &np));
+    cudaGraph_t body = np.conditional.phGraph_out[0];
+    TPSS_CUDA(cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    mg->desc.use_graph = 0;  // V-cycle kernels inline in the body
+    try
+    {
+      loop_body(mg, h, s);
+    }
+    catch(...)
+    {
+      cudaGraph_t tmp = nullptr;
+      cudaStreamEndCapture(s, &tmp);
+      throw;
+    }
+    mg->desc.use_graph = use_graph;
+    cudaGraph_t captured = nullptr;
+    TPSS_CUDA(cudaStreamEndCapture(s, &captured));  // the body, owned by the node
+    TPSS_CUDA(cudaGraphInstantiate(&mg->g_loop, g, 0));
+  }
+  catch(...)
+  {
+    mg->desc.use_graph = use_graph;
+    cudaGraphDestroy(g);
+    throw;
+  }
+  cudaGraphDestroy(g);
+}
+
+bool device_loop(const tpss_mg *mg) { return mg->desc.use_graph && mg->desc.coarse_solver == 1; }
+
+// ensure the loop graph for max_iter iterations (the residual history holds max_iter + 1)
+void prepare_loop(tpss_mg *mg, int max_iter)
+{
+  const size_t cap = std::max<size_t>(256, (size_t)max_iter + 1);
+  if(!mg->g_loop || mg->hist.n < (size_t)max_iter + 1) capture_loop(mg, (int)cap);
+}
+
+// launch the device loop (p := 0, state reset) on stream s; r holds f, ub zero
+void launch_loop(tpss_mg *mg, double tol, int max_iter, cudaStream_t s, bool private_stream)
+{
+  const int64_t n = mg->lv.back().L->n_dofs;
+  TPSS_CUDA(cudaMemsetAsync(mg->p.ptr, 0, sizeof(double) * n, s));
+  cg_loop_init<<<1, 1, 0, s>>>(mg->loop_state.ptr, tol, max_iter, (int)mg->hist.n);
+  TPSS_CUDA(cudaGetLastError());
+  if(private_stream)
+    launch_graph(mg, mg->g_loop, s);
+  else
+    TPSS_CUDA(cudaGraphLaunch(mg->g_loop, s));
+}
+}  // namespace
+
 extern "C" int tpss_mg_cg_solve(tpss_mg *mg, double *u, const double *f, double rel_tol,
                                 double abs_tol, int max_iter, int *iterations,
                                 double *res_history, void *stream)
@@ -620,6 +800,36 @@ extern "C" int tpss_mg_cg_solve(tpss_mg *mg, double *u, const double *f, double 
     double *r = mg->r.ptr, *p = mg->p.ptr, *Ap = mg->Ap.ptr;
     double *d_rz = mg->scal.ptr + 8, *d_pAp = mg->scal.ptr + 9, *d_rr = mg->scal.ptr + 10,
            *d_rz_new = mg->scal.ptr + 11;
+    if(device_loop(mg))
+    {
+      // the iteration loop on the device: one graph launch, one synchronization
+      if(mg->ub.n < (size_t)n) mg->ub.resize(n);
+      cg_start(mg, mg->ub.ptr, f, s);
+      TPSS_CUDA(cudaStreamSynchronize(s));
+      const double res0 = std::sqrt(mg->h_scal[4]);
+      if(res_history) res_history[0] = res0;
+      const double tol = std::max(abs_tol, rel_tol * res0);
+      int it = 0;
+      bool converged = res0 <= tol;
+      if(!converged && max_iter > 0)
+      {
+        prepare_loop(mg, max_iter);
+        launch_loop(mg, tol, max_iter, s, true);
+        CgLoopState st{};
+        TPSS_CUDA(cudaMemcpyAsync(mg->h_scal + 8, mg->loop_state.ptr, sizeof(CgLoopState),
+                                  cudaMemcpyDeviceToHost, s));
+        TPSS_CUDA(cudaStreamSynchronize(s));
+        std::memcpy(&st, mg->h_scal + 8, sizeof(CgLoopState));
+        it = st.it;
+        converged = st.converged != 0;
+        if(res_history && it > 0)
+          TPSS_CUDA(cudaMemcpy(res_history + 1, mg->hist.ptr + 1, sizeof(double) * it, cudaMemcpyDeviceToHost));
+      }
+      TPSS_CUDA(cudaMemcpyAsync(u, mg->ub.ptr, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+      *iterations = converged ? it : -1;
+      if(!converged) fail(TPSS_ERR_NOT_CONVERGED, "CG did not reach the tolerance within max_iter");
+      return;
+    }
     TPSS_CUDA(cudaMemsetAsync(u, 0, sizeof(double) * n, s));
     TPSS_CUDA(cudaMemcpyAsync(r, f, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
     vec_dot(n, r, r, mg->partial.ptr, d_rr, s);
@@ -664,102 +874,25 @@ extern "C" int tpss_mg_cg_solve(tpss_mg *mg, double *u, const double *f, double 
   });
 }
 
-// ---- batched solves: CG on many independent hierarchies in lockstep ------------------------
-// Every round launches, for every active problem, one CUDA graph holding a whole CG iteration
-// (operator, device-side alpha / beta, the next V-cycle), then synchronizes once and reads all
-// residual norms; a problem leaves the batch when it meets its ReductionControl tolerance
+// ---- batched solves: many independent hierarchies ------------------------------------------
+// Every problem's CG runs as its device loop graph (conditional WHILE node), launched once on
+// one of n_streams streams: the problems are dealt to the streams largest first, each to the
+// stream with the least work so far (estimated as DoFs x (degree + 1) plus a fixed cost per
+// problem for its launch-bound small levels); one host synchronization at the end reads all
+// iteration counts. A problem stops at its own ReductionControl tolerance
 // (apps/rt_parameter.h:39-41).
 struct tpss_batch
 {
   std::vector<tpss_mg *> mg;
   std::vector<cudaStream_t> streams;
+  std::vector<int> stream_of;  // stream of every problem
+  std::vector<int> order;      // launch order: estimated work, largest first
   ~tpss_batch()
   {
     for(tpss_mg *m : mg) delete m;
     for(cudaStream_t s : streams) cudaStreamDestroy(s);
   }
 };
-
-namespace
-{
-struct CgRun
-{
-  double *u = nullptr;
-  double tol = 0.0;
-  int it = 0;
-  bool done = false, converged = false;
-};
-
-void cg_start(tpss_mg *mg, double *u, const double *f, cudaStream_t s)
-{
-  MgLevel &top = mg->lv.back();
-  const int64_t n = top.L->n_dofs;
-  TPSS_CUDA(cudaMemsetAsync(u, 0, sizeof(double) * n, s));
-  TPSS_CUDA(cudaMemcpyAsync(mg->r.ptr, f, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
-  vec_dot(n, mg->r.ptr, mg->r.ptr, mg->partial.ptr, mg->scal.ptr + 10, s);
-  TPSS_CUDA(cudaMemcpyAsync(mg->h_scal + 4, mg->scal.ptr + 10, sizeof(double), cudaMemcpyDeviceToHost, s));
-}
-
-// z = V(r), then p = z (first) or p = z + (rz_new / rz) p; rz updated
-void cg_precondition(tpss_mg *mg, bool first, cudaStream_t s)
-{
-  MgLevel &top = mg->lv.back();
-  const int64_t n = top.L->n_dofs;
-  double *d_rz = mg->scal.ptr + 8, *d_rz_new = mg->scal.ptr + 11;
-  TPSS_CUDA(cudaMemcpyAsync(top.b.ptr, mg->r.ptr, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
-  vcycle(mg, s);
-  if(first)
-  {
-    TPSS_CUDA(cudaMemcpyAsync(mg->p.ptr, top.x.ptr, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
-    vec_dot(n, mg->r.ptr, top.x.ptr, mg->partial.ptr, d_rz, s);
-  }
-  else
-  {
-    vec_dot(n, mg->r.ptr, top.x.ptr, mg->partial.ptr, d_rz_new, s);
-    cg_update_p<<<grid_for(n), 256, 0, s>>>(n, mg->p.ptr, top.x.ptr, d_rz_new, d_rz);
-    TPSS_CUDA(cudaMemcpyAsync(d_rz, d_rz_new, sizeof(double), cudaMemcpyDeviceToDevice, s));
-  }
-}
-
-// x += alpha p, r -= alpha A p, |r|^2 copied to the pinned host slot
-void cg_iterate(tpss_mg *mg, double *u, cudaStream_t s)
-{
-  MgLevel &top = mg->lv.back();
-  const int64_t n = top.L->n_dofs;
-  double *d_rz = mg->scal.ptr + 8, *d_pAp = mg->scal.ptr + 9, *d_rr = mg->scal.ptr + 10;
-  operator_apply(top.op, mg->Ap.ptr, mg->p.ptr, s);
-  vec_dot(n, mg->p.ptr, mg->Ap.ptr, mg->partial.ptr, d_pAp, s);
-  cg_update_xr<<<grid_for(n), 256, 0, s>>>(n, u, mg->r.ptr, mg->p.ptr, mg->Ap.ptr, d_rz, d_pAp);
-  vec_dot(n, mg->r.ptr, mg->r.ptr, mg->partial.ptr, d_rr, s);
-  TPSS_CUDA(cudaMemcpyAsync(mg->h_scal + 4, d_rr, sizeof(double), cudaMemcpyDeviceToHost, s));
-}
-}  // namespace
-
-// one lockstep iteration: cg_iterate on ub, then the next preconditioning (run also after the
-// last iteration; it changes p and the V-cycle vectors only), captured into one graph with the
-// V-cycle's kernels inline. Capture after the first V-cycle: its lazy set-up (scratch, lists)
-// is done by then.
-void batch_iteration(tpss_mg *mg, cudaStream_t s)
-{
-  cg_iterate(mg, mg->ub.ptr, s);
-  cg_precondition(mg, false, s);
-}
-
-void capture_iteration(tpss_mg *mg)
-{
-  const int use_graph = mg->desc.use_graph;
-  mg->desc.use_graph = 0;  // V-cycle kernels inline in this graph
-  try
-  {
-    capture(mg, batch_iteration, &mg->g_iter);
-  }
-  catch(...)
-  {
-    mg->desc.use_graph = use_graph;
-    throw;
-  }
-  mg->desc.use_graph = use_graph;
-}
 
 extern "C" int tpss_batch_create(const tpss_mg_desc *descs, int n_problems, int n_streams, tpss_batch **out)
 {
@@ -768,21 +901,34 @@ extern "C" int tpss_batch_create(const tpss_mg_desc *descs, int n_problems, int 
     *out = nullptr;
     auto b = std::make_unique<tpss_batch>();
     for(int i = 0; i < n_problems; ++i)
-      TPSS_REQUIRE(descs[i].coarse_solver == 1,
-                   "batched solves run every CG iteration as one CUDA graph: they need the dense coarse "
-                   "solver (coarse_solver = 1); the coarse CG waits for the host");
+      TPSS_REQUIRE(descs[i].coarse_solver == 1 && descs[i].use_graph,
+                   "batched solves run every CG loop as one CUDA graph: they need the dense coarse "
+                   "solver (coarse_solver = 1; the coarse CG waits for the host) and use_graph = 1");
+    std::vector<double> work(n_problems);
     for(int i = 0; i < n_problems; ++i)
     {
       tpss_mg *m = nullptr;
       const int rc = tpss_mg_create(&descs[i], &m);
       if(rc) fail(rc, std::string("problem ") + std::to_string(i) + ": " + tpss_last_error());
       b->mg.push_back(m);
+      work[i] = double(m->lv.back().L->n_dofs) * (descs[i].degree + 1) + 2.0e5;
     }
     for(int i = 0; i < n_streams; ++i)
     {
       cudaStream_t s;
       TPSS_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
       b->streams.push_back(s);
+    }
+    b->order.resize(n_problems);
+    for(int i = 0; i < n_problems; ++i) b->order[i] = i;
+    std::stable_sort(b->order.begin(), b->order.end(), [&](int x, int y) { return work[x] > work[y]; });
+    std::vector<double> load(n_streams, 0.0);
+    b->stream_of.assign(n_problems, 0);
+    for(int i : b->order)
+    {
+      const int k = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+      b->stream_of[i] = k;
+      load[k] += work[i];
     }
     *out = b.release();
   });
@@ -801,13 +947,13 @@ extern "C" int tpss_batch_solve(tpss_batch *b, double *const *u, const double *c
 {
   return guarded([&] {
     TPSS_REQUIRE(b && u && f && iterations && max_iter >= 0, "invalid argument");
-    const int P = (int)b->mg.size(), S = (int)b->streams.size();
+    const int P = (int)b->mg.size();
     cudaStream_t caller = as_stream(stream);
+    auto st_of = [&](int i) { return b->streams[b->stream_of[i]]; };
     cudaEvent_t ev;
     TPSS_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
     TPSS_CUDA(cudaEventRecord(ev, caller));
     for(cudaStream_t s : b->streams) TPSS_CUDA(cudaStreamWaitEvent(s, ev, 0));
-    std::vector<CgRun> run(P);
     auto sync_all = [&]() {
       for(cudaStream_t s : b->streams) TPSS_CUDA(cudaStreamSynchronize(s));
     };
@@ -817,49 +963,42 @@ extern "C" int tpss_batch_solve(tpss_batch *b, double *const *u, const double *c
       tpss_mg *m = b->mg[i];
       const size_t n = (size_t)m->lv.back().L->n_dofs;
       if(m->ub.n < n) m->ub.resize(n);
-      run[i].u = u[i];
-      cg_start(m, m->ub.ptr, f[i], b->streams[i % S]);
+      cg_start(m, m->ub.ptr, f[i], st_of(i));
     }
     sync_all();
-    int active = 0;
+    std::vector<double> tol(P);
+    std::vector<char> active(P), converged(P);
+    std::vector<int> its(P, 0);
     for(int i = 0; i < P; ++i)
     {
       const double r0 = std::sqrt(b->mg[i]->h_scal[4]);
-      run[i].tol = std::max(abs_tol, rel_tol * r0);
-      run[i].done = run[i].converged = r0 <= run[i].tol;
-      if(!run[i].done)
-      {
-        cg_precondition(b->mg[i], true, b->streams[i % S]);
-        ++active;
-      }
+      tol[i] = std::max(abs_tol, rel_tol * r0);
+      converged[i] = r0 <= tol[i];
+      active[i] = !converged[i] && max_iter > 0;
     }
-    // iteration graphs (captured once per problem, after its first V-cycle above)
+    // loop graphs: captured once per problem (after an eager V-cycle on its private stream)
+    for(int i = 0; i < P; ++i)
+      if(active[i]) prepare_loop(b->mg[i], max_iter);
+    for(int i : b->order)
+      if(active[i]) launch_loop(b->mg[i], tol[i], max_iter, st_of(i), false);
+    for(int i = 0; i < P; ++i)
+      if(active[i])
+        TPSS_CUDA(cudaMemcpyAsync(b->mg[i]->h_scal + 8, b->mg[i]->loop_state.ptr, sizeof(CgLoopState),
+                                  cudaMemcpyDeviceToHost, st_of(i)));
     sync_all();
     for(int i = 0; i < P; ++i)
-      if(!run[i].done && !b->mg[i]->g_iter) capture_iteration(b->mg[i]);
-    while(active > 0)
     {
-      for(int i = 0; i < P; ++i)
-        if(!run[i].done) TPSS_CUDA(cudaGraphLaunch(b->mg[i]->g_iter, b->streams[i % S]));
-      sync_all();
-      for(int i = 0; i < P; ++i)
-      {
-        if(run[i].done) continue;
-        ++run[i].it;
-        const double res = std::sqrt(b->mg[i]->h_scal[4]);
-        if(res <= run[i].tol || run[i].it >= max_iter)
-        {
-          run[i].done = true;
-          run[i].converged = res <= run[i].tol;
-          --active;
-        }
-      }
+      if(!active[i]) continue;
+      CgLoopState st{};
+      std::memcpy(&st, b->mg[i]->h_scal + 8, sizeof(CgLoopState));
+      its[i] = st.it;
+      converged[i] = st.converged != 0;
     }
     for(int i = 0; i < P; ++i)
     {
       tpss_mg *m = b->mg[i];
-      TPSS_CUDA(cudaMemcpyAsync(run[i].u, m->ub.ptr, sizeof(double) * m->lv.back().L->n_dofs,
-                                cudaMemcpyDeviceToDevice, b->streams[i % S]));
+      TPSS_CUDA(cudaMemcpyAsync(u[i], m->ub.ptr, sizeof(double) * m->lv.back().L->n_dofs,
+                                cudaMemcpyDeviceToDevice, st_of(i)));
     }
     for(cudaStream_t s : b->streams)
     {
@@ -870,8 +1009,8 @@ extern "C" int tpss_batch_solve(tpss_batch *b, double *const *u, const double *c
     bool all = true;
     for(int i = 0; i < P; ++i)
     {
-      iterations[i] = run[i].converged ? run[i].it : -1;
-      all = all && run[i].converged;
+      iterations[i] = converged[i] ? its[i] : -1;
+      all = all && converged[i];
     }
     if(!all) fail(TPSS_ERR_NOT_CONVERGED, "some problems of the batch did not converge");
   });
