@@ -418,12 +418,16 @@ def test_fp32_streamed_and_color_kernels(tpss, oracle, cuda, k, nc, variant):
 
 
 @pytest.mark.parametrize("k,nc,variant", [(3, (6, 5, 10), 0), (4, (8, 11, 9), 4), (4, (8, 11, 9), 6),
-                                         (4, (7, 5, 12), 7)])
+                                         (4, (7, 5, 12), 7), (5, (6, 7, 9), 4), (5, (5, 6, 7), 1)])
 def test_streamed_kernel_general_layouts(tpss, oracle, cuda, k, nc, variant):
     """Permuted cell numbering, non-uniform tensor-product h (1-D problems without mirror
     symmetry everywhere, so the plane passes run their full-matrix path) and RAS weights, for
-    pencil and plane decompositions."""
+    pencil and plane decompositions. Tolerance 2e-5, at degree 5 3e-4: FP32 fast
+    diagonalization of the degree-5 1-D problems on these graded cells (widths up to 3x apart)
+    ends 1.4e-4 from the FP64 oracle in the per-color kernel as well (FP64 kernels: 3e-11), so
+    at degree 5 the streamed result must also be as close as the per-color kernel's."""
     import torch
+    tol = 2e-5 if k <= 4 else 3e-4
     g = np.random.default_rng(11)
     h = [g.uniform(0.5, 1.5, n) for n in nc]
     h = [x / x.sum() for x in h]
@@ -442,7 +446,15 @@ def test_streamed_kernel_general_layouts(tpss, oracle, cuda, k, nc, variant):
         p.vmult(d, s)
         ref = oracle.schwarz_vmult(3, k, nc, src, patch_variant=1, omega=0.7, h=h,
                                    cell_start=cell_start, use_ras=ras)
-        assert rel_err(d.cpu().numpy(), ref) <= 2e-5, ras
+        err = rel_err(d.cpu().numpy(), ref)
+        assert err <= tol, ras
+        if k == 5:
+            pc = tpss.SchwarzPreconditioner()
+            pc.initialize(sh, None, tpss.SchwarzPreconditioner.AdditionalData(
+                relaxation=0.7, precision=1, kernel_variant=1, use_ras_weights=ras))
+            dc = torch.empty_like(s)
+            pc.vmult(dc, s)
+            assert err <= 1.1 * rel_err(dc.cpu().numpy(), ref), ras
 
 
 @pytest.mark.parametrize("variant", [0, 6])
@@ -531,7 +543,8 @@ def test_streamed_kernel_per_patch_tables(tpss, oracle, cuda, k, nc):
     assert np.array_equal(h_dst.numpy(), run(tpss.LocalSolver.ksum, 2, 5))
 
 
-@pytest.mark.parametrize("k,nc", [(4, (9, 6, 19)), (3, (7, 5, 13)), (2, (6, 6, 17)), (1, (5, 9, 18))])
+@pytest.mark.parametrize("k,nc", [(5, (6, 5, 11)), (4, (9, 6, 19)), (3, (7, 5, 13)), (2, (6, 6, 17)),
+                                  (1, (5, 9, 18))])
 def test_streamed_variants_and_autotune(tpss, oracle, cuda, k, nc):
     """Every work decomposition of the streamed kernel gives the oracle's result; the autotuner
     keeps one of them and leaves dst = P src."""
@@ -596,7 +609,7 @@ def test_color_kernel_variants_and_autotune(tpss, oracle, cuda, dim, k, nc, pv, 
 
 @pytest.mark.parametrize("k,nc,variant", [(4, (9, 6, 19), 0), (3, (7, 5, 33), 2), (2, (6, 6, 17), 3), (1, (5, 9, 40), 1),
                                          (4, (10, 7, 21), 4), (3, (6, 9, 18), 5), (4, (8, 11, 23), 6),
-                                         (4, (7, 5, 12), 7)])
+                                         (4, (7, 5, 12), 7), (5, (6, 5, 13), 0), (5, (5, 6, 11), 4)])
 def test_vmult_host_buffers_pipelined(tpss, oracle, cuda, k, nc, variant):
     """The host-buffer entry point (copies pipelined with the streamed kernel along z) gives
     the oracle's result and the bits of the device path with the decomposition the pipeline

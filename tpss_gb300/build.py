@@ -27,6 +27,7 @@ UNITS = [
     ("setup.cu", []), ("eigen.cu", []), ("layout.cu", []), ("precond.cu", []),
     ("operator.cu", []), ("mg.cu", []), ("diag.cu", []), ("stream3d.cu", []), ("mapped.cu", []), ("mapped_mf.cu", []), ("local.cu", []), ("mlp.cu", []), ("learned.cu", []), ("c0ip.cu", []),
     ("plane_inst.cu", ["-DPLANE_BZ=8"]), ("plane_inst.cu", ["-DPLANE_BZ=4"]),
+    ("stream_k5.cu", ["-DK5_PART=0"]), ("stream_k5.cu", ["-DK5_PART=1"]),
     ("fd_inst.cu", ["-DFD_T=float", "-DFD_DIM=2"]),
     ("fd_inst.cu", ["-DFD_T=float", "-DFD_DIM=3"]),
     ("fd_inst.cu", ["-DFD_T=double", "-DFD_DIM=2"]),

@@ -484,6 +484,10 @@ bool launch_plane3d_host_bz8(const tpss_layout &L, const StreamLaunch &l, HostPi
                              const double *h_src, cudaStream_t s);
 bool launch_plane3d_host_bz4(const tpss_layout &L, const StreamLaunch &l, HostPipe &pipe, double *h_dst,
                              const double *h_src, cudaStream_t s);
+// degree-5 decompositions of the streamed smoother (4 x 2 vertex columns, stream_k5.cu)
+bool launch_stream3d_k5(const tpss_layout &L, const StreamLaunch &l, cudaStream_t s);
+bool launch_stream3d_host_k5(const tpss_layout &L, const StreamLaunch &l, HostPipe &pipe, double *h_dst,
+                             const double *h_src, cudaStream_t s);
 int stream_variant_count(const tpss_layout &L);
 bool launch_stream3d(const tpss_layout &L, const StreamLaunch &l, cudaStream_t s);
 

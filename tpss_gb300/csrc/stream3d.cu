@@ -20,7 +20,7 @@ bool stream_supported(const tpss_layout &L)
   // per-patch 1-D problems (distorted levels) up to k = 3: their table slots for the 16 patches
   // of a vertex layer fit next to the staged layers
   return L.dim == 3 && L.patch_variant == TPSS_PATCH_VERTEX && (!L.per_patch_fd || L.k <= 3) && L.k >= 1 &&
-         L.k <= 4 && L.nc[0] >= 2 && L.nc[1] >= 2 && L.nc[2] >= 2;
+         L.k <= 5 && L.nc[0] >= 2 && L.nc[1] >= 2 && L.nc[2] >= 2;
 }
 
 // the same decomposition with per-patch 1-D problems (registers hold these kernels to one CTA per
@@ -158,6 +158,7 @@ bool launch_stream3d_host(const tpss_layout &L, const StreamLaunch &l, HostPipe 
   case 2: return launch_variant_host<3>(L, l, pp, h_dst, h_src, s, v);
   case 3: return launch_variant_host<4>(L, l, pp, h_dst, h_src, s, v);
   case 4: return launch_variant_host<5>(L, l, pp, h_dst, h_src, s, v);
+  case 5: return launch_stream3d_host_k5(L, l, pp, h_dst, h_src, s);  // stream_k5.cu
   default: return false;
   }
 }
@@ -171,6 +172,7 @@ bool launch_stream3d(const tpss_layout &L, const StreamLaunch &l, cudaStream_t s
   case 2: return launch_variant<3>(L, l, s, v);
   case 3: return launch_variant<4>(L, l, s, v);
   case 4: return launch_variant<5>(L, l, s, v);
+  case 5: return launch_stream3d_k5(L, l, s);  // stream_k5.cu
   default: return false;
   }
 }

@@ -982,17 +982,25 @@ __global__ void fixup_kernel(StreamArgs a)
 
 // The same sums from a precomputed list of the shared cells: per record (10 int64) the first
 // dst DoF of the cell, the partial count (low 32 bits) and the RAS scale bits (high 32 bits),
-// then up to 8 halo offsets in the fixup_kernel order. Blocks of 128 threads take
-// 128 / CD cells at a time, one thread per cell DoF; no index arithmetic per DoF.
+// then up to 8 halo offsets in the fixup_kernel order. Blocks of fixup_threads<C>() threads (128,
+// or CD rounded up to a warp multiple when a cell has more than 128 DoFs) take
+// fixup_threads / CD cells at a time, one thread per cell DoF; no index arithmetic per DoF.
 constexpr int kFixRec = 10;
 
 template<class C>
-__global__ void __launch_bounds__(128) fixup_list_kernel(const int64_t *__restrict__ rec, int64_t n,
-                                                         const float *__restrict__ halo,
-                                                         double *__restrict__ dst)
+__host__ __device__ constexpr int fixup_threads()
+{
+  return C::CD <= 128 ? 128 : (C::CD + 31) / 32 * 32;
+}
+
+template<class C>
+__global__ void __launch_bounds__(fixup_threads<C>()) fixup_list_kernel(const int64_t *__restrict__ rec, int64_t n,
+                                                                        const float *__restrict__ halo,
+                                                                        double *__restrict__ dst)
 {
   constexpr int CD = C::CD;
-  constexpr int PER = 128 / CD;
+  constexpr int PER = fixup_threads<C>() / CD;
+  static_assert(PER >= 1, "a block covers at least one cell");
   const int lc = threadIdx.x / CD, e = threadIdx.x % CD;
   if(lc >= PER) return;
   for(int64_t r = (int64_t)blockIdx.x * PER + lc; r < n; r += (int64_t)gridDim.x * PER)

@@ -137,9 +137,10 @@ template<class C>
 void launch_fixup_range(const stream::StreamArgs &a, const int64_t *rec, int64_t n, cudaStream_t s)
 {
   if(n <= 0) return;
-  constexpr int per = 128 / C::CD;
+  constexpr int threads = stream::fixup_threads<C>(), per = threads / C::CD;
+  static_assert(per >= 1, "a block covers at least one cell");
   const int64_t fb = (n + per - 1) / per, fcap = (int64_t)num_sms() * 16;
-  stream::fixup_list_kernel<C><<<(int)(fb < fcap ? fb : fcap), 128, 0, s>>>(rec, n, a.halo, a.dst);
+  stream::fixup_list_kernel<C><<<(int)(fb < fcap ? fb : fcap), threads, 0, s>>>(rec, n, a.halo, a.dst);
 }
 
 // src and dst in host memory: the level is cut into chunks of z-items; per chunk the cell layers
