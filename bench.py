@@ -77,12 +77,16 @@ def parse():
                          "all-FP32 and all-FP64: iterations and seconds, one JSON line")
     ap.add_argument("--no-dgq3-2d", action="store_true",
                     help="skip the 2D SIPG DGQ3 64^2 section (both penalty modes)")
-    ap.add_argument("--profile-case", choices=["mapped", "perpatch", "c0ip", "mlp", "host"],
+    ap.add_argument("--profile-case", choices=["mapped", "perpatch", "cg2d", "cg2d_eager", "cg3dk5_eager", "c0ip",
+                                               "mlp", "host"],
                     help="run one small workload of a secondary kernel three times and exit (the "
                          "commands the ncu profiles capture): mapped = mapped SIPG operator on a "
                          "distorted 3D DGQ3 24^3 level; perpatch = FP32 smoother on per-patch 1-D "
                          "problems (distorted 3D DGQ3 56^3, surrogate widths), streamed decomposition 4 "
-                         "and the per-color kernel; c0ip = C0IP FE_Q(3) 512^2 operator and "
+                         "and the per-color kernel; cg2d = CG + V-cycle on 2D SIPG DGQ3 64^2 (2 root "
+                         "cells, damping 0.25, dense coarse solve), one solve after a warm-up solve (cg2d_eager: the same "
+                         "without CUDA graphs, every kernel launched from the host); cg3dk5_eager = the "
+                         "same for 3D SIPG DGQ5 32^3 with FP32 smoothers (the batch's largest problems); c0ip = C0IP FE_Q(3) 512^2 operator and "
                          "FP32 Bilaplacian-FD smoother; mlp = one training epoch of the "
                          "87 -> 3 x 64 -> 108 network on 119,164 samples; host = the FP32 "
                          "smoother between pinned host buffers on 3D DGQ4 64^3")
@@ -952,6 +956,27 @@ def profile_case(args):
             ms[label] = e0.elapsed_time(e1) / 10
             del p
         print(json.dumps({"profile_case": name, "n_dofs": sh.n_dofs(), "ms_per_vmult": ms}))
+    elif name in ("cg2d", "cg2d_eager"):
+        # small-problem latency: every kernel of a 65,536-DoF solve (20 iterations)
+        mg = tpss.MultigridSolver(2, 3, 2, 64, relaxation=0.25, precision=tpss.Precision.fp64,
+                                  coarse_solver=1, use_graph=name == "cg2d")
+        f = torch.rand(mg.n_dofs(), dtype=torch.float64, device="cuda") * 2 - 1
+        u = torch.zeros_like(f)
+        mg.solve(u, f, rel_tol=1e-8)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        it, _ = mg.solve(u, f, rel_tol=1e-8)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_case": name, "iterations": it, "seconds": time.perf_counter() - t0}))
+    elif name == "cg3dk5_eager":
+        mg = tpss.MultigridSolver(3, 5, 1, 32, precision=tpss.Precision.fp32, coarse_solver=1, use_graph=False,
+                                  autotune=True)
+        f = torch.rand(mg.n_dofs(), dtype=torch.float64, device="cuda") * 2 - 1
+        u = torch.zeros_like(f)
+        t0 = time.perf_counter()
+        it, _ = mg.solve(u, f, rel_tol=1e-8)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_case": name, "iterations": it, "seconds": time.perf_counter() - t0}))
     elif name == "c0ip":
         P = tpss.C0IPBiharmonic(3, 2, 512, local_solver=tpss.LocalSolver.fd, precision=tpss.Precision.fp32)
         x = torch.rand(P.n_dofs(), dtype=torch.float64, device="cuda")

@@ -162,7 +162,8 @@ typedef struct tpss_precond_desc
   int check_finite;            /* 1: vmult checks that dst is finite (one extra reduction) */
   int kernel_variant;          /* additive smoother kernel: TPSS_KERNEL_AUTO, TPSS_KERNEL_COLOR
                                   (one fused launch per color) or TPSS_KERNEL_STREAM (3D vertex
-                                  patches, FP32, k <= 4: column-streamed, one pass) */
+                                  patches, FP32, k <= 5 -- per-patch 1-D problems of distorted
+                                  levels k <= 3: column-streamed, one pass) */
   int stream_variant;          /* initial work decomposition of the smoother kernel (see
                                   tpss_precond_autotune): 0..5 for the column-streamed kernel
                                   (6, 7: plane passes in registers, degree 4 only; other

@@ -701,7 +701,8 @@ int fd_variants(bool fp32, int dim, int k, int ncp)
 }
 
 // the column-streamed FP32 smoother applies to this preconditioner: additive 3D vertex patches
-// on a Cartesian level with k <= 4, keyed FD tables (not dense inverses, not per-patch entries)
+// with k <= 5 and FD tables (keyed, or per patch up to k = 3 on distorted levels), not dense
+// inverses or the rank-2 Kronecker solver's product-form eigenvalues
 bool stream_eligible(const tpss_precond *p)
 {
   const tpss_layout &L = *p->tables->layout;
@@ -718,7 +719,9 @@ bool use_stream(const tpss_precond *p)
   if(p->desc.kernel_variant == TPSS_KERNEL_COLOR) return false;
   const bool ok = stream_eligible(p);
   if(p->desc.kernel_variant == TPSS_KERNEL_STREAM && !ok)
-    fail(TPSS_ERR_INVALID_ARGUMENT, "the streamed kernel needs additive 3D vertex patches, FP32, k <= 4");
+    fail(TPSS_ERR_INVALID_ARGUMENT,
+         "the streamed kernel needs additive 3D vertex patches, FP32, k <= 5 and fast-diagonalization "
+         "local solvers (per-patch 1-D problems: k <= 3)");
   return ok;
 }
 
