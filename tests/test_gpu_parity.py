@@ -351,6 +351,26 @@ def test_mg_cg_iterations_match_oracle(tpss, oracle, xcheck, cuda):
         assert it32 <= c["iterations"] + 2, (c, it32)
 
 
+@pytest.mark.parametrize("dim,k,n,prec", [(2, 3, 16, 0), (3, 2, 8, 1)])
+def test_device_cg_loop_equals_host_loop(tpss, cuda, dim, k, n, prec):
+    """The device-side CG loop (one graph, a conditional WHILE node around one iteration) runs
+    the host loop's kernels in the same order: same iteration count, residual history and
+    solution; both stop at max_iter with TPSSNotConverged."""
+    import torch
+    res = []
+    for use_graph in (True, False):
+        mg = tpss.MultigridSolver(dim, k, 1, n, precision=prec, coarse_solver=1, use_graph=use_graph)
+        f = torch.tensor(philox(91, mg.n_dofs()), dtype=torch.float64, device=cuda)
+        u = torch.zeros_like(f)
+        it, hist = mg.solve(u, f)
+        res.append((it, hist, u.cpu().numpy()))
+        with pytest.raises(tpss.TPSSNotConverged):
+            mg.solve(torch.zeros_like(f), f, max_iter=3)
+    assert res[0][0] == res[1][0] > 3
+    assert np.array_equal(res[0][1], res[1][1])
+    assert np.array_equal(res[0][2], res[1][2])
+
+
 def test_mg_solution_matches_oracle(tpss, oracle, xcheck, cuda):
     import torch
     dim, k, nrep, ncf = 2, 4, 2, 16

@@ -621,7 +621,7 @@ extern "C" int tpss_mg_create(const tpss_mg_desc *d, tpss_mg **out)
     if(device_loop(mg.get()))
     {
       TPSS_CUDA(cudaMemset(mg->r.ptr, 0, sizeof(double) * mg->r.n));
-      prepare_loop(mg.get(), 255);
+      prepare_loop(mg.get(), 1023);
     }
     *out = mg.release();
   });
@@ -769,7 +769,7 @@ bool device_loop(const tpss_mg *mg) { return mg->desc.use_graph && mg->desc.coar
 // ensure the loop graph for max_iter iterations (the residual history holds max_iter + 1)
 void prepare_loop(tpss_mg *mg, int max_iter)
 {
-  const size_t cap = std::max<size_t>(256, (size_t)max_iter + 1);
+  const size_t cap = std::max<size_t>(1024, (size_t)max_iter + 1);
   if(!mg->g_loop || mg->hist.n < (size_t)max_iter + 1) capture_loop(mg, (int)cap);
 }
 
