@@ -77,13 +77,14 @@ def parse():
                          "all-FP32 and all-FP64: iterations and seconds, one JSON line")
     ap.add_argument("--no-dgq3-2d", action="store_true",
                     help="skip the 2D SIPG DGQ3 64^2 section (both penalty modes)")
-    ap.add_argument("--profile-case", choices=["mapped", "perpatch", "cg2d", "cg2d_eager", "cg3dk5_eager", "c0ip",
-                                               "mlp", "host"],
+    ap.add_argument("--profile-case", choices=["mapped", "perpatch", "k5", "cg2d", "cg2d_eager", "cg3dk5_eager",
+                                               "c0ip", "mlp", "host"],
                     help="run one small workload of a secondary kernel three times and exit (the "
                          "commands the ncu profiles capture): mapped = mapped SIPG operator on a "
                          "distorted 3D DGQ3 24^3 level; perpatch = FP32 smoother on per-patch 1-D "
                          "problems (distorted 3D DGQ3 56^3, surrogate widths), streamed decomposition 4 "
-                         "and the per-color kernel; cg2d = CG + V-cycle on 2D SIPG DGQ3 64^2 (2 root "
+                         "and the per-color kernel; k5 = FP32 smoother on 3D DGQ5 40^3 (Cartesian), "
+                         "streamed decomposition 2 and the per-color kernel; cg2d = CG + V-cycle on 2D SIPG DGQ3 64^2 (2 root "
                          "cells, damping 0.25, dense coarse solve), one solve after a warm-up solve (cg2d_eager: the same "
                          "without CUDA graphs, every kernel launched from the host); cg3dk5_eager = the "
                          "same for 3D SIPG DGQ5 32^3 with FP32 smoothers (the batch's largest problems); c0ip = C0IP FE_Q(3) 512^2 operator and "
@@ -945,6 +946,28 @@ def profile_case(args):
             p = tpss.SchwarzPreconditioner()
             p.initialize(sh, None, tpss.SchwarzPreconditioner.AdditionalData(
                 relaxation=0.15, precision=tpss.Precision.fp32, kernel_variant=kv, stream_variant=4))
+            for _ in range(3):
+                p.vmult(y, x)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(10):
+                p.vmult(y, x)
+            e1.record()
+            torch.cuda.synchronize()
+            ms[label] = e0.elapsed_time(e1) / 10
+            del p
+        print(json.dumps({"profile_case": name, "n_dofs": sh.n_dofs(), "ms_per_vmult": ms}))
+    elif name == "k5":
+        # degree-5 streamed smoother (4 x 2 vertex columns) against the per-color kernel (src and
+        # dst 110 MB each: together larger than L2)
+        sh = tpss.SubdomainHandler(tpss.SubdomainHandler.AdditionalData(dim=3, degree=5, n_cells=(40,) * 3))
+        x = torch.rand(sh.n_dofs(), dtype=torch.float64, device="cuda")
+        y = torch.empty_like(x)
+        ms = {}
+        for label, kv in (("streamed_variant2", 2), ("per_color", 1)):
+            p = tpss.SchwarzPreconditioner()
+            p.initialize(sh, None, tpss.SchwarzPreconditioner.AdditionalData(
+                relaxation=0.15, precision=tpss.Precision.fp32, kernel_variant=kv, stream_variant=2))
             for _ in range(3):
                 p.vmult(y, x)
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
