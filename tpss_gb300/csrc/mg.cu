@@ -13,7 +13,9 @@
 // (stop at ||r|| <= max(abs_tol, rel_tol ||r_0||)).
 // The V-cycle can be captured in CUDA graphs: with the dense coarse solver the whole cycle is
 // one graph launch; with the CG coarse solver the down- and up-sweeps are two graphs around
-// the host-driven coarse iteration.
+// the host-driven coarse iteration. With the dense coarse solver the outer CG loop is a graph
+// too: a conditional WHILE node whose body holds one iteration and a one-thread kernel that
+// tests the residual and sets the loop condition (single solves and batches).
 #include <algorithm>
 #include <cmath>
 #include <cstring>
