@@ -176,3 +176,13 @@ def test_ctypes_descriptors_match_the_c_structs(tpss):
                 m = re.search(r"(\w+)\s*(\[\d+\])?\s*$", part.strip())
                 names.append(m.group(1))
         assert [f[0] for f in getattr(_lib, pyname)._fields_] == names, cname
+
+
+def test_build_compiles_every_cuda_source():
+    """Every translation unit under tpss_gb300/csrc is in the build's unit list (a kernel file
+    left out would leave its entry points unresolved in the library)."""
+    from tpss_gb300 import build
+    csrc = os.path.join(ROOT, "tpss_gb300", "csrc")
+    sources = sorted(f for f in os.listdir(csrc) if f.endswith(".cu"))
+    units = sorted({u[0] for u in build.UNITS})
+    assert units == sources
