@@ -799,7 +799,7 @@ def batch_section(tpss, args):
     from the seed; a draw beyond the per-problem or the total DoF cap is rejected and drawn again;
     one root cell, dense coarse solve, V-cycles in CUDA graphs, kernel decompositions chosen by the
     autotuner per level shape, FP32 smoothers, FP64 CG) solved as one batch (every problem's
-    device-side CG loop launched once on one of 16 streams), against solving them one after the
+    device-side CG loop launched once on one of 64 streams), against solving them one after the
     other with the single-problem solver (the same device loops, one synchronization each)."""
     import numpy as np
     import torch
@@ -808,7 +808,7 @@ def batch_section(tpss, args):
     for pr in problems:
         pr["precision"] = tpss.Precision.fp32
     t0 = time.perf_counter()
-    b = tpss.BatchSolver(problems, n_streams=16)
+    b = tpss.BatchSolver(problems, n_streams=64)
     fs = [torch.tensor(philox_src(n, args.seed + i), dtype=torch.float64, device="cuda")
           for i, n in enumerate(b.n_dofs)]
     us = [torch.empty_like(f) for f in fs]
