@@ -432,7 +432,7 @@ private:
 class BatchSolver
 {
 public:
-  BatchSolver(const std::vector<tpss_mg_desc> &problems, int n_streams = 8)
+  BatchSolver(const std::vector<tpss_mg_desc> &problems, int n_streams = 64)
   {
     check(tpss_batch_create(problems.data(), (int)problems.size(), n_streams, &handle_));
     n_ = (int)problems.size();

@@ -489,7 +489,7 @@ class BatchSolver:
     problem's device-side CG loop (one CUDA graph) launched once on one of n_streams streams,
     one host synchronization for the whole batch."""
 
-    def __init__(self, problems, n_streams=8):
+    def __init__(self, problems, n_streams=64):
         """problems: list of dicts with MultigridSolver keyword arguments (dim, degree, n_rep,
         n_cells_fine, relaxation, precision, coarse_solver, use_graph, ...)."""
         arr = (_lib.MgDesc * len(problems))()
