@@ -186,3 +186,18 @@ def test_build_compiles_every_cuda_source():
     sources = sorted(f for f in os.listdir(csrc) if f.endswith(".cu"))
     units = sorted({u[0] for u in build.UNITS})
     assert units == sources
+
+
+def test_batch_draw_is_seeded_and_respects_the_caps(tpss):
+    """The 512-problem family's draw: deterministic per seed, every problem within the
+    per-problem cap, the sum within the total budget, degrees and sizes from the stated sets."""
+    a, ra = tpss.draw_batch_problems(512, 4, 96_000_000, 8_000_000)
+    b, rb = tpss.draw_batch_problems(512, 4, 96_000_000, 8_000_000)
+    assert a == b and ra == rb and len(a) == 512
+    sizes = [(p["n_cells_fine"] * (p["degree"] + 1)) ** p["dim"] for p in a]
+    assert max(sizes) <= 8_000_000 and sum(sizes) <= 96_000_000
+    assert all(p["dim"] in (2, 3) and 2 <= p["degree"] <= 7 and p["n_cells_fine"] in (8, 16, 32, 64) for p in a)
+    c, _ = tpss.draw_batch_problems(512, 5, 96_000_000, 8_000_000)
+    assert c != a
+    with pytest.raises(ValueError):
+        tpss.draw_batch_problems(512, 4, 1000, 8_000_000)
